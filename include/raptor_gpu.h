@@ -1,0 +1,167 @@
+/* raptor_gpu.h - C ABI of the GB300 (sm_103a) engine for RAPTOR's per-pixel
+ * imaging hot path.
+ *
+ * The engine replaces the body of the reference's calculate_image
+ * (core.c:74-152, declared at functions.h:70): for every camera pixel it
+ * traces the null geodesic backward through Kerr spacetime in MKS
+ * coordinates (integrator.c:149-289, metric.c:94-137,207-231,538-638),
+ * samples the HARM primitives (raptor_harm_model.c:190-320, grmhd.c:35-71)
+ * and accumulates thermal-synchrotron transfer (radiative_transfer.c:49-119,
+ * j_nu.c:130-153,188-200).  Everything outside that loop - read_model,
+ * init_harm_data, set_units, set_constants, output_files - stays in the
+ * caller, with its model.in and file formats unchanged.
+ *
+ * Plain C types only.  The caller owns every host buffer; device memory
+ * belongs to the context and never crosses this interface.  Every call
+ * blocks until its results are on the host, returns RAPTOR_OK (0) or a
+ * negative status, and never exits the process (unlike core.c:15 or
+ * raptor_harm_model.c:84).  One context per host thread.
+ */
+#ifndef RAPTOR_GPU_H
+#define RAPTOR_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAPTOR_GPU_ABI_VERSION 1
+#define RAPTOR_MAX_FREQS 8  /* frequencies per image in one render */
+#define RAPTOR_MAX_GRIDS 16 /* dumps resident in one context */
+
+/* status codes */
+#define RAPTOR_OK 0
+#define RAPTOR_ERR_INVALID (-1)  /* bad argument (sizes, ids, non-finite input) */
+#define RAPTOR_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define RAPTOR_ERR_DEVICE (-3)   /* the kernels flagged an error (see last_error) */
+#define RAPTOR_ERR_NOMEM (-4)    /* device or pinned allocation failed */
+#define RAPTOR_ERR_NODEVICE (-5) /* no usable sm_103 device */
+
+/* arithmetic forms */
+#define RAPTOR_PREC_FP64 0  /* everything FP64, the reference's arithmetic */
+#define RAPTOR_PREC_MIXED 1 /* FP64 geodesic + metric, FP32 fluid/emission/transfer */
+
+/* integrators (parameters.h:186-189) */
+#define RAPTOR_RK4 4
+#define RAPTOR_RK2 2
+
+typedef struct raptor_gpu_options {
+    int device;          /* CUDA device ordinal */
+    int block_size;      /* threads per block of the ray kernel; 0 = default/tuned */
+    int blocks_per_sm;   /* resident blocks per SM of the persistent grid; 0 = default/tuned */
+    int refill_interval; /* geodesic steps between lane refills ("steps per chunk"); 0 = 1 */
+    int autotune;        /* 1: tune block size / refill interval on a ray sample once per
+                            (device, batch signature) and reuse the result */
+    int use_graph;       /* 1: replay a render through a captured CUDA graph when the batch
+                            signature repeats */
+    int reserved[8];
+} raptor_gpu_options;
+
+/* Grid geometry: the HARM header fields the hot path uses
+ * (raptor_harm_model.c:90-115).  stopx = startx + n*dx is derived inside,
+ * as raptor_harm_model.c:127-128 does. */
+typedef struct raptor_grid_geom {
+    int n1, n2;
+    double startx1, startx2;
+    double dx1, dx2;
+    double a;      /* black-hole spin */
+    double hslope; /* MKS theta compression */
+    double R0;     /* MKS radial offset */
+} raptor_grid_geom;
+
+/* One image: the model.in + argv values that calculate_image reads through
+ * globals (core.c:22-42, parameters.h). */
+typedef struct raptor_image_desc {
+    int width, height;            /* IMG_WIDTH, IMG_HEIGHT */
+    double cam_size_x, cam_size_y; /* CAM_SIZE_X/Y, in Rg */
+    double inclination;           /* INCLINATION, degrees */
+    double mbh;                   /* MBH, g */
+    double m_unit;                /* M_UNIT, g */
+    double r_high, r_low;         /* R_HIGH, R_LOW (R-beta electron temperature) */
+    double stepsize;              /* STEPSIZE */
+    int integrator;               /* RAPTOR_RK4 or RAPTOR_RK2 */
+    int grid;                     /* id from raptor_gpu_upload_grid */
+    int n_freq;                   /* 1..RAPTOR_MAX_FREQS */
+    double freq[RAPTOR_MAX_FREQS]; /* Hz */
+} raptor_image_desc;
+
+typedef struct raptor_gpu_stats {
+    double kernel_ms;  /* ray kernel, CUDA events on the context stream */
+    double device_ms;  /* all device work of the render (reset, ray kernel, spectrum), same events */
+    double total_ms;   /* whole call, host wall time */
+    double h2d_bytes, d2h_bytes;
+    long long rays;
+    long long steps;      /* geodesic (RK) steps */
+    long long rt_calls;   /* steps inside the grid (radiative_transfer calls) */
+    long long rt_samples; /* calls that passed the sigma cut (emission evaluated) */
+    long long max_ray_steps;
+    long long n_stepcap;  /* rays stopped by max_steps (parameters.h:182) */
+    long long n_nonfinite;
+    double kk_max;        /* max |g k k| / (k^t)^2 over rays at termination */
+    int block_size, blocks_per_sm, refill_interval, grid_blocks;
+    int graph_replayed;
+} raptor_gpu_stats;
+
+/* Gradients of a scalar loss L(I) of the output image, given dL/dI. */
+typedef struct raptor_grad {
+    double d_m_unit;      /* dL/dM_UNIT */
+    double d_r_high;      /* dL/dR_HIGH */
+    double d_r_low;       /* dL/dR_LOW  (dL/d(T_p/T_e) = d_r_high + d_r_low when equal) */
+    double d_inclination; /* dL/dINCLINATION, per degree */
+    double *d_rho;        /* [n1*n2] dL/d rho per cell (caller-allocated, may be NULL) */
+    double *d_u;          /* [n1*n2] dL/d u per cell (caller-allocated, may be NULL) */
+} raptor_grad;
+
+typedef struct raptor_gpu_ctx raptor_gpu_ctx;
+
+/* Create a context on options->device (NULL: defaults).  Replaces the
+ * OpenACC data region set-up of core.c:78. */
+int raptor_gpu_init(const raptor_gpu_options *options, raptor_gpu_ctx **out);
+void raptor_gpu_destroy(raptor_gpu_ctx *ctx);
+/* Text of the last error on this context ("" if none). */
+const char *raptor_gpu_last_error(const raptor_gpu_ctx *ctx);
+
+/* Upload a dump's eight primitives, float64 [8][n1][n2] in HARM order
+ * (rho, u, U1, U2, U3, B1, B2, B3) - the contiguous form of the
+ * reference's p[NPRIM][N1][N2][1] (grmhd.c:76-91, copied in at core.c:78).
+ * Returns the grid id in *grid_id.  Re-uploading to an existing id
+ * (*grid_id >= 0 on entry and geometry unchanged) reuses its memory. */
+int raptor_gpu_upload_grid(raptor_gpu_ctx *ctx, const double *prims, const raptor_grid_geom *geom,
+                           int *grid_id);
+
+/* Render n_imgs images in one persistent launch (core.c:97-142 for each).
+ * I_out: concatenation over images of intensityfield[W*H][n_freq]
+ * (pixel x + y*W, frequency fastest), already multiplied by nu^3 as
+ * core.c:136 does.  spectrum_out: [sum over images of n_freq], the plain
+ * pixel sum of core.c:146-150 (the caller applies JANSKY_FACTOR when
+ * writing, core.c:177,192,195).  Either output may be NULL. */
+int raptor_gpu_render(raptor_gpu_ctx *ctx, const raptor_image_desc *imgs, int n_imgs, int precision,
+                      double *I_out, double *spectrum_out);
+
+/* Same, restricted to the global ray range [ray_begin, ray_begin+ray_count)
+ * of the batch (rays numbered image by image, pixel x + y*W within one).
+ * Pixels outside the range are written as 0 and left out of the spectrum.
+ * Lets a caller split one batch across processes or devices. */
+int raptor_gpu_render_range(raptor_gpu_ctx *ctx, const raptor_image_desc *imgs, int n_imgs,
+                            int precision, long long ray_begin, long long ray_count,
+                            double *I_out, double *spectrum_out);
+
+/* Number of doubles raptor_gpu_render writes to I_out / spectrum_out. */
+long long raptor_gpu_output_size(const raptor_image_desc *imgs, int n_imgs);
+long long raptor_gpu_spectrum_size(const raptor_image_desc *imgs, int n_imgs);
+
+/* Statistics of the last render or VJP on this context. */
+int raptor_gpu_get_stats(const raptor_gpu_ctx *ctx, raptor_gpu_stats *out);
+
+/* Vector-Jacobian product of one image: given dL_dI [W*H][n_freq] (same
+ * layout and nu^3 scaling as I_out), returns dL/d(M_UNIT, R_HIGH, R_LOW,
+ * INCLINATION) and, if the pointers are set, dL/d rho and dL/d u on the
+ * image's grid.  I_out receives the forward image (may be NULL). */
+int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
+                   const double *dL_dI, double *I_out, raptor_grad *grad);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,80 @@
+// Internal state shared by the engine's translation units (not part of the
+// C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "image_desc.cuh"
+#include "raptor_gpu.h"
+
+struct LaunchShape {
+    int block = 128;   // threads per block
+    int bps = 1;       // resident blocks per SM
+    int grid = 0;      // blocks in the persistent grid
+    int refill = 1;    // steps between lane refills
+};
+
+using RayLaunchFn = void (*)(const LaunchShape&, cudaStream_t, const raptor::DevImage*, int, long long, long long,
+                             unsigned long long*, double*);
+
+struct GridSlot {
+    bool used = false;
+    raptor_grid_geom geom{};
+    double* c64 = nullptr;
+    float* c32 = nullptr;
+    double* staging = nullptr;
+};
+
+struct Batch {
+    int n = 0;
+    long long total_rays = 0, out_len = 0;
+    int spec_len = 0, max_nf = 1;
+    size_t h2d_bytes = 0;
+    std::vector<raptor::DevImage> host;
+    std::vector<int> spec_img, spec_f;
+};
+
+struct raptor_gpu_ctx {
+    raptor_gpu_options opt{};
+    int device = 0;
+    int num_sms = 0;
+    char device_name[256] = {0};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evA = nullptr, evB = nullptr;  // ray kernel / whole render
+    GridSlot grids[RAPTOR_MAX_GRIDS];
+    raptor::DevImage* d_imgs = nullptr;
+    size_t imgs_cap = 0;
+    raptor::DevImage* h_imgs = nullptr;
+    size_t h_imgs_cap = 0;
+    double* d_out = nullptr;
+    size_t out_cap = 0;
+    double* d_spec = nullptr;
+    size_t spec_cap = 0;
+    int* d_spec_map = nullptr;
+    size_t spec_map_cap = 0;
+    unsigned long long* d_counters = nullptr;
+    int* d_flag = nullptr;
+    double* d_grad = nullptr;
+    size_t grad_cap = 0;
+    double* d_dldi = nullptr;
+    size_t dldi_cap = 0;
+    Batch batch;
+    raptor_gpu_stats stats{};
+    double last_upload_ms = 0.0;
+    std::map<std::string, LaunchShape> tuned;  // autotuner cache, keyed by batch signature
+    char err[512] = {0};
+};
+
+int ctx_fail(raptor_gpu_ctx* ctx, int code, const char* fmt, ...);
+int ensure_buffer(raptor_gpu_ctx* ctx, void** ptr, size_t* cap, size_t bytes);
+int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, raptor::DevImage& im);
+int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs, Batch& b);
+RayLaunchFn pick_ray_kernel(int nf, bool mixed, const void** fn);
+LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn);
+LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, RayLaunchFn fn, const void* fnp);
+int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, long long rb, long long re,
+                   const LaunchShape& ls, RayLaunchFn fn, bool timed);
+int collect_stats(raptor_gpu_ctx* ctx, bool timed);

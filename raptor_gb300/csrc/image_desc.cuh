@@ -1,0 +1,52 @@
+// Per-image constants as the ray kernels see them.  Built on the host in
+// FP64 from a raptor_image_desc and its grid (camera set-up of
+// metric.c:650-727 and BL_to_KS_u GRmath.c:135-184 that is common to all
+// pixels, set_units grmhd.c:17-33, set_constants utilities.c:17-26).
+#pragma once
+#include "kerr_mks.cuh"
+
+namespace raptor {
+
+constexpr int kMaxFreqs = 8;
+constexpr double kRcam = 1.e4;                 // parameters.h:163
+constexpr double kCutoffOuter = kRcam * 1.01;  // parameters.h:184
+constexpr int kMaxOrder = 100;                 // parameters.h:170
+constexpr double kMaxSteps = 1e5;              // parameters.h:182
+
+// cgs constants, constants.h:16-29 and j_nu.c:15
+constexpr double kECharge = 4.8032068e-10;
+constexpr double kEMass = 9.1093826e-28;
+constexpr double kPMass = 1.67262171e-24;
+constexpr double kBoltz = 1.3806505e-16;
+constexpr double kC = 2.99792458e10;
+constexpr double kPlanck = 6.6260693e-27;
+constexpr double kGGrav = 6.6742e-8;
+constexpr double kE2C = 7.695589048e-30;
+constexpr double kE2CH = 1.161410e-03;
+
+struct DevImage {
+    long long ray_begin;   // first global ray of this image
+    long long out_offset;  // first double of this image in the output
+    int width, height, nfreq, integrator;
+    // grid: cells [n1][n2][8], primitives interleaved per cell
+    const double* cells64;
+    const float* cells32;
+    int n1, n2;
+    double startx1, startx2, stopx1, stopx2, idx1, idx2;
+    Geo geo;
+    // camera (integrator.c:188-191, metric.c:652-692)
+    double stepx, stepy, half_x, half_y;
+    double sin_mu, mu0sq, cc_over_sc, cosc2;
+    double g11, gu00, gu03, gu33, gu22;  // BL metric at the camera
+    double t01, t31;                     // BL -> KS transform at the camera
+    double k2fac;                        // d theta / d x2 at the camera's x2
+    double xcam[4];                      // MKS camera position
+    // model
+    double stepsize, inv_stepsize, cutoff_inner;
+    double Ne_unit, B_unit, inv_B_unit, r_high, r_low;
+    double freq[kMaxFreqs];
+    double nu3[kMaxFreqs];        // freq^3 (core.c:136)
+    double rg_over_nu[kMaxFreqs]; // R_g / freq (radiative_transfer.c:88)
+};
+
+}  // namespace raptor

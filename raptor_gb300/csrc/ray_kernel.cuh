@@ -1,0 +1,303 @@
+// Persistent ray kernel: the per-pixel loop of calculate_image
+// (core.c:107-114) and integrate_geodesic (integrator.c:149-289) for every
+// pixel of every image in a batch.
+//
+// Launch shape: one grid of (SM count x resident blocks) that stays
+// resident.  Each lane owns one ray; when a lane's ray terminates it takes
+// the next ray index from a device-wide counter (warp-aggregated atomicAdd,
+// one per warp per refill) so horizon-captured rays (~200 steps) and
+// photon-ring rays (thousands) share the SMs without tail imbalance.  Rays
+// are numbered image by image, pixel x + y*W within an image, so a warp's
+// lanes start on neighbouring pixels.  There are no spin-waits: the only
+// inter-thread communication is the atomic counter, so every launch ends.
+#pragma once
+#include "transfer.cuh"
+
+namespace raptor {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Stats slots in the counters buffer (counters[0] is the ray queue).
+enum : int {
+    kCtrQueue = 0,
+    kCtrSteps = 1,
+    kCtrRtCalls = 2,
+    kCtrRtSamples = 3,
+    kCtrRays = 4,
+    kCtrStepCap = 5,
+    kCtrNonFinite = 6,
+    kCtrMaxSteps = 7,
+    kCtrKkMax = 8,  // bits of a non-negative double, atomicMax as integer
+    kCtrCount = 16
+};
+
+__device__ __forceinline__ int find_image(const DevImage* __restrict__ imgs, int n_imgs, long long ray) {
+    int lo = 0, hi = n_imgs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&imgs[mid].ray_begin) <= ray) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Initial photon (metric.c:650-727, GRmath.c:135-184, newtonraphson.c:76-97);
+// the pixel-independent part lives in DevImage.
+__device__ __forceinline__ void init_photon(const DevImage& im, int x, int yy, double y[8], double& beta) {
+    const double alpha = -im.half_x + (x + 0.5) * im.stepx;
+    beta = -im.half_y + (yy + 0.5) * im.stepy;
+    const double ll = -alpha * im.sin_mu;
+    const double qq = beta * beta + im.mu0sq * (alpha * alpha - 1.0);
+    const double sg = (beta < 0.0) ? -1.0 : ((beta > 0.0) ? 1.0 : 0.0);
+    const double kd2 = sg * sqrt(fabs(qq - ll * ll * im.cc_over_sc + im.cosc2));
+    const double kd0 = -1.0, kd3 = ll;
+    const double ku0 = im.gu00 * kd0 + im.gu03 * kd3;
+    const double ku3 = im.gu33 * kd3 + im.gu03 * kd0;
+    const double ku2 = im.gu22 * kd2;
+    const double ku1 = sqrt((-ku0 * kd0 - ku2 * kd2 - ku3 * kd3) / im.g11);
+    y[0] = im.xcam[0];
+    y[1] = im.xcam[1];
+    y[2] = im.xcam[2];
+    y[3] = im.xcam[3];
+    y[4] = ku0 + im.t01 * ku1;
+    y[5] = ku1;
+    y[6] = ku2 / im.k2fac;
+    y[7] = im.t31 * ku1 + ku3;
+}
+
+// stepsize (integrator.c:109-122) with the reciprocals folded:
+// 1/(eps/|k|) = |k|/eps; the tiny^2 guards keep the reference's limits.
+__device__ __forceinline__ double step_size(const DevImage& im, const double y[8]) {
+    const double t = 1.e-40;
+    const double m2 = fmin(y[2], 1.0 - y[2]);
+    const double i1 = (fabs(y[5]) + t) * im.inv_stepsize;
+    const double i2 = (fabs(y[6]) + t) * im.inv_stepsize / m2;
+    const double i3 = (fabs(y[7]) + t) * im.inv_stepsize;
+    return -fmax(1.0 / (i1 + i2 + i3), 1e-12);
+}
+
+__device__ __forceinline__ void rhs(const MksPoint& p, const Geo& g, const double ys[8], double f[8]) {
+    f[0] = ys[4];
+    f[1] = ys[5];
+    f[2] = ys[6];
+    f[3] = ys[7];
+    geodesic_accel(p, g, ys + 4, f + 4);
+}
+
+// One RK4 step (integrator.c:13-41): stage weights 1/2, 1/2, 1 and
+// y += (k1 + 2 k2 + 2 k3 + k4)/6 summed in the reference's order.
+// p holds the point at y on entry and at the new y on exit.
+__device__ __forceinline__ void rk4_step(const Geo& g, double y[8], MksPoint& p, double dt) {
+    double acc[8], ys[8], f[8];
+    rhs(p, g, y, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const double d = dt * f[i];
+        acc[i] = d;
+        ys[i] = y[i] + d * 0.5;
+    }
+    MksPoint q;
+    mks_point(ys[1], ys[2], g, q);
+    rhs(q, g, ys, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const double d = dt * f[i];
+        acc[i] = acc[i] + d * 2.0;
+        ys[i] = y[i] + d * 0.5;
+    }
+    mks_point(ys[1], ys[2], g, q);
+    rhs(q, g, ys, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const double d = dt * f[i];
+        acc[i] = acc[i] + d * 2.0;
+        ys[i] = y[i] + d;
+    }
+    mks_point(ys[1], ys[2], g, q);
+    rhs(q, g, ys, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        acc[i] = acc[i] + dt * f[i];
+        y[i] = y[i] + 1.0 / 6.0 * acc[i];
+    }
+    mks_point(y[1], y[2], g, p);
+}
+
+// RK2 midpoint step (integrator.c:44-70).
+__device__ __forceinline__ void rk2_step(const Geo& g, double y[8], MksPoint& p, double dt) {
+    double ys[8], f[8];
+    rhs(p, g, y, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) ys[i] = y[i] + dt * f[i] * 0.5;
+    MksPoint q;
+    mks_point(ys[1], ys[2], g, q);
+    rhs(q, g, ys, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) y[i] = y[i] + dt * f[i];
+    mks_point(y[1], y[2], g, p);
+}
+
+__device__ __forceinline__ double null_drift(const MksPoint& p, const Geo& g, const double y[8]) {
+    MetricDD d;
+    MetricUU u;
+    mks_metric(p, g, d, u);
+    const double k0 = y[4], k1 = y[5], k2 = y[6], k3 = y[7];
+    const double kk = d.g00 * k0 * k0 + d.g11 * k1 * k1 + d.g22 * k2 * k2 + d.g33 * k3 * k3 +
+                      2.0 * (d.g01 * k0 * k1 + d.g03 * k0 * k3 + d.g13 * k1 * k3);
+    return fabs(kk) / (k0 * k0);
+}
+
+template <int NF, bool MIXED>
+struct RayState {
+    double y[8];
+    MksPoint p;
+    double beta, thdot_prev;
+    int steps, turns, stop, img, pix;
+    double tau[NF], I[NF];  // FP64 form
+    float tf[NF], tc[NF], If[NF], Ic[NF];  // FP32 form (tau, tau compensation, I, I compensation)
+};
+
+template <int NF, bool MIXED>
+__global__ void __launch_bounds__(256)
+    ray_kernel(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
+               unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval) {
+    const int lane = threadIdx.x & 31;
+    RayState<NF, MIXED> s;
+    bool active = false, live = true;
+    const DevImage* im = imgs;
+    unsigned long long n_steps = 0, n_rt_calls = 0, n_rt_samples = 0, n_rays = 0, n_cap = 0, n_nan = 0;
+    unsigned long long max_steps = 0;
+    double kk_max = 0.0;
+
+    while (true) {
+        // refill idle lanes from the device-wide ray queue
+        const unsigned need = __ballot_sync(kFull, !active && live);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (!active && live) {
+                const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
+                if (rid < ray_end) {
+                    s.img = find_image(imgs, n_imgs, rid);
+                    im = imgs + s.img;
+                    s.pix = (int)(rid - im->ray_begin);
+                    const int px = s.pix % im->width, py = s.pix / im->width;
+                    init_photon(*im, px, py, s.y, s.beta);
+                    mks_point(s.y[1], s.y[2], im->geo, s.p);
+                    s.steps = 0;
+                    s.turns = 0;
+                    s.stop = 0;
+                    s.thdot_prev = 0.0;
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        s.tau[f] = 0.0; s.I[f] = 0.0;
+                        s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
+                    }
+                    active = true;
+                } else {
+                    live = false;
+                }
+            }
+        }
+        if (!__any_sync(kFull, active)) break;
+        if (active) {
+            for (int it = 0; it < refill_interval; ++it) {
+                // while-condition of integrator.c:228-229 (r = exp(x1), no R0)
+                const double r = s.p.rp;
+                bool done = !(r < kCutoffOuter && r > im->cutoff_inner && (double)s.steps < kMaxSteps &&
+                              !s.stop);
+                if (!done) {
+                    // theta turning points limit the lensed-image order (integrator.c:243-247)
+                    if (s.thdot_prev * s.y[6] < 0.0 && s.steps > 2) s.turns += 1;
+                    s.thdot_prev = s.y[6];
+                    if ((s.beta < 0.0 && s.turns > kMaxOrder) || (s.beta > 0.0 && s.turns > kMaxOrder + 1))
+                        s.stop = 1;
+                    const double dl = step_size(*im, s.y);
+                    if (im->integrator == 2) rk2_step(im->geo, s.y, s.p, dl);
+                    else rk4_step(im->geo, s.y, s.p, dl);
+                    s.steps += 1;
+                    if (s.y[1] > im->stopx1 && s.y[5] < 0.0) {
+                        done = true;  // escaped outward (integrator.c:271-272)
+                    } else if (s.y[1] < im->stopx1 && s.y[1] > im->startx1 && s.y[2] > im->startx2 &&
+                               s.y[2] < im->stopx2) {
+                        ++n_rt_calls;
+                        bool sampled;
+                        if constexpr (MIXED) sampled = rt_sample_fp32<NF>(*im, s.y, s.p, fabs(dl), s.tf, s.tc, s.If, s.Ic);
+                        else sampled = rt_sample_fp64<NF>(*im, s.y, s.p, fabs(dl), s.tau, s.I);
+                        n_rt_samples += sampled ? 1 : 0;
+                    }
+                }
+                if (done) {
+                    // write intensityfield[pix][f] * nu^3 (core.c:136)
+                    double* o = out + im->out_offset + (long long)s.pix * im->nfreq;
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        if (f >= im->nfreq) break;
+                        double v;
+                        if constexpr (MIXED) v = ((double)s.If[f] + (double)s.Ic[f]) * kE2C;
+                        else v = s.I[f];
+                        o[f] = v * im->nu3[f];
+                    }
+                    n_steps += (unsigned long long)s.steps;
+                    n_rays += 1;
+                    if ((double)s.steps >= kMaxSteps) ++n_cap;
+                    if (!(s.p.rp == s.p.rp) || !isfinite(s.y[5])) ++n_nan;
+                    max_steps = max(max_steps, (unsigned long long)s.steps);
+                    const double kk = null_drift(s.p, im->geo, s.y);
+                    if (kk == kk) kk_max = fmax(kk_max, kk);
+                    active = false;
+                    break;
+                }
+            }
+        }
+    }
+    // fold per-lane statistics: warp shuffle, then one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_steps += __shfl_xor_sync(kFull, n_steps, o);
+        n_rt_calls += __shfl_xor_sync(kFull, n_rt_calls, o);
+        n_rt_samples += __shfl_xor_sync(kFull, n_rt_samples, o);
+        n_rays += __shfl_xor_sync(kFull, n_rays, o);
+        n_cap += __shfl_xor_sync(kFull, n_cap, o);
+        n_nan += __shfl_xor_sync(kFull, n_nan, o);
+        max_steps = max(max_steps, __shfl_xor_sync(kFull, max_steps, o));
+        kk_max = fmax(kk_max, __shfl_xor_sync(kFull, kk_max, o));
+    }
+    if (lane == 0) {
+        atomicAdd(&counters[kCtrSteps], n_steps);
+        atomicAdd(&counters[kCtrRtCalls], n_rt_calls);
+        atomicAdd(&counters[kCtrRtSamples], n_rt_samples);
+        atomicAdd(&counters[kCtrRays], n_rays);
+        atomicAdd(&counters[kCtrStepCap], n_cap);
+        atomicAdd(&counters[kCtrNonFinite], n_nan);
+        atomicMax(&counters[kCtrMaxSteps], max_steps);
+        atomicMax(&counters[kCtrKkMax], (unsigned long long)__double_as_longlong(kk_max));
+    }
+}
+
+// Spectrum: core.c:146-150 sums intensityfield over pixels per frequency.
+// One block per (image, frequency) in a fixed-order tree, so the result is
+// deterministic.  spec_img[s], spec_f[s] map spectrum slot s to its source.
+__global__ void spectrum_kernel(const DevImage* __restrict__ imgs, const int* __restrict__ spec_img,
+                                const int* __restrict__ spec_f, const double* __restrict__ out,
+                                double* __restrict__ spectrum) {
+    __shared__ double red[256];
+    const int sidx = blockIdx.x;
+    const DevImage& im = imgs[spec_img[sidx]];
+    const int f = spec_f[sidx];
+    const long long npix = (long long)im.width * im.height;
+    const double* o = out + im.out_offset + f;
+    double acc = 0.0;
+    for (long long k = threadIdx.x; k < npix; k += blockDim.x) acc += o[k * im.nfreq];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) spectrum[sidx] = red[0];
+}
+
+}  // namespace raptor

@@ -1,0 +1,280 @@
+// One radiative-transfer sample at the post-step position of a ray:
+// get_fluid_params (raptor_harm_model.c:190-320) with Xtoij / bilinear
+// interpolation (grmhd.c:35-71), pitch_angle and freq_in_plasma_frame
+// (radiative_transfer.c:17-47), thermal synchrotron j_nu and Kirchhoff
+// a_nu (j_nu.c:130-153, 188-200) and the tau / I update of
+// radiative_transfer.c:71-98.
+//
+// Two forms share the sampling structure:
+//  * rt_sample_fp64 - FP64 throughout, the reference's arithmetic (pow of
+//    1/2, 1/6, 1/3 written as sqrt / cbrt; a = j e2_ch / B_nu / e2_c kept
+//    literally so its edge cases match the reference's).
+//  * rt_sample_fp32 - metric in FP64, then fluid, tetrad projection,
+//    emissivity and the tau / I accumulation in FP32 with Neumaier
+//    compensated sums.  Emissivity is carried without the e2_c factor and
+//    the absorptivity as j_hat (e^x - 1) / nu^2 so every intermediate stays
+//    inside FP32's range; e2_c is applied once per ray in FP64.
+#pragma once
+#include "image_desc.cuh"
+
+namespace raptor {
+
+struct CellCoef {
+    int base;    // (i * n2 + j): first of the four cells
+    double d1, d2;
+};
+
+// Xtoij (grmhd.c:46-71): cell-centred index, truncation toward zero,
+// clamped to [0, N-2] with del = 0 / 1 at the clamps.  del is formed as
+// t - i with t = (x - startx)/dx - 1/2, the reference's
+// (x - ((i + 1/2) dx + startx))/dx regrouped.
+__device__ __forceinline__ CellCoef cell_coef(const DevImage& im, double x1, double x2) {
+    CellCoef cc;
+    const double t1 = (x1 - im.startx1) * im.idx1 - 0.5;
+    const double t2 = (x2 - im.startx2) * im.idx2 - 0.5;
+    int i = (int)t1, j = (int)t2;
+    double d1, d2;
+    if (i < 0) { i = 0; d1 = 0.0; }
+    else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = 1.0; }
+    else d1 = t1 - (double)i;
+    if (j < 0) { j = 0; d2 = 0.0; }
+    else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = 1.0; }
+    else d2 = t2 - (double)j;
+    cc.base = i * im.n2 + j;
+    cc.d1 = d1;
+    cc.d2 = d2;
+    return cc;
+}
+
+__device__ __forceinline__ void load_cell(const double* __restrict__ c, double v[8]) {
+    const double2* p = reinterpret_cast<const double2*>(c);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double2 t = __ldg(p + q);
+        v[2 * q] = t.x;
+        v[2 * q + 1] = t.y;
+    }
+}
+__device__ __forceinline__ void load_cell(const float* __restrict__ c, float v[8]) {
+    const float4* p = reinterpret_cast<const float4*>(c);
+    const float4 t0 = __ldg(p), t1 = __ldg(p + 1);
+    v[0] = t0.x; v[1] = t0.y; v[2] = t0.z; v[3] = t0.w;
+    v[4] = t1.x; v[5] = t1.y; v[6] = t1.z; v[7] = t1.w;
+}
+
+// Bilinear interpolation of all eight primitives, coefficient order of
+// raptor_harm_model.c:213-216 and term order of grmhd.c:38-41.
+template <class T>
+__device__ __forceinline__ void interp_prims(const T* __restrict__ cells, int n2, const CellCoef& cc,
+                                             T v[8]) {
+    const T d1 = (T)cc.d1, d2 = (T)cc.d2;
+    const T c0 = (T(1) - d1) * (T(1) - d2), c1 = (T(1) - d1) * d2;
+    const T c2 = d1 * (T(1) - d2), c3 = d1 * d2;
+    T a[8], b[8], e[8], f[8];
+    const T* p = cells + (size_t)cc.base * 8;
+    load_cell(p, a);
+    load_cell(p + 8, b);
+    load_cell(p + (size_t)n2 * 8, e);
+    load_cell(p + (size_t)n2 * 8 + 8, f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = a[q] * c0 + b[q] * c1 + e[q] * c2 + f[q] * c3;
+}
+
+template <class T>
+struct MetricT {
+    T d00, d01, d03, d11, d13, d22, d33;
+    T u00, u01, u11, u13, u22, u33;
+};
+
+template <class T>
+__device__ __forceinline__ MetricT<T> metric_cast(const MetricDD& d, const MetricUU& u) {
+    MetricT<T> m;
+    m.d00 = (T)d.g00; m.d01 = (T)d.g01; m.d03 = (T)d.g03; m.d11 = (T)d.g11;
+    m.d13 = (T)d.g13; m.d22 = (T)d.g22; m.d33 = (T)d.g33;
+    m.u00 = (T)u.g00; m.u01 = (T)u.g01; m.u11 = (T)u.g11; m.u13 = (T)u.g13;
+    m.u22 = (T)u.g22; m.u33 = (T)u.g33;
+    return m;
+}
+
+template <class T>
+__device__ __forceinline__ void lowerT(const MetricT<T>& g, const T v[4], T out[4]) {
+    out[0] = g.d00 * v[0] + g.d01 * v[1] + g.d03 * v[3];
+    out[1] = g.d01 * v[0] + g.d11 * v[1] + g.d13 * v[3];
+    out[2] = g.d22 * v[2];
+    out[3] = g.d03 * v[0] + g.d13 * v[1] + g.d33 * v[3];
+}
+
+template <class T>
+struct Fluid {
+    T ne, thetae, B, bsq;
+    T ucon[4], bcon[4];
+};
+
+// get_fluid_params (raptor_harm_model.c:190-290) from interpolated
+// primitives.  Returns false in the sigma = b^2/rho > 1 cut (line 285).
+template <class T>
+__device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>& g, T Ne_unit, T B_unit,
+                                                 T r_high, T r_low, Fluid<T>& fl) {
+    const T tiny = (T)1.e-20;
+    const T rho = v[0], uu = v[1];
+    const T V1 = v[2], V2 = v[3], V3 = v[4];
+    const T Bp1 = v[5], Bp2 = v[6], Bp3 = v[7];
+    fl.ne = rho * Ne_unit;
+    // g_ij V^i V^j, i,j = 1..3, in the reference's loop order with its zeros dropped
+    const T VdotV = g.d11 * V1 * V1 + g.d13 * V1 * V3 + g.d22 * V2 * V2 + g.d13 * V3 * V1 +
+                    g.d33 * V3 * V3;
+    const T Vfac = sqrt(T(-1) / g.u00 * (T(1) + fabs(VdotV)));
+    T* U = fl.ucon;
+    U[0] = -Vfac * g.u00;
+    U[1] = V1 - Vfac * g.u01;
+    U[2] = V2;  // g^{02} = 0
+    U[3] = V3;  // g^{03} = 0
+    T Ucov[4];
+    lowerT(g, U, Ucov);
+    const T UdotBp = Ucov[1] * Bp1 + Ucov[2] * Bp2 + Ucov[3] * Bp3;
+    T* Bc = fl.bcon;
+    const T iU0 = T(1) / U[0];
+    Bc[0] = UdotBp;
+    Bc[1] = (Bp1 + U[1] * UdotBp) * iU0;
+    Bc[2] = (Bp2 + U[2] * UdotBp) * iU0;
+    Bc[3] = (Bp3 + U[3] * UdotBp) * iU0;
+    T Bcov[4];
+    lowerT(g, Bc, Bcov);
+    const T Bsq = Bc[0] * Bcov[0] + Bc[1] * Bcov[1] + Bc[2] * Bcov[2] + Bc[3] * Bcov[3];
+    fl.bsq = Bsq;
+    fl.B = sqrt(Bsq) * B_unit + tiny;
+    // R-beta electron temperature, raptor_harm_model.c:262-276
+    const T beta = uu * (T(4) / T(3) - T(1)) / (T(0.5) * (Bsq + tiny));
+    const T b2 = beta * beta;
+    const T i1b2 = T(1) / (T(1) + b2);
+    const T trat = r_high * b2 * i1b2 + r_low * i1b2;
+    const T two_temp_gam = T(0.5) * ((T(1) + T(2) / T(3) * (trat + T(1)) / (trat + T(2))) + T(4) / T(3));
+    const T Thetae_unit = (two_temp_gam - T(1)) * (T)(kPMass / kEMass) / (T(1) + trat);
+    T th = (uu / rho) * Thetae_unit;
+    if (th < T(0)) th = tiny;
+    fl.thetae = th;
+    return !(Bsq / rho > T(1));
+}
+
+// ---------------------------------------------------------------- FP64 form
+template <int NF>
+__device__ __forceinline__ bool rt_sample_fp64(const DevImage& im, const double y[8], const MksPoint& p,
+                                               double adl, double (&tau)[NF], double (&I)[NF]) {
+    MetricDD gd;
+    MetricUU gu;
+    mks_metric(p, im.geo, gd, gu);
+    const MetricT<double> g = metric_cast<double>(gd, gu);
+    const CellCoef cc = cell_coef(im, y[1], y[2]);
+    double v[8];
+    interp_prims(im.cells64, im.n2, cc, v);
+    Fluid<double> fl;
+    if (!fluid_from_prims(v, g, im.Ne_unit, im.B_unit, im.r_high, im.r_low, fl)) return false;
+
+    const double k[4] = {y[4], y[5], y[6], y[7]};
+    double kd[4];
+    lowerT(g, k, kd);
+    const double* U = fl.ucon;
+    const double* Bc = fl.bcon;
+    const double kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
+    // pitch_angle (radiative_transfer.c:32-47): cosine, clamped to [-1, 1]
+    double pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) /
+                   (fabs(kU) * fl.B * im.inv_B_unit);
+    if (fabs(pitch) > 1.0) pitch /= fabs(pitch);
+    const double sth = sqrt(1.0 - pitch * pitch);
+    const double nuc = kECharge * fl.B / (2.0 * CUDART_PI * kEMass * kC);
+    const double nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
+    const bool emits = (fabs(sth) >= 1.e-10) && (fl.thetae > 1e-4);
+    const double K2 = 2.0 * fl.thetae * fl.thetae;
+    const double T = fl.thetae * kEMass * kC * kC / kBoltz;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        if (f >= im.nfreq) break;
+        // freq_in_plasma_frame with nu scaling folded: -(u . k_d) nu
+        double nup = -kU * im.freq[f];
+        if (nup <= 0.0) nup = 1.0;
+        const double dlf = adl * im.rg_over_nu[f];
+        if (emits && nup != 1.0) {
+            const double X = nup / nus;
+            const double cb = cbrt(X);
+            const double sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);  // 2^(11/12)
+            const double j = fl.ne * 1.4142135623730951 * CUDART_PI * nus / (3.0 * K2) * (sq * sq) *
+                             exp(-cb) * kE2C;
+            const double Bnu = 2.0 * nup * nup * nup / (kC * kC) * 1.0 /
+                               (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
+            const double an = j * kE2CH / Bnu / kE2C;
+            tau[f] += nup * an * dlf;
+            const double dI = (j / (nup * nup)) * exp(-tau[f]) * dlf;
+            if (tau[f] < 6.907755278982137 && !(tau[f] < 0.0)) I[f] += dI;  // log(1000)
+        } else {
+            // j = 0.  a = 0 / B_nu is 0 unless B_nu underflowed to 0 (exp
+            // overflow at very low Theta_e), where the reference gets NaN and
+            // tau stays NaN for the rest of the ray.
+            const double Bnu = 2.0 * nup * nup * nup / (kC * kC) * 1.0 /
+                               (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
+            if (!(Bnu != 0.0)) tau[f] = __longlong_as_double(0x7ff8000000000000ll);
+        }
+    }
+    return true;
+}
+
+// ------------------------------------------------------------- FP32 form
+__device__ __forceinline__ void neumaier_add(float& s, float& c, float x) {
+    const float t = s + x;
+    if (fabsf(s) >= fabsf(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
+template <int NF>
+__device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double y[8], const MksPoint& p,
+                                               double adl, float (&tau)[NF], float (&tauc)[NF],
+                                               float (&I)[NF], float (&Ic)[NF]) {
+    MetricDD gd;
+    MetricUU gu;
+    mks_metric(p, im.geo, gd, gu);
+    const MetricT<float> g = metric_cast<float>(gd, gu);
+    const CellCoef cc = cell_coef(im, y[1], y[2]);
+    float v[8];
+    interp_prims(im.cells32, im.n2, cc, v);
+    Fluid<float> fl;
+    if (!fluid_from_prims(v, g, (float)im.Ne_unit, (float)im.B_unit, (float)im.r_high, (float)im.r_low, fl))
+        return false;
+    const float k[4] = {(float)y[4], (float)y[5], (float)y[6], (float)y[7]};
+    float kd[4];
+    lowerT(g, k, kd);
+    const float* U = fl.ucon;
+    const float* Bc = fl.bcon;
+    const float kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
+    float pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) /
+                  (fabsf(kU) * (fl.B * (float)im.inv_B_unit));
+    if (fabsf(pitch) > 1.0f) pitch /= fabsf(pitch);
+    const float sth = sqrtf(1.0f - pitch * pitch);
+    const float nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
+    const float nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
+    const bool emits = (fabsf(sth) >= 1.e-10f) && (fl.thetae > 1e-4f);
+    // j / e2_c = n_e sqrt(2) pi nu_s / (3 K2) F(X) with K2 = 2 Theta^2, nu_s = (2/9) nu_c Theta^2 sin
+    const float jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
+    const float xpre = (float)(kPlanck / (kEMass * kC * kC)) / fl.thetae;  // h nu / (k T) per Hz
+    const float ktau = (float)(kE2CH * kC * kC * 0.5);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        if (f >= im.nfreq) break;
+        float nup = -kU * (float)im.freq[f];
+        if (nup <= 0.0f) nup = 1.0f;
+        if (!(emits && nup != 1.0f)) continue;
+        const float dlf = (float)(adl * im.rg_over_nu[f]);
+        const float X = nup / nus;
+        const float cb = cbrtf(X);
+        const float sq = sqrtf(X) + 1.8877486f * sqrtf(cb);
+        const float jh = jpre * (sq * sq) * expf(-cb);
+        const float q = (jh / nup) / nup;
+        const float dtau = q * expm1f(xpre * nup) * ktau * dlf;
+        neumaier_add(tau[f], tauc[f], dtau);
+        const float t = tau[f] + tauc[f];
+        const float dI = q * expf(-t) * dlf;
+        if (t < 6.9077553f && !(t < 0.0f)) neumaier_add(I[f], Ic[f], dI);
+    }
+    return true;
+}
+
+}  // namespace raptor

@@ -1,0 +1,139 @@
+"""Parity of the CUDA engine (through its C ABI) with the reference's
+outputs (golden fixtures) and with the oracle port.
+
+FP64 form: per-pixel relative error <= 1e-6 except <= 0.1% grazing pixels,
+total flux within 1e-6 (tests/parity.py).  Mixed form: total flux within 1e-4.
+"""
+import numpy as np
+import pytest
+
+from tests.parity import FLUX_RTOL_MIXED, assert_fp64_parity, load_golden, pixel_errors
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from raptor_gb300 import engine
+    e = engine.Engine()
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope="module")
+def small():
+    return load_golden("small_g64.npz")
+
+
+def _desc(params, grid):
+    from raptor_gb300 import engine
+    w, h, incl, freq, rk, eps, mu, rh, rl = params
+    return engine.image_desc(int(w), int(h), [freq], grid=grid, inclination=incl, stepsize=eps, m_unit=mu,
+                             r_high=rh, r_low=rl, integrator=int(rk))
+
+
+NAMES = ["g64_i60_rk4", "g64_i17_rk4", "g64_i120_rk4_86", "g64_i60_rk2", "g64_i35_rk4_odd"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fp64_matches_reference_small(eng, torus64, small, name):
+    from raptor_gb300 import engine
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    img, spec = eng.render(_desc(small[f"{name}_params"], gid), engine.PREC_FP64)
+    assert_fp64_parity(img, small[f"{name}_img"], name)
+    assert spec[0] == pytest.approx(small[f"{name}_spec"][0], rel=1e-6)
+    st = eng.stats()
+    assert st["rays"] == img.size and st["n_nonfinite"] == 0
+
+
+def test_fp64_matches_reference_100x100_on_256(eng, torus256):
+    from raptor_gb300 import engine
+    g = load_golden("img100_g256.npz")
+    gid = eng.upload_grid(torus256.geom, torus256.prims)
+    img, spec = eng.render(_desc(g["params"], gid), engine.PREC_FP64)
+    assert_fp64_parity(img, g["img"], "100x100 on 256^2")
+    assert spec[0] == pytest.approx(g["spec"][0], rel=1e-6)
+
+
+def test_fp64_matches_port_and_step_counts(eng, torus64):
+    """Step and sample counters agree with the oracle's, ray by ray in sum."""
+    from oracle import port
+    from raptor_gb300 import engine
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    d = engine.image_desc(20, 20, [230e9, 86e9], grid=gid, inclination=45.0)
+    img, _ = eng.render(d, engine.PREC_FP64)
+    st = eng.stats()
+    sc = port.Scene(torus64.geom, torus64.prims, 20, 20, inclination=45.0)
+    ref, _, rs = sc.render([230e9, 86e9], with_stats=True)
+    assert_fp64_parity(img.reshape(-1, 2)[:, 0], ref[:, 0], "f0")
+    assert_fp64_parity(img.reshape(-1, 2)[:, 1], ref[:, 1], "f1")
+    assert abs(st["steps"] - int(rs["steps"].sum())) <= 0.001 * st["steps"]
+    assert abs(st["rt_calls"] - int(rs["rt_calls"].sum())) <= 0.001 * st["rt_calls"]
+
+
+def test_mixed_flux_within_1e4(eng, torus256):
+    from raptor_gb300 import engine
+    g = load_golden("img100_g256.npz")
+    gid = eng.upload_grid(torus256.geom, torus256.prims)
+    img, spec = eng.render(_desc(g["params"], gid), engine.PREC_MIXED)
+    ref_flux = g["spec"][0]
+    assert abs(spec[0] - ref_flux) / ref_flux <= FLUX_RTOL_MIXED
+    err = pixel_errors(img, g["img"])
+    assert np.median(err) < 1e-4
+
+
+def test_deterministic(eng, torus64):
+    from raptor_gb300 import engine
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    d = engine.image_desc(24, 24, [230e9], grid=gid)
+    a, sa = eng.render(d, engine.PREC_FP64)
+    b, sb = eng.render(d, engine.PREC_FP64)
+    assert np.array_equal(a, b) and np.array_equal(sa, sb)
+
+
+def test_batch_equals_single_images(eng, torus64):
+    """Images of different sizes, angles and frequencies in one launch give
+    exactly what they give alone."""
+    from raptor_gb300 import engine
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    descs = [engine.image_desc(17, 9, [230e9], grid=gid, inclination=30.0),
+             engine.image_desc(8, 12, [86e9, 345e9], grid=gid, inclination=150.0, m_unit=5e18),
+             engine.image_desc(5, 5, [230e9], grid=gid, inclination=90.0, integrator=engine.RK2)]
+    for prec in (engine.PREC_FP64, engine.PREC_MIXED):
+        batch, bspec = eng.render(descs, prec)
+        off = 0
+        soff = 0
+        for d in descs:
+            one, ospec = eng.render(d, prec)
+            assert np.array_equal(batch[off:off + one.size], one)
+            assert np.array_equal(bspec[soff:soff + d.n_freq], ospec)
+            off += one.size
+            soff += d.n_freq
+
+
+def test_range_render_is_a_slice(eng, torus64):
+    from raptor_gb300 import engine
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    d = engine.image_desc(16, 16, [230e9], grid=gid)
+    full, _ = eng.render(d, engine.PREC_FP64)
+    part, _ = eng.render(d, engine.PREC_FP64, ray_begin=37, ray_count=100)
+    assert np.array_equal(part[37:137], full[37:137])
+    assert not np.any(part[:37]) and not np.any(part[137:])
+
+
+def test_invalid_arguments_are_rejected(eng, torus64):
+    from raptor_gb300 import engine
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    with pytest.raises(engine.EngineError):
+        eng.render(engine.image_desc(4, 4, [230e9], grid=gid + 5))
+    with pytest.raises(engine.EngineError):
+        eng.render(engine.image_desc(4, 4, [230e9], grid=gid, integrator=3))
+    with pytest.raises(engine.EngineError):
+        eng.render(engine.image_desc(0, 4, [230e9], grid=gid))
+    bad = torus64.prims.copy()
+    bad[0, 3, 3] = np.nan
+    with pytest.raises(engine.EngineError):
+        eng.upload_grid(torus64.geom, bad)
+    # the context stays usable after rejected calls
+    img, _ = eng.render(engine.image_desc(4, 4, [230e9], grid=gid))
+    assert np.all(np.isfinite(img))

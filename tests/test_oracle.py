@@ -1,0 +1,117 @@
+"""The oracle (C port) pinned against the reference's own outputs: golden
+fixtures made by tests/golden/make_golden.py from the reference build."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.parity import assert_fp64_parity, load_golden
+
+
+@pytest.fixture(scope="module")
+def small():
+    return load_golden("small_g64.npz")
+
+
+def _scene(dump, params):
+    from oracle import port
+    w, h, incl, freq, rk, eps, mu, rh, rl = params
+    return port.Scene(dump.geom, dump.prims, int(w), int(h), inclination=incl, stepsize=eps, m_unit=mu,
+                      r_high=rh, r_low=rl, integrator=int(rk)), freq
+
+
+def test_generator_matches_golden(torus64, small):
+    from tests.golden.make_golden import prim_checksum
+    np.testing.assert_allclose(prim_checksum(torus64.prims), small["prim_checksum"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["g64_i60_rk4", "g64_i17_rk4", "g64_i120_rk4_86", "g64_i60_rk2",
+                                  "g64_i35_rk4_odd"])
+def test_port_matches_reference_images(torus64, small, name):
+    sc, freq = _scene(torus64, small[f"{name}_params"])
+    out, _ = sc.render([freq])
+    assert_fp64_parity(out[:, 0], small[f"{name}_img"], name)
+    np.testing.assert_allclose(out[:, 0].sum(), small[f"{name}_spec"][0], rtol=1e-6)
+
+
+def test_port_matches_reference_100x100_on_256(torus256):
+    g = load_golden("img100_g256.npz")
+    from tests.golden.make_golden import prim_checksum
+    np.testing.assert_allclose(prim_checksum(torus256.prims), g["prim_checksum"], rtol=1e-12)
+    sc, freq = _scene(torus256, g["params"])
+    out, _ = sc.render([freq])
+    assert_fp64_parity(out[:, 0], g["img"], "100x100 on 256^2")
+
+
+def test_port_function_kats(torus64, small):
+    sc, _ = _scene(torus64, small["g64_i60_rk4_params"])
+    for k, X in enumerate(small["kat_X"]):
+        np.testing.assert_allclose(sc.metric_dd(X).ravel(), small["kat_gdd"][k], rtol=1e-13, atol=1e-300)
+        np.testing.assert_allclose(sc.metric_uu(X).ravel(), small["kat_guu"][k], rtol=1e-13, atol=1e-300)
+        np.testing.assert_allclose(sc.connection(X).ravel(), small["kat_gamma"][k], rtol=1e-12, atol=1e-14)
+    from oracle import port
+    lib = port.load()
+    lat = small["kat_lattice"]
+    for i, (B, cp, th, nu, ne) in enumerate(lat):
+        j = lib.port_j_thsynch(B, cp, th, nu, ne)
+        # exp(-X^(1/3)) with X^(1/3) up to ~600 amplifies argument rounding
+        assert j == pytest.approx(small["kat_j"][i], rel=1e-11, abs=0)
+        assert lib.port_a_th(j, nu, th) == pytest.approx(small["kat_a"][i], rel=1e-11, abs=0)
+    for k, X in enumerate(small["kat_fluid_X"]):
+        ok, f = sc.fluid(X)
+        assert ok == small["kat_fluid_ok"][k]
+        # u^1 = V^1 - Vfac g^{01} cancels; compare to 1e-11 relative or 1e-15 absolute
+        np.testing.assert_allclose(f, small["kat_fluid"][k], rtol=1e-11, atol=1e-15)
+
+
+def test_connection_is_metric_derivative(torus64, small):
+    """Gamma^i_jk = 1/2 g^il (d_j g_lk + d_k g_lj - d_l g_jk) by central
+    differences (the reference's connection_num_udd check, metric.c:255-328)."""
+    sc, _ = _scene(torus64, small["g64_i60_rk4_params"])
+    h = 1e-6
+    for X in small["kat_X"][:8]:
+        dg = np.zeros((4, 4, 4))
+        for l in (1, 2):
+            Xp = X.copy(); Xp[l] += h
+            Xm = X.copy(); Xm[l] -= h
+            dg[l] = (sc.metric_dd(Xp) - sc.metric_dd(Xm)) / (2 * h)
+        gi = sc.metric_uu(X)
+        G = 0.5 * (np.einsum("il,jlk->ijk", gi, dg) + np.einsum("il,klj->ijk", gi, dg)
+                   - np.einsum("il,ljk->ijk", gi, dg))
+        np.testing.assert_allclose(sc.connection(X), G, rtol=2e-5, atol=1e-7 * np.abs(G).max())
+
+
+def test_initial_photon_is_null(torus64, small):
+    sc, _ = _scene(torus64, small["g64_i60_rk4_params"])
+    for alpha, beta in [(-7.3, 3.1), (0.4, -12.0), (19.0, 19.0), (-0.2, 0.2)]:
+        ph = sc.init_photon(alpha, beta)
+        g = sc.metric_dd(ph[:4])
+        kk = ph[4:] @ g @ ph[4:]
+        assert abs(kk) / ph[4] ** 2 < 1e-9
+
+
+def test_camera_angle_root(torus64, small):
+    sc, _ = _scene(torus64, small["g64_i60_rk4_params"])
+    x2 = sc.camera_x2()
+    th = np.pi * x2 + 0.5 * (1 - 0.3) * np.sin(2 * np.pi * x2)
+    assert th == pytest.approx(np.arccos(np.cos(np.radians(60.0))), abs=1e-14)
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(os.environ.get("RAPTOR_REFERENCE_DIR", "/root/reference"),
+                                                    "integrator.c")),
+                    reason="reference sources not present on this machine")
+def test_port_vs_reference_fresh_seed(tmp_path):
+    """Port against the reference build on a torus the fixtures never saw."""
+    from oracle import port, ref
+    from raptor_gb300 import harm, synth
+    from tests.golden.make_golden import quiet
+    d = synth.make_torus(n1=64, n2=64, a=0.5, seed=99)
+    path = str(tmp_path / "t.dump")
+    harm.write_dump(path, d)
+    model = harm.ModelIn(IMG_WIDTH=20, IMG_HEIGHT=20, STEPSIZE=0.05)
+    with quiet():
+        s = ref.RefSession(path, model, 2e19, 75.0, 5.0, 2.0, 0.0, n1=64, n2=64, workdir=str(tmp_path))
+        img, spec, _ = s.render_serial(345e9)
+    sc = port.Scene(d.geom, d.prims, 20, 20, inclination=75.0, m_unit=2e19, r_high=5.0, r_low=2.0)
+    out, _ = sc.render([345e9])
+    assert_fp64_parity(out[:, 0], img, "fresh seed")

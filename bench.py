@@ -36,12 +36,6 @@ INCL = 60.0
 FREQ = 230e9
 EPS = 0.05
 L2_FLUSH_BYTES = 512 << 20
-# Algorithmic FP64 work per unit, counted on the oracle's restatement of the
-# reference (tests/test_flop_count.py pins these): one RK4 geodesic step, and
-# one radiative-transfer sample with F frequencies.
-FLOP_PER_RK4_STEP = 1260.0
-FLOP_PER_SAMPLE_BASE = 316.0
-FLOP_PER_SAMPLE_FREQ = 63.0
 NOMINAL_FP64_TFLOPS = 1.25
 
 
@@ -262,7 +256,7 @@ def run_engine(args, rank, world, local):
     e2e_ms = []
     if barrier:
         barrier()
-    for _ in range(args.steps):
+    for _ in range(0 if args.no_e2e else args.steps):
         blib.raptor_bench_flush_l2(dev, L2_FLUSH_BYTES)
         t0 = time.perf_counter()
         eng.upload_grid(dump.geom, prims_pinned, grid_id=gid)
@@ -279,14 +273,18 @@ def run_engine(args, rank, world, local):
     st = results["fp64"]["stats"]
     t_fp64 = maxed(float(np.mean(results["fp64"]["device_ms"])))
     t_mixed = maxed(float(np.mean(results["mixed"]["device_ms"])))
-    t_e2e = maxed(float(np.mean(e2e_ms)))
+    t_e2e = maxed(float(np.mean(e2e_ms))) if e2e_ms else None
+    e2e_h2d = int(dump.prims.nbytes + e2e_stats["h2d_bytes"])  # grid upload + descriptors
     k_fp64 = float(np.mean(results["fp64"]["kernel_ms"]))
-    flop = FLOP_PER_RK4_STEP * st["steps"] + (FLOP_PER_SAMPLE_BASE + FLOP_PER_SAMPLE_FREQ * 1) * st["rt_samples"]
+    from raptor_gb300 import workload
+    flop = workload.image_flops(st["rays"], st["steps"], st["rt_samples"], 1, rk4=True)
     achieved = flop / (k_fp64 * 1e-3) / 1e12
 
     # VJP / forward ratio (if the adjoint is available)
     vjp = None
     try:
+        if args.no_e2e:
+            raise RuntimeError("skipped in the profile workload")
         dl = np.ones(W * H) * 1e-3
         t0 = time.perf_counter()
         eng.vjp(desc, dl, engine.PREC_FP64, want_fields=True)
@@ -310,8 +308,10 @@ def run_engine(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": t_fp64, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fishbone-Moncrief torus)",
         "config": dict(workload_config(), parallelism=f"replicas{n}"),
-        "e2e": {"value": t_e2e / n, "unit": "ms/image", "h2d_bytes_per_step": int(e2e_stats["h2d_bytes"]),
-                "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"])},
+        "e2e": ({"value": t_e2e / n, "unit": "ms/image", "h2d_bytes_per_step": e2e_h2d,
+                 "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"]),
+                 "path": "raptor_gpu_upload_grid (pinned host prims) + raptor_gpu_render (host image out)"}
+                if t_e2e is not None else None),
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value if peak.value > 0 else None, "traffic": None,
@@ -342,8 +342,17 @@ def main():
     ap.add_argument("--impl", choices=("engine", "reference"), default="engine")
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--workload", choices=("1024", "profile"), default="1024",
+                    help="profile: a 256x256 image on a 256x256 torus, render timings only (for ncu captures)")
     args = ap.parse_args()
+    if args.workload == "profile":
+        global W, H, GRID_N
+        W = H = 256
+        GRID_N = 256
+        args.no_cpu_baseline = True
+        args.no_e2e = True
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)

@@ -154,6 +154,17 @@ long long raptor_gpu_spectrum_size(const raptor_image_desc *imgs, int n_imgs);
 /* Statistics of the last render or VJP on this context. */
 int raptor_gpu_get_stats(const raptor_gpu_ctx *ctx, raptor_gpu_stats *out);
 
+/* Per-step record of one ray, the engine's form of the reference's GEOD
+ * switch (integrator.c:172-184,208-210,238-240, which writes x1,x2,x3 per
+ * step to geod/geodesic_x_y.dat).  records[k*16 + c] after step k (k = 0 is
+ * the initial photon): c = 0..7 photon_u, 8 d lambda, 9 tau of the first
+ * frequency, 10 its intensity before the nu^3 scaling, 11 steps, 12 theta
+ * turns, 13 event (0 no transfer, 1 sigma cut, 2 sampled, 3 escaped), 14 the
+ * order-limit stop flag, 15 unused.  *n_records = records written. */
+#define RAPTOR_TRACE_WIDTH 16
+int raptor_gpu_trace_ray(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision, int pixel,
+                         int max_records, double *records, int *n_records);
+
 /* Vector-Jacobian product of one image: given dL_dI [W*H][n_freq] (same
  * layout and nu^3 scaling as I_out), returns dL/d(M_UNIT, R_HIGH, R_LOW,
  * INCLINATION) and, if the pointers are set, dL/d rho and dL/d u on the

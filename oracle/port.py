@@ -67,6 +67,8 @@ def load() -> ctypes.CDLL:
     lib.port_a_th.restype = D
     lib.port_fluid.argtypes = [S, P(D), P(D)]
     lib.port_fluid.restype = ctypes.c_int
+    lib.port_trace_ray.argtypes = [S, ctypes.c_int, P(D), ctypes.c_int, ctypes.c_int, P(D)]
+    lib.port_trace_ray.restype = ctypes.c_int
     _LIB = lib
     return lib
 
@@ -106,6 +108,14 @@ class Scene:
             st = np.ctypeslib.as_array(stats)[:len(pix)]
             return out, dt, st
         return out, dt
+
+    def trace_ray(self, pixel, freqs, cap=4096):
+        freqs = np.atleast_1d(np.asarray(freqs, dtype=np.float64))
+        rec = np.zeros((cap, 16))
+        n = self.lib.port_trace_ray(ctypes.byref(self.c), pixel, _dp(freqs), len(freqs), cap, _dp(rec))
+        if n < 0:
+            raise RuntimeError("port_trace_ray failed")
+        return rec[:n]
 
     def metric_dd(self, X):
         g = np.zeros(16)

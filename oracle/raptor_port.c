@@ -14,14 +14,38 @@
  * find the same root of a monotone function; the reference stops at a
  * 1e-6 relative step, so the two differ by at most ~1e-12 in the camera
  * angle. */
-#include "raptor_port.h"
-
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
+
+/* Operation counting (tests/test_flop_count.py): compiled as C++ with
+ * -DPORT_COUNT_FLOPS, `double` becomes a type that counts every arithmetic
+ * operation and libm call, and the ray loop files the counts under ray
+ * set-up, geodesic step, and transfer call (sampled or cut). */
+#ifdef PORT_COUNT_FLOPS
+#include "flopcount.hpp"
+#define double cdouble
+unsigned long long port_flop_counter = 0;
+static unsigned long long flop_bucket[8];
+#define FLOP_SNAP(v) unsigned long long v = port_flop_counter
+#define FLOP_ADD(b, v) (flop_bucket[b] += port_flop_counter - (v))
+extern "C" void port_flop_buckets(unsigned long long out[8], int reset)
+{
+    for (int i = 0; i < 8; i++) {
+        out[i] = flop_bucket[i];
+        if (reset)
+            flop_bucket[i] = 0;
+    }
+}
+#else
+#define FLOP_SNAP(v)
+#define FLOP_ADD(b, v)
+#endif
+
+#include "raptor_port.h"
 
 /* constants.h:16-29, j_nu.c:15 (cgs) */
 #define K_ECHARGE 4.8032068e-10
@@ -532,9 +556,28 @@ static int transfer(const ray_ctx *c, const double X[4], const double k[4], doub
     return 1;
 }
 
+/* one per-step record, the layout of raptor_gpu_trace_ray */
+static void record(double *rec, int cap, int steps, const double ph[8], double dl, double tau0, double I0,
+                   int turns, int event, int stop)
+{
+    if (!rec || steps >= cap)
+        return;
+    double *r = rec + (size_t)steps * 16;
+    for (int i = 0; i < 8; i++)
+        r[i] = ph[i];
+    r[8] = dl;
+    r[9] = tau0;
+    r[10] = I0;
+    r[11] = steps;
+    r[12] = turns;
+    r[13] = event;
+    r[14] = stop;
+    r[15] = 0.;
+}
+
 /* ---- the per-pixel loop, integrator.c:149-289 ---- */
 static void trace(const ray_ctx *c, int x, int y, const double *freqs, int nf, double *I,
-                  port_ray_stats *st)
+                  port_ray_stats *st, double *rec, int cap)
 {
     const port_scene *s = c->s;
     double tau[64];
@@ -547,11 +590,15 @@ static void trace(const ray_ctx *c, int x, int y, const double *freqs, int nf, d
     double alpha = -s->cam_size_x * 0.5 + (x + 0.5) * stepx;
     double beta = -s->cam_size_y * 0.5 + (y + 0.5) * stepy;
     double ph[8];
+    FLOP_SNAP(f_init);
     init_photon(c, alpha, beta, ph);
     double r = exp(ph[1]);
+    FLOP_ADD(0, f_init);
     int steps = 0, turns = 0, stop = 0, samples = 0, calls = 0, reason = 0;
     double thdot_prev = 0.;
+    record(rec, cap, 0, ph, 0., tau[0], I[0], 0, 0, 0);
     while (r < K_CUTOFF_OUTER && r > c->cutoff_inner && steps < K_MAX_STEPS && !stop) {
+        FLOP_SNAP(f_step);
         if (thdot_prev * ph[6] < 0. && steps > 2)
             turns += 1;
         thdot_prev = ph[6];
@@ -566,15 +613,26 @@ static void trace(const ray_ctx *c, int x, int y, const double *freqs, int nf, d
         if (ph[1] > c->stopx1 && ph[5] < 0) {
             reason = 2;
             steps++;
+            FLOP_ADD(1, f_step);
+            record(rec, cap, steps, ph, dl, tau[0], I[0], turns, 3, stop);
             break;
         }
         r = exp(ph[1]);
+        FLOP_ADD(1, f_step);
+        int event = 0;
         if (ph[1] < c->stopx1 && ph[1] > s->startx1 && ph[2] > s->startx2 && ph[2] < c->stopx2) {
             calls++;
-            samples += transfer(c, ph, ph + 4, adl, freqs, nf, tau, I);
+            FLOP_SNAP(f_rt);
+            int ok = transfer(c, ph, ph + 4, adl, freqs, nf, tau, I);
+            FLOP_ADD(ok ? 3 : 2, f_rt);
+            samples += ok;
+            event = ok ? 2 : 1;
         }
+        record(rec, cap, steps + 1, ph, dl, tau[0], I[0], turns, event, stop);
+        FLOP_SNAP(f_tail);
         r = exp(ph[1]);
         steps = steps + 1;
+        FLOP_ADD(1, f_tail);
     }
     if (!reason) {
         if (!(r == r))
@@ -604,25 +662,42 @@ static void trace(const ray_ctx *c, int x, int y, const double *freqs, int nf, d
     }
 }
 
+static void make_ctx(const port_scene *s, ray_ctx *c)
+{
+    memset(c, 0, sizeof *c);
+    c->s = s;
+    c->stopx1 = s->startx1 + s->n1 * s->dx1;
+    c->stopx2 = s->startx2 + s->n2 * s->dx2;
+    /* set_constants, utilities.c:19-20; set_units, grmhd.c:17-33 */
+    double Rh = (1. + sqrt(1. - s->a * s->a));
+    c->cutoff_inner = Rh * (1. + K_HORIZON_MARG);
+    double L = K_GGRAV * s->mbh / (K_CLIGHT * K_CLIGHT);
+    double rho_unit = s->m_unit / pow(L, 3);
+    c->B_unit = K_CLIGHT * sqrt(4. * K_PI * rho_unit);
+    c->Ne_unit = rho_unit / (K_PMASS + K_EMASS);
+    c->Rg = K_GGRAV * s->mbh / K_CLIGHT / K_CLIGHT;
+    c->cam_x2 = port_camera_x2(s);
+}
+
+int port_trace_ray(const port_scene *s, int pixel, const double *freqs, int nfreq, int cap, double *records)
+{
+    if (nfreq < 1 || nfreq > 64 || pixel < 0 || pixel >= s->width * s->height)
+        return -1;
+    ray_ctx c;
+    make_ctx(s, &c);
+    double I[64];
+    port_ray_stats st;
+    trace(&c, pixel % s->width, pixel / s->width, freqs, nfreq, I, &st, records, cap);
+    return st.steps + 1 < cap ? st.steps + 1 : cap;
+}
+
 int port_render(const port_scene *s, const int *pixels, int n, const double *freqs, int nfreq,
                 double *out, port_ray_stats *stats, int nthreads)
 {
     if (nfreq < 1 || nfreq > 64)
         return -1;
     ray_ctx c;
-    memset(&c, 0, sizeof c);
-    c.s = s;
-    c.stopx1 = s->startx1 + s->n1 * s->dx1;
-    c.stopx2 = s->startx2 + s->n2 * s->dx2;
-    /* set_constants, utilities.c:19-20; set_units, grmhd.c:17-33 */
-    double Rh = (1. + sqrt(1. - s->a * s->a));
-    c.cutoff_inner = Rh * (1. + K_HORIZON_MARG);
-    double L = K_GGRAV * s->mbh / (K_CLIGHT * K_CLIGHT);
-    double rho_unit = s->m_unit / pow(L, 3);
-    c.B_unit = K_CLIGHT * sqrt(4. * K_PI * rho_unit);
-    c.Ne_unit = rho_unit / (K_PMASS + K_EMASS);
-    c.Rg = K_GGRAV * s->mbh / K_CLIGHT / K_CLIGHT;
-    c.cam_x2 = port_camera_x2(s);
+    make_ctx(s, &c);
     double nu3[64];
     for (int f = 0; f < nfreq; f++)
         nu3[f] = pow(freqs[f], 3.);
@@ -635,7 +710,7 @@ int port_render(const port_scene *s, const int *pixels, int n, const double *fre
         int pix = pixels[k];
         int yy = pix / s->width, xx = pix % s->width;
         double I[64];
-        trace(&c, xx, yy, freqs, nfreq, I, stats ? &stats[k] : NULL);
+        trace(&c, xx, yy, freqs, nfreq, I, stats ? &stats[k] : NULL, NULL, 0);
         for (int f = 0; f < nfreq; f++)
             out[(size_t)k * nfreq + f] = I[f] * nu3[f];
     }

@@ -41,6 +41,10 @@ typedef struct port_ray_stats {
 int port_render(const port_scene *s, const int *pixels, int n, const double *freqs, int nfreq,
                 double *out, port_ray_stats *stats, int nthreads);
 
+/* Per-step records of one ray, the layout of raptor_gpu_trace_ray (16
+ * doubles per step, step 0 = initial photon).  Returns records written. */
+int port_trace_ray(const port_scene *s, int pixel, const double *freqs, int nfreq, int cap, double *records);
+
 /* Function-level entry points (for known-answer tests). */
 void port_metric_dd(const port_scene *s, const double X[4], double g[16]);
 void port_metric_uu(const port_scene *s, const double X[4], double g[16]);

@@ -18,7 +18,7 @@ struct LaunchShape {
 };
 
 using RayLaunchFn = void (*)(const LaunchShape&, cudaStream_t, const raptor::DevImage*, int, long long, long long,
-                             unsigned long long*, double*);
+                             unsigned long long*, double*, raptor::TraceSpec);
 
 struct GridSlot {
     bool used = false;
@@ -61,6 +61,8 @@ struct raptor_gpu_ctx {
     size_t grad_cap = 0;
     double* d_dldi = nullptr;
     size_t dldi_cap = 0;
+    double* d_trace = nullptr;
+    size_t trace_cap = 0;
     Batch batch;
     raptor_gpu_stats stats{};
     double last_upload_ms = 0.0;
@@ -76,5 +78,5 @@ RayLaunchFn pick_ray_kernel(int nf, bool mixed, const void** fn);
 LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn);
 LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, RayLaunchFn fn, const void* fnp);
 int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, long long rb, long long re,
-                   const LaunchShape& ls, RayLaunchFn fn, bool timed);
+                   const LaunchShape& ls, RayLaunchFn fn, bool timed, raptor::TraceSpec tr = {-1, nullptr, 0});
 int collect_stats(raptor_gpu_ctx* ctx, bool timed);

@@ -49,4 +49,15 @@ struct DevImage {
     double rg_over_nu[kMaxFreqs]; // R_g / freq (radiative_transfer.c:88)
 };
 
+// Per-step record of one traced ray (the analogue of the reference's GEOD
+// switch, integrator.c:172-240): y[8], d lambda, tau_0, raw I_0, steps,
+// theta turns, event (0 no transfer, 1 sigma cut, 2 sampled, 3 escaped),
+// stop flag, 0.
+constexpr int kTraceWidth = 16;
+struct TraceSpec {
+    long long ray;  // global ray index to record, or -1
+    double* out;    // [cap][kTraceWidth]
+    int cap;
+};
+
 }  // namespace raptor

@@ -12,8 +12,8 @@
 #include <vector>
 
 #include "raptor_gpu.h"
-#include "ray_kernel.cuh"
 #include "engine_internal.h"
+#include "ray_kernel.cuh"
 
 using namespace raptor;
 
@@ -225,6 +225,7 @@ extern "C" void raptor_gpu_destroy(raptor_gpu_ctx* ctx) {
     cudaFree(ctx->d_flag);
     cudaFree(ctx->d_grad);
     cudaFree(ctx->d_dldi);
+    cudaFree(ctx->d_trace);
     cudaFreeHost(ctx->h_imgs);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -340,8 +341,8 @@ extern "C" long long raptor_gpu_spectrum_size(const raptor_image_desc* imgs, int
 // ----------------------------------------------------------------- render
 template <int NF, bool MIXED>
 static void launch_ray(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b, long long e,
-                       unsigned long long* ctr, double* out) {
-    ray_kernel<NF, MIXED><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill);
+                       unsigned long long* ctr, double* out, TraceSpec tr) {
+    ray_kernel<NF, MIXED><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
 }
 
 RayLaunchFn pick_ray_kernel(int nf, bool mixed, const void** fn) {
@@ -429,12 +430,12 @@ LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn) {
 // Enqueue the whole render (counters reset, ray kernel, spectrum) on the
 // context stream; used directly and under stream capture.
 int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, long long rb, long long re,
-                   const LaunchShape& ls, RayLaunchFn fn, bool timed) {
+                   const LaunchShape& ls, RayLaunchFn fn, bool timed, TraceSpec tr) {
     if (timed) CK(cudaEventRecord(ctx->evA, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_counters, 0, kCtrCount * sizeof(unsigned long long), ctx->stream));
     if (rb > 0 || re < b.total_rays) CK(cudaMemsetAsync(ctx->d_out, 0, sizeof(double) * b.out_len, ctx->stream));
     if (timed) CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    fn(ls, ctx->stream, ctx->d_imgs, b.n, rb, re, ctx->d_counters, ctx->d_out);
+    fn(ls, ctx->stream, ctx->d_imgs, b.n, rb, re, ctx->d_counters, ctx->d_out, tr);
     CK(cudaGetLastError());
     if (timed) CK(cudaEventRecord(ctx->ev1, ctx->stream));
     spectrum_kernel<<<(unsigned)b.spec_len, 256, 0, ctx->stream>>>(ctx->d_imgs, ctx->d_spec_map,
@@ -526,4 +527,39 @@ extern "C" int raptor_gpu_render_range(raptor_gpu_ctx* ctx, const raptor_image_d
                                        double* spectrum_out) {
     if (ray_begin < 0 || ray_count < 0) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "negative ray range");
     return render_impl(ctx, imgs, n_imgs, precision, ray_begin, ray_count, I_out, spectrum_out);
+}
+
+extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, int pixel,
+                                    int max_records, double* records, int* n_records) {
+    if (!ctx) return RAPTOR_ERR_INVALID;
+    ctx->err[0] = 0;
+    if (!img || !records || !n_records || max_records <= 0)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "trace_ray: null output or non-positive max_records");
+    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "precision %d unknown", precision);
+    if (pixel < 0 || (long long)pixel >= (long long)img->width * img->height)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "pixel %d outside the %dx%d image", pixel, img->width, img->height);
+    CK(cudaSetDevice(ctx->device));
+    Batch& b = ctx->batch;
+    int rc = prepare_batch(ctx, img, 1, b);
+    if (rc) return rc;
+    const size_t bytes = sizeof(double) * (size_t)max_records * kTraceWidth;
+    rc = ensure_buffer(ctx, (void**)&ctx->d_trace, &ctx->trace_cap, bytes);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(ctx->d_trace, 0, bytes, ctx->stream));
+    const void* fnp = nullptr;
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision == RAPTOR_PREC_MIXED, &fnp);
+    LaunchShape ls = default_shape(ctx, fnp);
+    ls.grid = 1;
+    ls.block = 32;
+    TraceSpec tr{pixel, ctx->d_trace, max_records};
+    rc = enqueue_render(ctx, b, precision == RAPTOR_PREC_MIXED, pixel, pixel + 1, ls, fn, true, tr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(records, ctx->d_trace, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    rc = collect_stats(ctx, true);
+    if (rc) return rc;
+    const long long steps = ctx->stats.steps;
+    *n_records = (int)std::min<long long>(steps + 1, max_records);
+    return RAPTOR_OK;
 }

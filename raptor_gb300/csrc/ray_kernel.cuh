@@ -152,15 +152,38 @@ struct RayState {
     double y[8];
     MksPoint p;
     double beta, thdot_prev;
+    long long rid;
     int steps, turns, stop, img, pix;
     double tau[NF], I[NF];  // FP64 form
     float tf[NF], tc[NF], If[NF], Ic[NF];  // FP32 form (tau, tau compensation, I, I compensation)
 };
 
 template <int NF, bool MIXED>
+__device__ __forceinline__ void trace_record(const TraceSpec& tr, const RayState<NF, MIXED>& s, double dl, int event) {
+    if (s.steps >= tr.cap) return;
+    double* r = tr.out + (long long)s.steps * kTraceWidth;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r[i] = s.y[i];
+    r[8] = dl;
+    if constexpr (MIXED) {
+        r[9] = (double)s.tf[0] + (double)s.tc[0];
+        r[10] = ((double)s.If[0] + (double)s.Ic[0]) * kE2C;
+    } else {
+        r[9] = s.tau[0];
+        r[10] = s.I[0];
+    }
+    r[11] = s.steps;
+    r[12] = s.turns;
+    r[13] = event;
+    r[14] = s.stop;
+    r[15] = 0.0;
+}
+
+template <int NF, bool MIXED>
 __global__ void __launch_bounds__(256)
     ray_kernel(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
-               unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval) {
+               unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval,
+               TraceSpec tr) {
     const int lane = threadIdx.x & 31;
     RayState<NF, MIXED> s;
     bool active = false, live = true;
@@ -183,6 +206,7 @@ __global__ void __launch_bounds__(256)
                     s.img = find_image(imgs, n_imgs, rid);
                     im = imgs + s.img;
                     s.pix = (int)(rid - im->ray_begin);
+                    s.rid = rid;
                     const int px = s.pix % im->width, py = s.pix / im->width;
                     init_photon(*im, px, py, s.y, s.beta);
                     mks_point(s.y[1], s.y[2], im->geo, s.p);
@@ -196,6 +220,7 @@ __global__ void __launch_bounds__(256)
                         s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
                     }
                     active = true;
+                    if (tr.out && rid == tr.ray) trace_record<NF, MIXED>(tr, s, 0.0, 0);
                 } else {
                     live = false;
                 }
@@ -218,8 +243,10 @@ __global__ void __launch_bounds__(256)
                     if (im->integrator == 2) rk2_step(im->geo, s.y, s.p, dl);
                     else rk4_step(im->geo, s.y, s.p, dl);
                     s.steps += 1;
+                    int event = 0;
                     if (s.y[1] > im->stopx1 && s.y[5] < 0.0) {
                         done = true;  // escaped outward (integrator.c:271-272)
+                        event = 3;
                     } else if (s.y[1] < im->stopx1 && s.y[1] > im->startx1 && s.y[2] > im->startx2 &&
                                s.y[2] < im->stopx2) {
                         ++n_rt_calls;
@@ -227,7 +254,9 @@ __global__ void __launch_bounds__(256)
                         if constexpr (MIXED) sampled = rt_sample_fp32<NF>(*im, s.y, s.p, fabs(dl), s.tf, s.tc, s.If, s.Ic);
                         else sampled = rt_sample_fp64<NF>(*im, s.y, s.p, fabs(dl), s.tau, s.I);
                         n_rt_samples += sampled ? 1 : 0;
+                        event = sampled ? 2 : 1;
                     }
+                    if (tr.out && s.rid == tr.ray) trace_record<NF, MIXED>(tr, s, dl, event);
                 }
                 if (done) {
                     // write intensityfield[pix][f] * nu^3 (core.c:136)

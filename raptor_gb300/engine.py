@@ -24,12 +24,13 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 RK4 = 4
 RK2 = 2
+TRACE_WIDTH = 16
 
 STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "DEVICE", -4: "NOMEM", -5: "NODEVICE"}
 
 EXPORTED = ("raptor_gpu_init", "raptor_gpu_destroy", "raptor_gpu_last_error", "raptor_gpu_upload_grid",
             "raptor_gpu_render", "raptor_gpu_render_range", "raptor_gpu_output_size",
-            "raptor_gpu_spectrum_size", "raptor_gpu_get_stats", "raptor_gpu_vjp")
+            "raptor_gpu_spectrum_size", "raptor_gpu_get_stats", "raptor_gpu_vjp", "raptor_gpu_trace_ray")
 
 
 class EngineError(RuntimeError):
@@ -106,6 +107,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.raptor_gpu_spectrum_size.restype = ctypes.c_longlong
     lib.raptor_gpu_get_stats.argtypes = [ctypes.c_void_p, P(Stats)]
     lib.raptor_gpu_vjp.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, P(D), P(D), P(GradC)]
+    lib.raptor_gpu_trace_ray.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         P(D), P(ctypes.c_int)]
     _LIB = lib
     return lib
 
@@ -190,6 +193,14 @@ class Engine:
         s = Stats()
         self._check(self.lib.raptor_gpu_get_stats(self.h, ctypes.byref(s)))
         return s.as_dict()
+
+    def trace_ray(self, img: ImageDesc, pixel: int, precision=PREC_FP64, max_records=4096) -> np.ndarray:
+        """Per-step states of one ray, [n][16] (see raptor_gpu_trace_ray)."""
+        rec = np.zeros((max_records, TRACE_WIDTH))
+        n = ctypes.c_int(0)
+        self._check(self.lib.raptor_gpu_trace_ray(self.h, ctypes.byref(img), precision, pixel, max_records,
+                                                  _dp(rec), ctypes.byref(n)))
+        return rec[:n.value]
 
     def vjp(self, img: ImageDesc, dL_dI: np.ndarray, precision=PREC_FP64, want_fields=True):
         geom = self.grids[img.grid]

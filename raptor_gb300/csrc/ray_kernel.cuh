@@ -44,8 +44,12 @@ __device__ __forceinline__ int find_image(const DevImage* __restrict__ imgs, int
 // Initial photon (metric.c:650-727, GRmath.c:135-184, newtonraphson.c:76-97);
 // the pixel-independent part lives in DevImage.
 __device__ __forceinline__ void init_photon(const DevImage& im, int x, int yy, double y[8], double& beta) {
-    const double alpha = -im.half_x + (x + 0.5) * im.stepx;
-    beta = -im.half_y + (yy + 0.5) * im.stepy;
+    // Impact parameters with the multiply and the add rounded separately, as
+    // the reference computes them (integrator.c:190-191, C99 without FMA
+    // contraction): on the middle row of an odd-height image beta is then
+    // exactly 0, and sign(beta) = 0 selects k_theta = 0 (metric.c:669).
+    const double alpha = __dadd_rn(-im.half_x, __dmul_rn(x + 0.5, im.stepx));
+    beta = __dadd_rn(-im.half_y, __dmul_rn(yy + 0.5, im.stepy));
     const double ll = -alpha * im.sin_mu;
     const double qq = beta * beta + im.mu0sq * (alpha * alpha - 1.0);
     const double sg = (beta < 0.0) ? -1.0 : ((beta > 0.0) ? 1.0 : 0.0);

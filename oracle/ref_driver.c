@@ -113,3 +113,27 @@ double ref_wtime(void) { return omp_get_wtime(); }
 int ref_grid_n1(void) { return N1; }
 int ref_grid_n2(void) { return N2; }
 int ref_int_method(void) { return int_method; }
+
+/* Write the reference's own output files (core.c:154-200) for a given
+ * image, into ./output of the current directory.  field[W*H] holds
+ * intensityfield[k][0]; spectrum is energy_spectrum[0]. */
+int ref_output_files(const double *field, double spectrum, double freq)
+{
+    int npix = IMG_WIDTH * IMG_HEIGHT;
+    real **f = (real **)malloc((size_t)npix * sizeof(real *));
+    real *store = (real *)malloc((size_t)npix * num_indices * sizeof(real));
+    if (!f || !store)
+        return -3;
+    for (int i = 0; i < npix; i++) {
+        f[i] = store + (size_t)i * num_indices;
+        f[i][0] = field[i];
+    }
+    real energy_spectrum[num_indices];
+    real frequencies[num_indices];
+    energy_spectrum[0] = spectrum;
+    frequencies[0] = freq;
+    output_files(f, energy_spectrum, frequencies);
+    free(f);
+    free(store);
+    return 0;
+}

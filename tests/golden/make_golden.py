@@ -156,6 +156,32 @@ def kats(dump_path, n):
                 kat_fluid_X=fx, kat_fluid=fluid, kat_fluid_ok=fok)
 
 
+def ref_output_files(dump, img, spec):
+    """The reference's own output_files (core.c:154-200) for the 32x32 image,
+    run in a scratch directory with relative file names, copied to
+    tests/golden/ref_output/."""
+    import shutil
+    tmp = tempfile.mkdtemp(prefix="rgo_out_", dir="/tmp")
+    harm.write_dump(os.path.join(tmp, "torus64.dump"), dump)
+    model = harm.ModelIn(IMG_WIDTH=32, IMG_HEIGHT=32, FREQ_MIN=230e9, FREQ_MAX=230e9, STEPSIZE=0.05)
+    cwd = os.getcwd()
+    os.chdir(tmp)
+    try:
+        lib = ref.load(64, 64, "RK4")
+        lib.ref_output_files.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double]
+        with quiet():
+            ref.RefSession("torus64.dump", model, 1e19, 60.0, 3.0, 3.0, 1.0, n1=64, n2=64, workdir=tmp)
+            field = np.ascontiguousarray(img, dtype=np.float64)
+            lib.ref_output_files(field.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), spec, 230e9)
+    finally:
+        os.chdir(cwd)
+    dst = os.path.join(OUT, "ref_output")
+    os.makedirs(dst, exist_ok=True)
+    for fn in os.listdir(os.path.join(tmp, "output")):
+        shutil.copy(os.path.join(tmp, "output", fn), os.path.join(dst, fn))
+    model.write(os.path.join(dst, "model.in"))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
@@ -177,6 +203,7 @@ def main():
     res["names"] = np.array(names)
     res.update(kats(p64, 64))
     np.savez_compressed(os.path.join(OUT, "small_g64.npz"), **res)
+    ref_output_files(d64, res["g64_i60_rk4_img"], res["g64_i60_rk4_spec"][0])
 
     # the 100x100 image on the 256x256 torus (RK4, eps 0.05, i = 60, 230 GHz)
     d256, p256 = torus_and_dump(256, tmp)

@@ -172,6 +172,36 @@ int raptor_gpu_trace_ray(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
 int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
                    const double *dL_dI, double *I_out, raptor_grad *grad);
 
+/* ---- Render without allocating device memory ----
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc - an application that embeds the renderer and owns all device
+ * memory through its own pool (a GRMHD code imaging its grid in place between
+ * time steps under a fixed memory budget), or a latency-critical loop that
+ * must not take the allocator's lock and implicit device synchronisation.
+ *
+ * Renders n_imgs (1..RAPTOR_NOALLOC_MAX_IMAGES) FP64 images of one grid, as
+ * raptor_gpu_render does, without a context and without allocating:
+ *   d_cells         device memory, the grid as float64 [n1][n2][8] (the eight
+ *                   primitives of a cell contiguous, in HARM order)
+ *   geom            the grid geometry (imgs[k].grid is ignored)
+ *   d_I_out         device memory, raptor_gpu_output_size(imgs, n_imgs) doubles
+ *   d_spectrum_out  device memory, raptor_gpu_spectrum_size doubles, or NULL
+ *   stream          a cudaStream_t, or NULL for the default stream
+ * Returns when the results are in device memory.  Its scratch (ray queue,
+ * counters, descriptors: RAPTOR_NOALLOC_SCRATCH_BYTES) is one fixed device
+ * array in the library that every GPU loading the library keeps until exit;
+ * its device address is looked up on the first call on each device, so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls whose GPU work overlaps race on it and must be serialised by the
+ * caller.  A batch larger than RAPTOR_NOALLOC_MAX_IMAGES is rejected with
+ * RAPTOR_ERR_NOALLOC_LIMIT; other bad arguments with RAPTOR_ERR_INVALID. */
+#define RAPTOR_NOALLOC_MAX_IMAGES 16
+#define RAPTOR_NOALLOC_SCRATCH_BYTES 16384
+#define RAPTOR_ERR_NOALLOC_LIMIT (-6)
+int raptor_gpu_render_noalloc(int device, const double *d_cells, const raptor_grid_geom *geom,
+                              const raptor_image_desc *imgs, int n_imgs, double *d_I_out, double *d_spectrum_out,
+                              void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256)
 // Spectrum: core.c:146-150 sums intensityfield over pixels per frequency.
 // One block per (image, frequency) in a fixed-order tree, so the result is
 // deterministic.  spec_img[s], spec_f[s] map spectrum slot s to its source.
-__global__ void spectrum_kernel(const DevImage* __restrict__ imgs, const int* __restrict__ spec_img,
+static __global__ void spectrum_kernel(const DevImage* __restrict__ imgs, const int* __restrict__ spec_img,
                                 const int* __restrict__ spec_f, const double* __restrict__ out,
                                 double* __restrict__ spectrum) {
     __shared__ double red[256];

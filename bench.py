@@ -110,7 +110,7 @@ def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, re
     kind = "port"
     threads = nthreads or os.cpu_count() or 1
     sess = None
-    if ref.available(GRID_N, GRID_N):
+    if ref.available(GRID_N, GRID_N, opt="stock"):
         try:
             import tempfile
             from raptor_gb300 import harm
@@ -120,7 +120,8 @@ def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, re
             harm.write_dump(path, dump)
             model = harm.ModelIn(IMG_WIDTH=W, IMG_HEIGHT=H, FREQ_MIN=FREQ, FREQ_MAX=FREQ, STEPSIZE=EPS)
             with quiet():
-                sess = ref.RefSession(path, model, 1e19, INCL, 3.0, 3.0, 0.0, n1=GRID_N, n2=GRID_N, workdir=tmp)
+                sess = ref.RefSession(path, model, 1e19, INCL, 3.0, 3.0, 0.0, n1=GRID_N, n2=GRID_N, workdir=tmp,
+                                      opt="stock")
             kind = "reference"
         except Exception:
             sess = None

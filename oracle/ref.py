@@ -2,7 +2,9 @@
 infrastructure).
 
 The shared library is the reference's own C sources, compiled unmodified by
-oracle/Makefile with compile-time overrides (ref_config.h).  This module is
+oracle/Makefile with compile-time overrides (ref_config.h).  opt="ieee" (-O2,
+the source's IEEE semantics) is the parity oracle; opt="stock" (-Ofast, the
+reference makefile's flags) is only timed.  This module is
 imported only by tests/, by tests/golden/make_golden.py and by bench.py's
 CPU-baseline leg; the engine never calls it.
 
@@ -29,37 +31,37 @@ def sources_present() -> bool:
     return os.path.isfile(os.path.join(REF_SRC_DIR, "integrator.c"))
 
 
-def lib_path(n1: int, n2: int, rk: str = "RK4") -> str:
-    return os.path.join(HERE, "_ref", f"libraptor_ref_{n1}x{n2}_{rk}.so")
+def lib_path(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> str:
+    return os.path.join(HERE, "_ref", f"libraptor_ref_{n1}x{n2}_{rk}_{opt}.so")
 
 
-def build(n1: int, n2: int, rk: str = "RK4") -> str:
-    path = lib_path(n1, n2, rk)
+def build(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> str:
+    path = lib_path(n1, n2, rk, opt)
     if not os.path.exists(path):
         if not sources_present():
             raise FileNotFoundError("reference sources are not present on this machine")
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"N1={n1}", f"N2={n2}", f"RK={rk}",
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"N1={n1}", f"N2={n2}", f"RK={rk}", f"OPT={opt}",
                         f"REFDIR={REF_SRC_DIR}"], check=True)
     return path
 
 
-def available(n1: int, n2: int, rk: str = "RK4") -> bool:
+def available(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> bool:
     """True if a reference library for this grid can be loaded here."""
-    path = lib_path(n1, n2, rk)
+    path = lib_path(n1, n2, rk, opt)
     if not os.path.exists(path) and not sources_present():
         return False
     try:
-        load(n1, n2, rk)
+        load(n1, n2, rk, opt)
         return True
     except OSError:
         return False
 
 
-def load(n1: int, n2: int, rk: str = "RK4") -> ctypes.CDLL:
-    key = (n1, n2, rk)
+def load(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> ctypes.CDLL:
+    key = (n1, n2, rk, opt)
     if key in _LIBS:
         return _LIBS[key]
-    lib = ctypes.CDLL(build(n1, n2, rk), mode=ctypes.RTLD_LOCAL)
+    lib = ctypes.CDLL(build(n1, n2, rk, opt), mode=ctypes.RTLD_LOCAL)
     D = ctypes.c_double
     P = ctypes.POINTER
     lib.ref_setup.argtypes = [ctypes.c_char_p, ctypes.c_char_p, D, D, D, D, D]
@@ -83,7 +85,7 @@ class RefSession:
     list with OpenMP."""
 
     def __init__(self, dump_path: str, model, m_unit: float, inclination: float,
-                 r_high: float, r_low: float, time_init: float = 0.0, rk: str = "RK4",
+                 r_high: float, r_low: float, time_init: float = 0.0, rk: str = "RK4", opt: str = "ieee",
                  n1: int | None = None, n2: int | None = None, workdir: str | None = None):
         from raptor_gb300.harm import read_dump
         if n1 is None:
@@ -92,7 +94,7 @@ class RefSession:
             n1, n2 = int(head[1]), int(head[2])
         self.n1, self.n2 = n1, n2
         self.model = model
-        self.lib = load(n1, n2, rk)
+        self.lib = load(n1, n2, rk, opt)
         self._tmp = tempfile.mkdtemp(prefix="rgo_", dir=workdir or "/tmp")
         self.model_path = os.path.join(self._tmp, "model.in")
         model.write(self.model_path)

@@ -145,3 +145,23 @@ def test_invalid_arguments_are_rejected(eng, torus64):
     # the context stays usable after rejected calls
     img, _ = eng.render(engine.image_desc(4, 4, [230e9], grid=gid))
     assert np.all(np.isfinite(img))
+
+
+@pytest.mark.parametrize("incl", [60.0, 17.0])
+def test_1024_on_512_against_reference(eng, incl):
+    """Full-size images (BASELINE configuration 2): the reference rendered the
+    1024x1024 image of the 512x512 torus here with 8 threads; the fixture keeps
+    its flux and a strided 17,190-pixel subsample."""
+    from raptor_gb300 import engine, synth
+    g = load_golden("img1024_g512_sub.npz")
+    from tests.golden.make_golden import prim_checksum
+    d = synth.make_torus(n1=512, n2=512)
+    np.testing.assert_allclose(prim_checksum(d.prims), g["prim_checksum"], rtol=1e-12)
+    gid = eng.upload_grid(d.geom, d.prims)
+    desc = engine.image_desc(1024, 1024, [230e9], grid=gid, inclination=incl)
+    tag = f"i{int(incl)}"
+    img, spec = eng.render(desc, engine.PREC_FP64)
+    assert_fp64_parity(img[g[f"{tag}_sub_pixels"]], g[f"{tag}_sub_vals"], f"1024 {tag} subsample")
+    assert abs(spec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= 1e-6
+    mimg, mspec = eng.render(desc, engine.PREC_MIXED)
+    assert abs(mspec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= FLUX_RTOL_MIXED

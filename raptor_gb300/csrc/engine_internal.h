@@ -26,6 +26,7 @@ struct GridSlot {
     double* c64 = nullptr;
     float* c32 = nullptr;
     double* staging = nullptr;
+    long long cap_cells = 0;  // cells the buffers hold
 };
 
 struct Batch {

@@ -114,6 +114,7 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
     im.geo.R0 = g.R0;
     im.geo.one_m_h = 1.0 - g.hslope;
     im.geo.half_1mh = 0.5 * (1.0 - g.hslope);
+    im.geo.th_coef = (1.0 - g.hslope) / (2.0 * M_PI);
 
     // camera grid (integrator.c:188-191)
     im.stepx = d.cam_size_x / (double)d.width;
@@ -272,6 +273,7 @@ extern "C" int raptor_gpu_upload_grid(raptor_gpu_ctx* ctx, const double* prims, 
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "hslope %g outside [0, 2): theta(x2) would not be monotone", g.hslope);
     auto t0 = std::chrono::steady_clock::now();
     CK(cudaSetDevice(ctx->device));
+    cudaGetLastError();  // a failed earlier call must not fail this one
     int id = *grid_id;
     if (id >= 0) {
         if (id >= RAPTOR_MAX_GRIDS || !ctx->grids[id].used)
@@ -293,6 +295,12 @@ extern "C" int raptor_gpu_upload_grid(raptor_gpu_ctx* ctx, const double* prims, 
     }
     GridSlot& s = ctx->grids[id];
     const long long ncell = (long long)g.n1 * g.n2;
+    if (s.c64 && s.cap_cells < ncell) {  // a released slot keeps its buffers; grow them if too small
+        cudaFree(s.c64);
+        cudaFree(s.c32);
+        cudaFree(s.staging);
+        s = GridSlot();
+    }
     if (!s.c64) {
         if (cudaMalloc(&s.c64, ncell * 8 * sizeof(double)) != cudaSuccess ||
             cudaMalloc(&s.c32, ncell * 8 * sizeof(float)) != cudaSuccess ||
@@ -304,6 +312,7 @@ extern "C" int raptor_gpu_upload_grid(raptor_gpu_ctx* ctx, const double* prims, 
             s = GridSlot();
             return ctx_fail(ctx, RAPTOR_ERR_NOMEM, "grid allocation failed");
         }
+        s.cap_cells = ncell;
     }
     s.used = true;
     s.geom = g;
@@ -415,15 +424,16 @@ int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs
 
 LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn) {
     LaunchShape ls;
-    ls.block = ctx->opt.block_size > 0 ? ctx->opt.block_size : 128;
-    ls.block = std::max(32, std::min(256, ls.block / 32 * 32));
+    ls.block = ctx->opt.block_size > 0 ? ctx->opt.block_size : kRayMaxBlock;
+    ls.block = std::max(32, std::min(kRayMaxBlock, ls.block / 32 * 32));
     int occ = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, ls.block, 0);
     occ = std::max(occ, 1);
     int bps = ctx->opt.blocks_per_sm > 0 ? std::min(ctx->opt.blocks_per_sm, occ) : occ;
     ls.grid = ctx->num_sms * bps;
     ls.bps = bps;
-    ls.refill = ctx->opt.refill_interval > 0 ? ctx->opt.refill_interval : 1;
+    // lanes refill every 8 steps: measured 1.3 % faster than every step at 1024^2
+    ls.refill = ctx->opt.refill_interval > 0 ? ctx->opt.refill_interval : 8;
     return ls;
 }
 
@@ -478,6 +488,7 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "precision %d unknown", precision);
     CK(cudaSetDevice(ctx->device));
+    cudaGetLastError();  // a failed earlier call must not fail this one
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, imgs, n_imgs, b);
     if (rc) return rc;
@@ -540,6 +551,7 @@ extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc
     if (pixel < 0 || (long long)pixel >= (long long)img->width * img->height)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "pixel %d outside the %dx%d image", pixel, img->width, img->height);
     CK(cudaSetDevice(ctx->device));
+    cudaGetLastError();  // a failed earlier call must not fail this one
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, img, 1, b);
     if (rc) return rc;

@@ -41,46 +41,66 @@ __device__ __forceinline__ int find_image(const DevImage* __restrict__ imgs, int
     return lo;
 }
 
+// The inclination-dependent camera constants of initialize_photon
+// (metric.c:652-692, 722-725): plain values for the forward kernels, values
+// with their inclination tangent for the adjoint.
+template <class R>
+struct CamT {
+    R sin_mu, mu0sq, cc_over_sc, cosc2;
+    R g11, gu00, gu03, gu33, gu22;
+    R x2c, k2fac;
+};
+
+__device__ __forceinline__ CamT<double> camera_of(const DevImage& im) {
+    return CamT<double>{im.sin_mu, im.mu0sq, im.cc_over_sc, im.cosc2, im.g11, im.gu00,
+                        im.gu03,   im.gu33,  im.gu22,       im.xcam[2], im.k2fac};
+}
+
 // Initial photon (metric.c:650-727, GRmath.c:135-184, newtonraphson.c:76-97);
-// the pixel-independent part lives in DevImage.
-__device__ __forceinline__ void init_photon(const DevImage& im, int x, int yy, double y[8], double& beta) {
+// the pixel-independent part lives in DevImage / CamT.
+template <class R>
+__device__ __forceinline__ void init_photon(const DevImage& im, const CamT<R>& cam, int x, int yy, R y[8],
+                                            double& beta) {
     // Impact parameters with the multiply and the add rounded separately, as
     // the reference computes them (integrator.c:190-191, C99 without FMA
     // contraction): on the middle row of an odd-height image beta is then
     // exactly 0, and sign(beta) = 0 selects k_theta = 0 (metric.c:669).
     const double alpha = __dadd_rn(-im.half_x, __dmul_rn(x + 0.5, im.stepx));
     beta = __dadd_rn(-im.half_y, __dmul_rn(yy + 0.5, im.stepy));
-    const double ll = -alpha * im.sin_mu;
-    const double qq = beta * beta + im.mu0sq * (alpha * alpha - 1.0);
+    const R ll = -alpha * cam.sin_mu;
+    const R qq = beta * beta + cam.mu0sq * (alpha * alpha - 1.0);
     const double sg = (beta < 0.0) ? -1.0 : ((beta > 0.0) ? 1.0 : 0.0);
-    const double kd2 = sg * sqrt(fabs(qq - ll * ll * im.cc_over_sc + im.cosc2));
-    const double kd0 = -1.0, kd3 = ll;
-    const double ku0 = im.gu00 * kd0 + im.gu03 * kd3;
-    const double ku3 = im.gu33 * kd3 + im.gu03 * kd0;
-    const double ku2 = im.gu22 * kd2;
-    const double ku1 = sqrt((-ku0 * kd0 - ku2 * kd2 - ku3 * kd3) / im.g11);
+    const R kd2 = sg * sqrt(fabs(qq - ll * ll * cam.cc_over_sc + cam.cosc2));
+    const double kd0 = -1.0;
+    const R kd3 = ll;
+    const R ku0 = cam.gu00 * kd0 + cam.gu03 * kd3;
+    const R ku3 = cam.gu33 * kd3 + cam.gu03 * kd0;
+    const R ku2 = cam.gu22 * kd2;
+    const R ku1 = sqrt((-ku0 * kd0 - ku2 * kd2 - ku3 * kd3) / cam.g11);
     y[0] = im.xcam[0];
     y[1] = im.xcam[1];
-    y[2] = im.xcam[2];
+    y[2] = cam.x2c;
     y[3] = im.xcam[3];
     y[4] = ku0 + im.t01 * ku1;
     y[5] = ku1;
-    y[6] = ku2 / im.k2fac;
+    y[6] = ku2 / cam.k2fac;
     y[7] = im.t31 * ku1 + ku3;
 }
 
 // stepsize (integrator.c:109-122) with the reciprocals folded:
 // 1/(eps/|k|) = |k|/eps; the tiny^2 guards keep the reference's limits.
-__device__ __forceinline__ double step_size(const DevImage& im, const double y[8]) {
+template <class R>
+__device__ __forceinline__ R step_size(const DevImage& im, const R y[8]) {
     const double t = 1.e-40;
-    const double m2 = fmin(y[2], 1.0 - y[2]);
-    const double i1 = (fabs(y[5]) + t) * im.inv_stepsize;
-    const double i2 = (fabs(y[6]) + t) * im.inv_stepsize / m2;
-    const double i3 = (fabs(y[7]) + t) * im.inv_stepsize;
+    const R m2 = fmin(y[2], 1.0 - y[2]);
+    const R i1 = (fabs(y[5]) + t) * im.inv_stepsize;
+    const R i2 = (fabs(y[6]) + t) * im.inv_stepsize / m2;
+    const R i3 = (fabs(y[7]) + t) * im.inv_stepsize;
     return -fmax(1.0 / (i1 + i2 + i3), 1e-12);
 }
 
-__device__ __forceinline__ void rhs(const MksPoint& p, const Geo& g, const double ys[8], double f[8]) {
+template <class R>
+__device__ __forceinline__ void rhs(const MksPointT<R>& p, const Geo& g, const R ys[8], R f[8]) {
     f[0] = ys[4];
     f[1] = ys[5];
     f[2] = ys[6];
@@ -91,49 +111,46 @@ __device__ __forceinline__ void rhs(const MksPoint& p, const Geo& g, const doubl
 // One RK4 step (integrator.c:13-41): stage weights 1/2, 1/2, 1 and
 // y += (k1 + 2 k2 + 2 k3 + k4)/6 summed in the reference's order.
 // p holds the point at y on entry and at the new y on exit.
-__device__ __forceinline__ void rk4_step(const Geo& g, double y[8], MksPoint& p, double dt) {
-    double acc[8], ys[8], f[8];
+// Stages 2-4 run as one rolled loop: the stage body (point transcendentals,
+// 40 Christoffels, contraction) is large, and one copy of it instead of
+// three keeps the kernel's hot loop inside the instruction cache.
+template <class R>
+__device__ __forceinline__ void rk4_step(const Geo& g, R y[8], MksPointT<R>& p, R dt) {
+    R acc[8], ys[8], f[8];
     rhs(p, g, y, f);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const double d = dt * f[i];
+        const R d = dt * f[i];
         acc[i] = d;
         ys[i] = y[i] + d * 0.5;
     }
-    MksPoint q;
-    mks_point(ys[1], ys[2], g, q);
-    rhs(q, g, ys, f);
+#pragma unroll 1
+    for (int q = 1; q < 4; ++q) {
+        MksPointT<R> qp;
+        mks_point(ys[1], ys[2], g, qp);
+        rhs(qp, g, ys, f);
+        const double wacc = (q == 3) ? 1.0 : 2.0;   // k2, k3 count twice
+        const double wnext = (q == 1) ? 0.5 : 1.0;  // stage weights 1/2, 1/2, 1
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const double d = dt * f[i];
-        acc[i] = acc[i] + d * 2.0;
-        ys[i] = y[i] + d * 0.5;
+        for (int i = 0; i < 8; ++i) {
+            const R d = dt * f[i];
+            acc[i] = acc[i] + d * wacc;
+            ys[i] = y[i] + d * wnext;
+        }
     }
-    mks_point(ys[1], ys[2], g, q);
-    rhs(q, g, ys, f);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const double d = dt * f[i];
-        acc[i] = acc[i] + d * 2.0;
-        ys[i] = y[i] + d;
-    }
-    mks_point(ys[1], ys[2], g, q);
-    rhs(q, g, ys, f);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        acc[i] = acc[i] + dt * f[i];
-        y[i] = y[i] + 1.0 / 6.0 * acc[i];
-    }
+    for (int i = 0; i < 8; ++i) y[i] = y[i] + 1.0 / 6.0 * acc[i];
     mks_point(y[1], y[2], g, p);
 }
 
 // RK2 midpoint step (integrator.c:44-70).
-__device__ __forceinline__ void rk2_step(const Geo& g, double y[8], MksPoint& p, double dt) {
-    double ys[8], f[8];
+template <class R>
+__device__ __forceinline__ void rk2_step(const Geo& g, R y[8], MksPointT<R>& p, R dt) {
+    R ys[8], f[8];
     rhs(p, g, y, f);
 #pragma unroll
     for (int i = 0; i < 8; ++i) ys[i] = y[i] + dt * f[i] * 0.5;
-    MksPoint q;
+    MksPointT<R> q;
     mks_point(ys[1], ys[2], g, q);
     rhs(q, g, ys, f);
 #pragma unroll
@@ -183,8 +200,17 @@ __device__ __forceinline__ void trace_record(const TraceSpec& tr, const RayState
     r[15] = 0.0;
 }
 
+// Launch bounds: blocks of at most 128 threads, at least kRayMinBlocks
+// resident per SM, so the register budget (<= 168 per thread at 3) keeps
+// 12 warps per SM to hide FP64 latency.
+#ifndef RAPTOR_RAY_MIN_BLOCKS
+#define RAPTOR_RAY_MIN_BLOCKS 3
+#endif
+constexpr int kRayMaxBlock = 128;
+constexpr int kRayMinBlocks = RAPTOR_RAY_MIN_BLOCKS;
+
 template <int NF, bool MIXED>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
     ray_kernel(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
                unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval,
                TraceSpec tr) {
@@ -212,7 +238,7 @@ __global__ void __launch_bounds__(256)
                     s.pix = (int)(rid - im->ray_begin);
                     s.rid = rid;
                     const int px = s.pix % im->width, py = s.pix / im->width;
-                    init_photon(*im, px, py, s.y, s.beta);
+                    init_photon(*im, camera_of(*im), px, py, s.y, s.beta);
                     mks_point(s.y[1], s.y[2], im->geo, s.p);
                     s.steps = 0;
                     s.turns = 0;

@@ -1,0 +1,23 @@
+"""The engine's table-driven FP64 exp and sincospi (csrc/fp64_math.cuh)
+against CUDA's exp and sincospi, on the GPU: <= 2 ulp, and sin/cos within
+2.3e-16 absolute near their zeros (where ulp counts are meaningless)."""
+import os
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_fast_math_against_cuda(tmp_path):
+    from raptor_gb300 import build
+    exe = str(tmp_path / "gpu_math_check")
+    subprocess.run([build.nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "-I" + os.path.join(ROOT, "raptor_gb300", "csrc"), os.path.join(ROOT, "tests", "gpu_math_check.cu"),
+                    "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    vals = dict(zip(out[0::2], out[1::2]))
+    assert vals["err"] == "no"
+    assert float(vals["exp_ulp"]) <= 2
+    assert float(vals["sin_abs"]) <= 2.3e-16 and float(vals["cos_abs"]) <= 2.3e-16

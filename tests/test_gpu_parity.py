@@ -20,6 +20,14 @@ def eng():
     e.close()
 
 
+def _grid(eng, dump):
+    """Upload each dump once per engine (the context holds 16 grid slots)."""
+    cache = eng.__dict__.setdefault("_test_grids", {})
+    if id(dump) not in cache:
+        cache[id(dump)] = eng.upload_grid(dump.geom, dump.prims)
+    return cache[id(dump)]
+
+
 @pytest.fixture(scope="module")
 def small():
     return load_golden("small_g64.npz")
@@ -38,7 +46,7 @@ NAMES = ["g64_i60_rk4", "g64_i17_rk4", "g64_i120_rk4_86", "g64_i60_rk2", "g64_i3
 @pytest.mark.parametrize("name", NAMES)
 def test_fp64_matches_reference_small(eng, torus64, small, name):
     from raptor_gb300 import engine
-    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    gid = _grid(eng, torus64)
     img, spec = eng.render(_desc(small[f"{name}_params"], gid), engine.PREC_FP64)
     assert_fp64_parity(img, small[f"{name}_img"], name)
     assert spec[0] == pytest.approx(small[f"{name}_spec"][0], rel=1e-6)
@@ -49,7 +57,7 @@ def test_fp64_matches_reference_small(eng, torus64, small, name):
 def test_fp64_matches_reference_100x100_on_256(eng, torus256):
     from raptor_gb300 import engine
     g = load_golden("img100_g256.npz")
-    gid = eng.upload_grid(torus256.geom, torus256.prims)
+    gid = _grid(eng, torus256)
     img, spec = eng.render(_desc(g["params"], gid), engine.PREC_FP64)
     assert_fp64_parity(img, g["img"], "100x100 on 256^2")
     assert spec[0] == pytest.approx(g["spec"][0], rel=1e-6)
@@ -59,7 +67,7 @@ def test_fp64_matches_port_and_step_counts(eng, torus64):
     """Step and sample counters agree with the oracle's, ray by ray in sum."""
     from oracle import port
     from raptor_gb300 import engine
-    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    gid = _grid(eng, torus64)
     d = engine.image_desc(20, 20, [230e9, 86e9], grid=gid, inclination=45.0)
     img, _ = eng.render(d, engine.PREC_FP64)
     st = eng.stats()
@@ -74,7 +82,7 @@ def test_fp64_matches_port_and_step_counts(eng, torus64):
 def test_mixed_flux_within_1e4(eng, torus256):
     from raptor_gb300 import engine
     g = load_golden("img100_g256.npz")
-    gid = eng.upload_grid(torus256.geom, torus256.prims)
+    gid = _grid(eng, torus256)
     img, spec = eng.render(_desc(g["params"], gid), engine.PREC_MIXED)
     ref_flux = g["spec"][0]
     assert abs(spec[0] - ref_flux) / ref_flux <= FLUX_RTOL_MIXED
@@ -84,7 +92,7 @@ def test_mixed_flux_within_1e4(eng, torus256):
 
 def test_deterministic(eng, torus64):
     from raptor_gb300 import engine
-    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    gid = _grid(eng, torus64)
     d = engine.image_desc(24, 24, [230e9], grid=gid)
     a, sa = eng.render(d, engine.PREC_FP64)
     b, sb = eng.render(d, engine.PREC_FP64)
@@ -99,7 +107,7 @@ def test_batch_equals_single_images(eng, torus64):
     batches of one-frequency images use the same instantiation and agree
     exactly."""
     from raptor_gb300 import engine
-    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    gid = _grid(eng, torus64)
     descs = [engine.image_desc(17, 9, [230e9], grid=gid, inclination=30.0),
              engine.image_desc(8, 12, [86e9, 345e9], grid=gid, inclination=150.0, m_unit=5e18),
              engine.image_desc(5, 5, [230e9], grid=gid, inclination=90.0, integrator=engine.RK2)]
@@ -121,7 +129,7 @@ def test_batch_equals_single_images(eng, torus64):
 
 def test_range_render_is_a_slice(eng, torus64):
     from raptor_gb300 import engine
-    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    gid = _grid(eng, torus64)
     d = engine.image_desc(16, 16, [230e9], grid=gid)
     full, _ = eng.render(d, engine.PREC_FP64)
     part, _ = eng.render(d, engine.PREC_FP64, ray_begin=37, ray_count=100)
@@ -131,7 +139,7 @@ def test_range_render_is_a_slice(eng, torus64):
 
 def test_invalid_arguments_are_rejected(eng, torus64):
     from raptor_gb300 import engine
-    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    gid = _grid(eng, torus64)
     with pytest.raises(engine.EngineError):
         eng.render(engine.image_desc(4, 4, [230e9], grid=gid + 5))
     with pytest.raises(engine.EngineError):

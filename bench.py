@@ -180,6 +180,161 @@ def workload_config():
             "integrator": "RK4", "l2": "flushed between timed renders (512 MiB write)"}
 
 
+def run_vjp_config4(reps=3):
+    """Adjoint configuration: 256x256 image of the 256x256 torus, loss = L2
+    distance to a target at M_unit x 1.3, R = 4, i = 62 deg.  Reports the
+    FP64 forward and VJP (forward pass + adjoint pass) device times."""
+    from raptor_gb300 import engine, synth
+    d = synth.make_torus(n1=256, n2=256)
+    eng = engine.Engine()
+    gid = eng.upload_grid(d.geom, d.prims)
+    desc = engine.image_desc(256, 256, [FREQ], grid=gid, inclination=60.0)
+    target, _ = eng.render(engine.image_desc(256, 256, [FREQ], grid=gid, inclination=62.0, m_unit=1.3e19,
+                                             r_high=4.0, r_low=4.0), engine.PREC_FP64)
+    fwd, vjp, grads = [], [], None
+    for _ in range(reps):
+        img, _ = eng.render(desc, engine.PREC_FP64)
+        fwd.append(eng.stats()["device_ms"])
+        _, grads = eng.vjp(desc, img - target, engine.PREC_FP64)
+        vjp.append(eng.stats()["device_ms"])
+    eng.close()
+    f, v = min(fwd), min(vjp)
+    return {"config": "256x256 image, 256x256 torus, i=60, 230 GHz; loss to target at M_unit*1.3, R=4, i=62",
+            "fwd_ms": f, "vjp_ms": v, "ratio": v / f,
+            "grad": {k: grads[k] for k in ("d_m_unit", "d_r_high", "d_r_low", "d_inclination")}}
+
+
+def run_batch_config3(dev):
+    """Batched configuration: 64 images (32x128^2, 24x256^2, 6x512^2,
+    2x1024^2) over two 256x256 dumps, seeded angles/frequencies/M_unit: one
+    graph-replayed persistent launch with the autotuned shape, against 64
+    sequential plain renders."""
+    from raptor_gb300 import engine, workloads
+    dumps = workloads.batch_dumps(256)
+    g_eng = engine.Engine(device=dev, use_graph=1, autotune=1)
+    gids = [g_eng.upload_grid(d.geom, d.prims) for d in dumps]
+    descs = workloads.batch_images(gids)
+    g_eng.render(descs, engine.PREC_FP64)  # tunes the shape and captures the graph
+    t0 = time.perf_counter()
+    g_eng.render(descs, engine.PREC_FP64)
+    wall_batch = (time.perf_counter() - t0) * 1e3
+    st = g_eng.stats()
+    p_eng = engine.Engine(device=dev)
+    for d in dumps:
+        p_eng.upload_grid(d.geom, d.prims)
+    seq_dev = 0.0
+    t0 = time.perf_counter()
+    for d in descs:
+        p_eng.render(d, engine.PREC_FP64)
+        seq_dev += p_eng.stats()["device_ms"]
+    wall_seq = (time.perf_counter() - t0) * 1e3
+    g_eng.close()
+    p_eng.close()
+    return {"images": len(descs), "rays": st["rays"], "graph_replayed": st["graph_replayed"],
+            "launch": [st["block_size"], st["blocks_per_sm"], st["refill_interval"]],
+            "batched_device_ms": st["device_ms"], "batched_wall_ms": wall_batch,
+            "sequential_device_ms": seq_dev, "sequential_wall_ms": wall_seq,
+            "speedup_wall": wall_seq / wall_batch, "rays_per_s": st["rays"] / (st["device_ms"] * 1e-3)}
+
+
+def _loss_delta(op, om, target):
+    """L(O+) - L(O-) for L = 1/2 sum (O - target)^2, without the cancellation
+    of subtracting two large sums."""
+    return 0.5 * float(np.sum((op - om) * (op + om - 2.0 * target)))
+
+
+def run_differentiable(dev, n_cells=4, reps=2):
+    """Large differentiable batch: a 2048x2048 image at 86/140/230/345/690 GHz
+    (with its spectrum) of the 512x512 torus.  Forward in the mixed form, then
+    the VJP of L = 1/2 |O - O_target|^2 (target at M_unit x 1.3, R = 4,
+    i = 62 deg) with respect to the scalars and the per-cell rho, u and
+    ln Theta_e fields.  Reports the forward and adjoint device times, the
+    engine's peak device memory, and agreement with central differences of
+    the FP64 forward (Richardson-extrapolated for the inclination) on the four
+    scalars and on rho and u of the n_cells cells with the largest gradient."""
+    from raptor_gb300 import engine
+    d = make_scene()
+    freqs = [86e9, 140e9, 230e9, 345e9, 690e9]
+    n = 2048
+    base = dict(m_unit=1e19, r_high=3.0, r_low=3.0, inclination=60.0)
+    eng = engine.Engine(device=dev)
+    gid = eng.upload_grid(d.geom, d.prims)
+    mk = lambda **o: engine.image_desc(n, n, freqs, grid=gid, **dict(base, **o))  # noqa: E731
+    target, _ = eng.render(mk(m_unit=1.3e19, r_high=4.0, r_low=4.0, inclination=62.0), engine.PREC_MIXED)
+    fwd_ms = []
+    for _ in range(reps):
+        img, spec = eng.render(mk(), engine.PREC_MIXED)
+        fwd_ms.append(eng.stats()["device_ms"])
+    dl = img - target
+    adj_ms, vjp_ms = [], []
+    for _ in range(reps):
+        _, g = eng.vjp(mk(), dl, engine.PREC_MIXED)
+        st = eng.stats()
+        adj_ms.append(st["kernel_ms"])
+        vjp_ms.append(st["device_ms"])
+    peak = eng.stats()["peak_device_bytes"]
+
+    # finite differences of the FP64 forward
+    def fd_scalar(key, rel, richardson):
+        diffs = []
+        for r in ((rel, rel / 2) if richardson else (rel,)):
+            h = r * base[key]
+            op, _ = eng.render(mk(**{key: base[key] + h}), engine.PREC_FP64)
+            om, _ = eng.render(mk(**{key: base[key] - h}), engine.PREC_FP64)
+            diffs.append(_loss_delta(op, om, target) / (2 * h))
+        return diffs[0] if not richardson else (4 * diffs[1] - diffs[0]) / 3
+
+    t0 = time.perf_counter()
+    scal = {}
+    for key, gk in (("m_unit", "d_m_unit"), ("r_high", "d_r_high"), ("r_low", "d_r_low"),
+                    ("inclination", "d_inclination")):
+        fd = fd_scalar(key, 1e-4, key == "inclination")
+        scal[key] = {"vjp": g[gk], "fd": fd, "rel_err": abs(g[gk] - fd) / abs(fd)}
+    cells = {}
+    order = np.argsort(-np.abs(g["d_rho"]).ravel())[:n_cells]
+    fd_all, vjp_all = [], []
+    for flat in order:
+        i, j = divmod(int(flat), d.geom.n2)
+        for q, field in ((0, "d_rho"), (1, "d_u")):
+            pr = d.prims.copy()
+            v = pr[q, i, j]
+            pr[q, i, j] = v * (1 + 1e-4)
+            eng.upload_grid(d.geom, pr, grid_id=gid)
+            op, _ = eng.render(mk(), engine.PREC_FP64)
+            pr[q, i, j] = v * (1 - 1e-4)
+            eng.upload_grid(d.geom, pr, grid_id=gid)
+            om, _ = eng.render(mk(), engine.PREC_FP64)
+            fd = _loss_delta(op, om, target) / (2e-4 * v)
+            cells[f"{field}[{i},{j}]"] = {"vjp": float(g[field][i, j]), "fd": fd}
+            fd_all.append(fd)
+            vjp_all.append(float(g[field][i, j]))
+    eng.upload_grid(d.geom, d.prims, grid_id=gid)
+    fd_s = time.perf_counter() - t0
+    scale = max(abs(x) for x in fd_all)
+    cell_err = max(abs(a - b) for a, b in zip(vjp_all, fd_all)) / scale
+    # uniform Theta_e factor = change of T_p/T_e at R_high = R_low = R
+    R = base["r_high"]
+    tg = 0.5 * ((1.0 + 2.0 / 3.0 * (R + 1.0) / (R + 2.0)) + 4.0 / 3.0)
+    dlnT_dR = (1.0 / 3.0) / (R + 2.0) ** 2 / (tg - 1.0) - 1.0 / (1.0 + R)
+    th_sum = float(np.sum(g["d_lnthetae"]))
+    th_want = (g["d_r_high"] + g["d_r_low"]) / dlnT_dR
+    eng.close()
+    f, a, v = min(fwd_ms), min(adj_ms), min(vjp_ms)
+    return {
+        "metric": "2048² x 5-frequency differentiable render: adjoint/forward time, peak device memory, "
+                  "finite-difference agreement",
+        "config": {"workload": "2048x2048 image at 86/140/230/345/690 GHz with spectrum, 512x512 torus a=0.9375, "
+                               "i=60, M_unit=1e19, R_high=R_low=3; loss to target at M_unit*1.3, R=4, i=62",
+                   "forward": "mixed", "adjoint": "fp64 (forward-mode tangents + suffix identity, no checkpoints)"},
+        "forward_ms": f, "adjoint_kernel_ms": a, "vjp_total_ms": v, "adjoint_over_forward": a / f,
+        "vjp_total_over_forward": v / f, "peak_device_bytes": peak,
+        "grad_values": int(3 * d.geom.n1 * d.geom.n2 + 4),
+        "fd": {"scalars": scal, "cells": cells, "cell_max_err_over_scale": cell_err,
+               "thetae_field_sum": th_sum, "thetae_sum_identity": th_want,
+               "thetae_rel_err": abs(th_sum - th_want) / abs(th_want), "seconds": fd_s},
+    }
+
+
 def run_engine(args, rank, world, local):
     from raptor_gb300 import engine
     dev = local
@@ -281,19 +436,10 @@ def run_engine(args, rank, world, local):
     flop = workload.image_flops(st["rays"], st["steps"], st["rt_samples"], 1, rk4=True)
     achieved = flop / (k_fp64 * 1e-3) / 1e12
 
-    # VJP / forward ratio (if the adjoint is available)
-    vjp = None
-    try:
-        if args.no_e2e:
-            raise RuntimeError("skipped in the profile workload")
-        dl = np.ones(W * H) * 1e-3
-        t0 = time.perf_counter()
-        eng.vjp(desc, dl, engine.PREC_FP64, want_fields=True)
-        vjp_ms = eng.stats()["device_ms"]
-        vjp = {"vjp_ms": vjp_ms, "fwd_ms": t_fp64, "ratio": vjp_ms / t_fp64,
-               "wall_ms": (time.perf_counter() - t0) * 1e3}
-    except Exception as ex:  # not built yet
-        vjp = {"unavailable": str(ex)[:120]}
+    vjp = batch = None
+    if not args.no_e2e:
+        vjp = run_vjp_config4()
+        batch = run_batch_config3(dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -313,7 +459,8 @@ def run_engine(args, rank, world, local):
                  "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"]),
                  "path": "raptor_gpu_upload_grid (pinned host prims) + raptor_gpu_render (host image out)"}
                 if t_e2e is not None else None),
-        "gpu_launches": 2 * args.steps,
+        # timed loop, per render of each form: L2 flush, ray kernel, spectrum kernel
+        "gpu_launches": 3 * 2 * args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value if peak.value > 0 else None, "traffic": None,
                      "peak_source": "measured DFMA loop on this GPU (MEASURED_PEAKS.json has no FP64 figure); "
@@ -328,6 +475,7 @@ def run_engine(args, rank, world, local):
             "mixed": {"ms_per_image": t_mixed, "speedup_vs_fp64": t_fp64 / t_mixed, "flux_err_vs_fp64": flux_err,
                       "pixel_err_median": float(np.median(pix_err)), "pixel_err_max": float(np.max(pix_err))},
             "vjp": vjp,
+            "batch": batch,
         },
     }
     if cpu:
@@ -345,9 +493,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", choices=("1024", "profile"), default="1024",
-                    help="profile: a 256x256 image on a 256x256 torus, render timings only (for ncu captures)")
+    ap.add_argument("--workload", choices=("1024", "profile", "differentiable"), default="1024",
+                    help="profile: a 256x256 image on a 256x256 torus, render timings only (for ncu captures); "
+                         "differentiable: the 2048x2048 5-frequency forward + VJP with finite-difference checks")
     args = ap.parse_args()
+    if args.workload == "differentiable":
+        print(json.dumps(run_differentiable(dist_env()[2])), flush=True)
+        return
     if args.workload == "profile":
         global W, H, GRID_N
         W = H = 256

@@ -101,6 +101,8 @@ typedef struct raptor_gpu_stats {
     double kk_max;        /* max |g k k| / (k^t)^2 over rays at termination */
     int block_size, blocks_per_sm, refill_interval, grid_blocks;
     int graph_replayed;
+    long long device_bytes;      /* device memory the context holds now */
+    long long peak_device_bytes; /* the most it has held */
 } raptor_gpu_stats;
 
 /* Gradients of a scalar loss L(I) of the output image, given dL/dI. */
@@ -111,6 +113,9 @@ typedef struct raptor_grad {
     double d_inclination; /* dL/dINCLINATION, per degree */
     double *d_rho;        /* [n1*n2] dL/d rho per cell (caller-allocated, may be NULL) */
     double *d_u;          /* [n1*n2] dL/d u per cell (caller-allocated, may be NULL) */
+    double *d_lnthetae;   /* [n1*n2] dL/d ln f per cell, f a per-cell factor on the electron
+                             temperature Theta_e of every sample, interpolated bilinearly as
+                             rho and u are (f = 1 renders the reference's image; may be NULL) */
 } raptor_grad;
 
 typedef struct raptor_gpu_ctx raptor_gpu_ctx;
@@ -167,8 +172,11 @@ int raptor_gpu_trace_ray(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
 
 /* Vector-Jacobian product of one image: given dL_dI [W*H][n_freq] (same
  * layout and nu^3 scaling as I_out), returns dL/d(M_UNIT, R_HIGH, R_LOW,
- * INCLINATION) and, if the pointers are set, dL/d rho and dL/d u on the
- * image's grid.  I_out receives the forward image (may be NULL). */
+ * INCLINATION) and, if the pointers are set, the per-cell gradients on the
+ * image's grid.  precision selects the form of the forward render whose image
+ * the adjoint uses (RAPTOR_PREC_FP64 or RAPTOR_PREC_MIXED); the adjoint pass
+ * itself runs in FP64.  I_out receives the forward image (may be NULL).
+ * No counterpart in the reference, which has no derivatives. */
 int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
                    const double *dL_dI, double *I_out, raptor_grad *grad);
 

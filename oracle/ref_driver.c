@@ -137,3 +137,13 @@ int ref_output_files(const double *field, double spectrum, double freq)
     free(store);
     return 0;
 }
+
+/* Scale one primitive of one cell of the loaded grid, p[q][i][j][0]
+ * (grmhd.c:76-91), for finite-difference checks of per-cell gradients. */
+int ref_scale_prim(int q, int i, int j, double factor)
+{
+    if (!p || q < 0 || q >= NPRIM || i < 0 || i >= N1 || j < 0 || j >= N2)
+        return -1;
+    p[q][i][j][0] *= factor;
+    return 0;
+}

@@ -68,6 +68,10 @@ struct raptor_gpu_ctx {
     raptor_gpu_stats stats{};
     double last_upload_ms = 0.0;
     std::map<std::string, LaunchShape> tuned;  // autotuner cache, keyed by batch signature
+    bool tune_file_loaded = false;
+    long long device_bytes = 0, peak_device_bytes = 0;  // cudaMalloc'd by this context
+    cudaGraphExec_t graph_exec = nullptr;       // captured render, replayed while graph_key repeats
+    std::string graph_key;
     char err[512] = {0};
 };
 

@@ -28,6 +28,8 @@ enum : int {
     kCtrNonFinite = 6,
     kCtrMaxSteps = 7,
     kCtrKkMax = 8,  // bits of a non-negative double, atomicMax as integer
+    kCtrVjpEmit = 9,  // adjoint pass: emitting (sample, frequency) pairs
+    kCtrVjpGate = 10, // adjoint pass: terms inside the tau gate
     kCtrCount = 16
 };
 

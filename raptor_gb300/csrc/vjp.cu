@@ -1,9 +1,469 @@
-// Vector-Jacobian product entry point (forward-mode tangent of the
-// geodesic plus reverse accumulation of the transfer).
+// Vector-Jacobian product of one image: raptor_gpu_vjp.
+//
+// Given dL/dO for the rendered image O (the nu^3-scaled intensities of
+// core.c:136), returns dL/d(M_UNIT, R_HIGH, R_LOW, INCLINATION) and, per grid
+// cell, dL/d rho, dL/d u and dL/d ln Theta_e (Theta_e of the samples scaled by
+// a bilinear per-cell factor).
+//
+// Structure of the computation, per ray and frequency (radiative_transfer.c:
+// 88-95): with delta_k = nu_p a dl and S_k = j / nu_p^2 dl at sample k,
+//   tau_k = sum_{m<=k} delta_m,   I = sum_k g_k S_k exp(-tau_k),
+// g_k the ln(1000) gate (held fixed).  Then
+//   dI/dS_k     = g_k exp(-tau_k)
+//   dI/ddelta_k = -sum_{k'>=k} g_k' S_k' exp(-tau_k') = -(I - I_<k)
+// so one forward sweep over the ray, knowing the ray's final I from the
+// forward render, gives the exact reverse-mode sensitivities of every sample
+// without storing or re-walking the ray backwards.
+//
+// * The four scalars go forward mode: the ray carries d tau / d theta and
+//   accumulates dI/d theta = sum_k g_k e^-tau_k (dS_k/d theta - S_k dtau_k/d theta).
+// * The inclination moves the camera and so the whole geodesic: its tangent
+//   runs through the camera constants (host, below) and every RK stage
+//   (Dual<1> over the same templated FP64 code as the forward kernel).
+// * The per-cell fields enter a sample only through the bilinear rho and u
+//   (grmhd.c:35-44), so each sample scatters
+//   w (g e^-tau dS/drho_s - (I - I_<k) ddelta/drho_s) times the four bilinear
+//   weights into dL/drho with FP64 atomics.  u reaches the emission only
+//   through Theta_e (raptor_harm_model.c:261-271), so the sample carries the
+//   direction d/d ln Theta_e instead of d/du_s and scatters both it and
+//   its product with d ln Theta_e/du_s.
+// Discrete decisions (step count, gates, sigma cut, clamps) are those of the
+// primal, as a finite difference of small step sees them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dual.cuh"
 #include "engine_internal.h"
+#include "ray_kernel.cuh"
+
+using namespace raptor;
+
+namespace {
+
+using D1 = Dual<1>;
+using D6 = Dual<6>;  // directions: 0 inclination, 1 rho_s, 2 ln Theta_e (u_s), 3 ln M_unit, 4 R_high, 5 R_low
+constexpr int kDirIncl = 0, kDirRho = 1, kDirU = 2, kDirLnM = 3, kDirRh = 4, kDirRl = 5;
+// the four scalar parameters' directions: 0 -> incl, 1 -> ln M, 2 -> R_high, 3 -> R_low
+__device__ __forceinline__ int gdir(int q) { return q == 0 ? kDirIncl : q + 2; }
+
+__device__ __forceinline__ D6 lift(const D1& a) {
+    D6 r(a.v);
+    r.d[kDirIncl] = a.d[0];
+    return r;
+}
+
+template <int NF>
+struct SampleTerms {
+    D6 S[NF], dtau[NF];
+    double dlnth_du;  // d ln Theta_e / d u_s
+    bool emit[NF], poison[NF];
+};
+
+// One transfer sample as value + six tangents: the same arithmetic as
+// rt_sample_fp64 (get_fluid_params raptor_harm_model.c:190-290,
+// pitch_angle radiative_transfer.c:32-47, j_nu.c:130-153, 188-200), split
+// into the per-frequency terms S and delta of the tau / I recurrence.
+template <int NF>
+__device__ bool sample_terms(const DevImage& im, const D1& x1, const D1& x2, const D1 k1[4], const MksPointT<D1>& p,
+                             const D1& adl1, CellCoef& cc, SampleTerms<NF>& out) {
+    MetricDDT<D1> gd1;
+    MetricUUT<D1> gu1;
+    mks_metric(p, im.geo, gd1, gu1);
+    MetricT<D6> g;
+    g.d00 = lift(gd1.g00); g.d01 = lift(gd1.g01); g.d03 = lift(gd1.g03); g.d11 = lift(gd1.g11);
+    g.d13 = lift(gd1.g13); g.d22 = lift(gd1.g22); g.d33 = lift(gd1.g33);
+    g.u00 = lift(gu1.g00); g.u01 = lift(gu1.g01); g.u11 = lift(gu1.g11); g.u13 = lift(gu1.g13);
+    g.u22 = lift(gu1.g22); g.u33 = lift(gu1.g33);
+
+    // Xtoij with the fractional offsets carrying their inclination tangent
+    cc = cell_coef(im, x1.v, x2.v);
+    const int i = cc.base / im.n2, j = cc.base % im.n2;
+    D6 d1 = D6(cc.d1), d2 = D6(cc.d2);
+    {
+        const double t1 = (x1.v - im.startx1) * im.idx1 - 0.5;
+        const double t2 = (x2.v - im.startx2) * im.idx2 - 0.5;
+        if ((int)t1 == i) d1.d[kDirIncl] = x1.d[0] * im.idx1;  // not clamped
+        if ((int)t2 == j) d2.d[kDirIncl] = x2.d[0] * im.idx2;
+    }
+    const D6 c0 = (1.0 - d1) * (1.0 - d2), c1 = (1.0 - d1) * d2, c2 = d1 * (1.0 - d2), c3 = d1 * d2;
+    double a[8], b[8], e[8], f[8];
+    const double* cp = im.cells64 + (size_t)cc.base * 8;
+    load_cell(cp, a);
+    load_cell(cp + 8, b);
+    load_cell(cp + (size_t)im.n2 * 8, e);
+    load_cell(cp + (size_t)im.n2 * 8 + 8, f);
+    D6 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = c0 * a[q] + c1 * b[q] + c2 * e[q] + c3 * f[q];
+    v[0].d[kDirRho] += 1.0;  // rho_s and u_s as independent variables
+    v[1].d[kDirU] += 1.0;
+
+    D6 Ne_unit(im.Ne_unit), B_unit(im.B_unit), r_high(im.r_high), r_low(im.r_low);
+    Ne_unit.d[kDirLnM] = im.Ne_unit;     // Ne_unit proportional to M_unit
+    B_unit.d[kDirLnM] = 0.5 * im.B_unit;  // B_unit proportional to sqrt(M_unit)
+    r_high.d[kDirRh] = 1.0;
+    r_low.d[kDirRl] = 1.0;
+    Fluid<D6> fl;
+    if (!fluid_from_prims(v, g, Ne_unit, B_unit, r_high, r_low, fl)) return false;
+    // u_s moves nothing but Theta_e: keep d ln Theta_e/du_s and turn the
+    // direction into d/d ln Theta_e
+    out.dlnth_du = fl.thetae.v > 0.0 ? fl.thetae.d[kDirU] / fl.thetae.v : 0.0;
+    fl.thetae.d[kDirU] = fl.thetae.v;
+
+    const D6 k[4] = {lift(k1[0]), lift(k1[1]), lift(k1[2]), lift(k1[3])};
+    D6 kd[4];
+    lowerT(g, k, kd);
+    const D6* U = fl.ucon;
+    const D6* Bc = fl.bcon;
+    const D6 kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
+    D6 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(kU) * fl.B / B_unit);
+    if (fabs(pitch.v) > 1.0) pitch = D6(pitch.v > 0 ? 1.0 : -1.0);
+    const D6 s2 = 1.0 - pitch * pitch;
+    const D6 sth = s2.v > 0.0 ? sqrt(s2) : D6(0.0);
+    const D6 nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
+    const D6 nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
+    const bool emits = (fabs(sth.v) >= 1.e-10) && (fl.thetae.v > 1e-4);
+    const D6 K2 = 2.0 * fl.thetae * fl.thetae;
+    const D6 T = fl.thetae * (kEMass * kC * kC / kBoltz);
+    const D6 adl = lift(adl1);
+#pragma unroll
+    for (int fi = 0; fi < NF; ++fi) {
+        out.emit[fi] = false;
+        out.poison[fi] = false;
+        if (fi >= im.nfreq) break;
+        D6 nup = -kU * im.freq[fi];
+        if (nup.v <= 0.0) nup = D6(1.0);
+        const D6 dlf = adl * im.rg_over_nu[fi];
+        if (emits && nup.v != 1.0) {
+            const D6 X = nup / nus;
+            const D6 cb = cbrt(X);
+            const D6 sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);
+            const D6 jn = fl.ne * (1.4142135623730951 * CUDART_PI) * nus / (3.0 * K2) * (sq * sq) * exp(-cb) * kE2C;
+            const D6 Bnu = 2.0 * nup * nup * nup / (kC * kC) / (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
+            const D6 an = jn * kE2CH / Bnu / kE2C;
+            out.dtau[fi] = nup * an * dlf;
+            out.S[fi] = jn / (nup * nup) * dlf;
+            out.emit[fi] = true;
+        } else {
+            const double Bnu = 2.0 * nup.v * nup.v * nup.v / (kC * kC) * 1.0 /
+                               (exp(kPlanck * nup.v / (kBoltz * T.v)) - 1.0);
+            out.poison[fi] = !(Bnu != 0.0);  // the primal's 0/0 (transfer.cuh)
+        }
+    }
+    return true;
+}
+
+// Inclination-dependent camera constants with their tangent per degree.
+struct HD {
+    double v, d;
+};
+HD operator+(HD a, HD b) { return {a.v + b.v, a.d + b.d}; }
+HD operator-(HD a, HD b) { return {a.v - b.v, a.d - b.d}; }
+HD operator*(HD a, HD b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+HD operator/(HD a, HD b) { return {a.v / b.v, (a.d - a.v / b.v * b.d) / b.v}; }
+HD cst(double x) { return {x, 0.0}; }
+HD hsin(HD a) { return {std::sin(a.v), std::cos(a.v) * a.d}; }
+HD hcos(HD a) { return {std::cos(a.v), -std::sin(a.v) * a.d}; }
+HD hsqrt(HD a) { const double s = std::sqrt(a.v); return {s, 0.5 / s * a.d}; }
+HD hacos(HD a) { return {std::acos(a.v), -a.d / std::sqrt(1.0 - a.v * a.v)}; }
+
+CamT<D1> camera_tangent(const DevImage& im, double inclination, double a, double hslope) {
+    const HD incl{inclination, 1.0};
+    const HD mu0 = hcos(incl * cst(M_PI / 180.));
+    const HD thc = hacos(mu0);
+    const HD sin_mu = hsqrt(cst(1.0) - mu0 * mu0);
+    const HD mu0sq = mu0 * mu0;
+    const HD sc2 = hsin(thc) * hsin(thc), cc2 = hcos(thc) * hcos(thc);
+    const HD st = hsin(thc), ct = hcos(thc);
+    const double r = kRcam;
+    const HD sig = cst(r * r) + cst(a * a) * ct * ct;
+    const double dl = r * r + a * a - 2. * r;
+    const HD A = cst((r * r + a * a) * (r * r + a * a)) - cst(dl * a * a) * st * st;
+    const HD g11 = sig / cst(dl) * cst(r * r);
+    const HD gu00 = cst(-1.0) * A / (sig * cst(dl));
+    const HD gu03 = cst(-2. * a * r) / (sig * cst(dl));
+    const HD gu33 = (cst(dl) - cst(a * a) * st * st) / (sig * cst(dl) * st * st);
+    const HD gu22 = cst(1.0) / sig;
+    // x2 solves pi x + (1-h)/2 sin(2 pi x) = theta: dx2/dtheta = 1/(pi (1 + (1-h) cos 2 pi x2)) = 1/k2fac
+    const double x2 = im.xcam[2];
+    const bool clamped = (x2 <= 0.0 || x2 >= 1.0);
+    const HD x2c{x2, clamped ? 0.0 : thc.d / im.k2fac};
+    const HD k2fac{im.k2fac, -M_PI * (1. - hslope) * 2. * M_PI * std::sin(2. * M_PI * x2) * x2c.d};
+    auto D = [](HD h) { D1 r(h.v); r.d[0] = h.d; return r; };
+    CamT<D1> c;
+    c.sin_mu = D(sin_mu);
+    c.mu0sq = D(mu0sq);
+    c.cc_over_sc = D(cc2 / sc2);
+    c.cosc2 = D(cc2);
+    c.g11 = D(g11);
+    c.gu00 = D(gu00);
+    c.gu03 = D(gu03);
+    c.gu33 = D(gu33);
+    c.gu22 = D(gu22);
+    c.x2c = D(x2c);
+    c.k2fac = D(k2fac);
+    return c;
+}
+
+constexpr int kVjpBlock = 128;
+
+template <int NF>
+__global__ void __launch_bounds__(kVjpBlock, 1)
+    vjp_kernel(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
+               const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
+               double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
+               double* __restrict__ g_th) {
+    const DevImage& im = *imp;
+    const int lane = threadIdx.x & 31;
+    const long long nrays = (long long)im.width * im.height;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0;
+    bool live = true;
+    while (true) {
+        const unsigned want = __ballot_sync(kFull, live);
+        if (!want) break;
+        const int leader = __ffs(want) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(want));
+        base = __shfl_sync(kFull, base, leader);
+        long long rid = -1;
+        if (live) {
+            rid = (long long)(base + __popc(want & ((1u << lane) - 1u)));
+            if (rid >= nrays) {
+                live = false;
+                rid = -1;
+            }
+        }
+        if (rid < 0) continue;
+
+        const int pix = (int)rid;
+        D1 y[8];
+        double beta;
+        init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
+        MksPointT<D1> p;
+        mks_point(y[1], y[2], im.geo, p);
+        double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dI[NF][4];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            tau[f] = 0.0;
+            Ipart[f] = 0.0;
+            Itot[f] = 0.0;
+            w[f] = 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dtg[f][q] = dI[f][q] = 0.0;
+            if (f < im.nfreq) {
+                const long long o = (long long)pix * im.nfreq + f;
+                Itot[f] = fwd[o] / im.nu3[f];
+                w[f] = dLdO[o] * im.nu3[f];
+            }
+        }
+        int steps = 0, turns = 0, stop = 0;
+        double thdot_prev = 0.0;
+        while (true) {
+            const double r = p.rp.v;
+            if (!(r < kCutoffOuter && r > im.cutoff_inner && (double)steps < kMaxSteps && !stop)) break;
+            if (thdot_prev * y[6].v < 0.0 && steps > 2) turns += 1;
+            thdot_prev = y[6].v;
+            if ((beta < 0.0 && turns > kMaxOrder) || (beta > 0.0 && turns > kMaxOrder + 1)) stop = 1;
+            const D1 dl = step_size(im, y);
+            if (im.integrator == 2) rk2_step(im.geo, y, p, dl);
+            else rk4_step(im.geo, y, p, dl);
+            steps += 1;
+            if (y[1].v > im.stopx1 && y[5].v < 0.0) break;
+            if (y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2) {
+                ++n_calls;
+                SampleTerms<NF> st;
+                CellCoef cc;
+                const D1 k1[4] = {y[4], y[5], y[6], y[7]};
+                if (sample_terms<NF>(im, y[1], y[2], k1, p, fabs(dl), cc, st)) {
+                    ++n_samples;
+                    double Gr = 0.0, Gt = 0.0;
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        if (f >= im.nfreq) break;
+                        if (st.emit[f]) {
+                            ++n_emit;
+                            const D6& S = st.S[f];
+                            const D6& dt = st.dtau[f];
+                            tau[f] += dt.v;
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) dtg[f][q] += dt.d[gdir(q)];
+                            const double e = exp(-tau[f]);
+                            const bool gate = tau[f] < 6.907755278982137 && !(tau[f] < 0.0);
+                            const double suffix = Itot[f] - Ipart[f];
+                            const double eS = gate ? e : 0.0;
+                            if (suffix != 0.0 || gate) {
+                                Gr += w[f] * (eS * S.d[kDirRho] - suffix * dt.d[kDirRho]);
+                                Gt += w[f] * (eS * S.d[kDirU] - suffix * dt.d[kDirU]);
+                            }
+                            if (gate) {
+                                ++n_gate;
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) dI[f][q] += e * (S.d[gdir(q)] - S.v * dtg[f][q]);
+                                Ipart[f] += S.v * e;
+                            }
+                        } else if (st.poison[f]) {
+                            tau[f] = __longlong_as_double(0x7ff8000000000000ll);
+                        }
+                    }
+                    const double Gu = Gt * st.dlnth_du;
+                    if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
+                        const double w0 = (1.0 - cc.d1) * (1.0 - cc.d2), w1 = (1.0 - cc.d1) * cc.d2;
+                        const double w2 = cc.d1 * (1.0 - cc.d2), w3 = cc.d1 * cc.d2;
+                        const long long c = cc.base, cn = cc.base + im.n2;
+                        atomicAdd(&g_rho[c], Gr * w0);
+                        atomicAdd(&g_rho[c + 1], Gr * w1);
+                        atomicAdd(&g_rho[cn], Gr * w2);
+                        atomicAdd(&g_rho[cn + 1], Gr * w3);
+                        atomicAdd(&g_u[c], Gu * w0);
+                        atomicAdd(&g_u[c + 1], Gu * w1);
+                        atomicAdd(&g_u[cn], Gu * w2);
+                        atomicAdd(&g_u[cn + 1], Gu * w3);
+                        atomicAdd(&g_th[c], Gt * w0);
+                        atomicAdd(&g_th[c + 1], Gt * w1);
+                        atomicAdd(&g_th[cn], Gt * w2);
+                        atomicAdd(&g_th[cn + 1], Gt * w3);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (isfinite(dI[f][q])) acc[q] += w[f] * dI[f][q];
+        atomicAdd(&counters[kCtrSteps], (unsigned long long)steps);
+        atomicAdd(&counters[kCtrRays], 1ull);
+    }
+    atomicAdd(&counters[kCtrRtCalls], n_calls);
+    atomicAdd(&counters[kCtrRtSamples], n_samples);
+    atomicAdd(&counters[kCtrVjpEmit], n_emit);
+    atomicAdd(&counters[kCtrVjpGate], n_gate);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        double v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+        if (lane == 0) atomicAdd(&gscal[q], v);
+    }
+}
+
+template <int NF>
+void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
+                const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt) {
+    vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt);
+}
+
+}  // namespace
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return ctx_fail(ctx, RAPTOR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));  \
+    } while (0)
 
 extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, const double* dL_dI,
                               double* I_out, raptor_grad* grad) {
-    (void)img; (void)precision; (void)dL_dI; (void)I_out; (void)grad;
-    return ctx_fail(ctx, RAPTOR_ERR_INVALID, "raptor_gpu_vjp: not built yet");
+    if (!ctx) return RAPTOR_ERR_INVALID;
+    ctx->err[0] = 0;
+    if (!img || !dL_dI || !grad) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: null image, dL_dI or grad");
+    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: precision %d is neither FP64 (0) nor mixed (1)", precision);
+    const bool mixed = precision == RAPTOR_PREC_MIXED;
+    auto t0 = std::chrono::steady_clock::now();
+    CK(cudaSetDevice(ctx->device));
+    cudaGetLastError();
+    Batch& b = ctx->batch;
+    int rc = prepare_batch(ctx, img, 1, b);
+    if (rc) return rc;
+    const DevImage& him = b.host[0];
+    const GridSlot& gs = ctx->grids[img->grid];
+    const long long ncell = (long long)gs.geom.n1 * gs.geom.n2;
+
+    // forward render (its image is the I of the suffix identity)
+    const void* fnp = nullptr;
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, mixed, &fnp);
+    LaunchShape ls = choose_shape(ctx, b, mixed, fn, fnp);
+    rc = enqueue_render(ctx, b, mixed, 0, b.total_rays, ls, fn, true);
+    if (rc) return rc;
+
+    const size_t nout = (size_t)b.out_len;
+    rc = ensure_buffer(ctx, (void**)&ctx->d_dldi, &ctx->dldi_cap, sizeof(double) * nout);
+    if (!rc) rc = ensure_buffer(ctx, (void**)&ctx->d_grad, &ctx->grad_cap, sizeof(double) * (4 + 3 * ncell));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_dldi, dL_dI, sizeof(double) * nout, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_grad, 0, sizeof(double) * (4 + 3 * ncell), ctx->stream));
+    unsigned long long fwd_ctr[kCtrCount];
+    CK(cudaMemcpyAsync(fwd_ctr, ctx->d_counters, sizeof fwd_ctr, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float fwd_ms = 0.f;
+    CK(cudaEventElapsedTime(&fwd_ms, ctx->evA, ctx->evB));
+    CK(cudaMemsetAsync(ctx->d_counters, 0, kCtrCount * sizeof(unsigned long long), ctx->stream));
+
+    const CamT<D1> cam = camera_tangent(him, img->inclination, gs.geom.a, gs.geom.hslope);
+    int occ = 1;
+    void (*vfn)(int, cudaStream_t, const DevImage*, const CamT<D1>&, const double*, const double*,
+                unsigned long long*, double*, double*, double*, double*) = nullptr;
+    const void* kp = nullptr;
+    if (b.max_nf <= 1) { vfn = launch_vjp<1>; kp = (const void*)vjp_kernel<1>; }
+    else if (b.max_nf <= 2) { vfn = launch_vjp<2>; kp = (const void*)vjp_kernel<2>; }
+    else if (b.max_nf <= 4) { vfn = launch_vjp<4>; kp = (const void*)vjp_kernel<4>; }
+    else { vfn = launch_vjp<8>; kp = (const void*)vjp_kernel<8>; }
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
+    const int grid = ctx->num_sms * std::max(occ, 1);
+    double* gsc = ctx->d_grad;
+    // the per-cell scatter runs when any of the three fields is asked for
+    const bool fields = grad->d_rho || grad->d_u || grad->d_lnthetae;
+    double* grho = fields ? ctx->d_grad + 4 : nullptr;
+    double* gu = fields ? ctx->d_grad + 4 + ncell : nullptr;
+    double* gth = fields ? ctx->d_grad + 4 + 2 * ncell : nullptr;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    vfn(grid, ctx->stream, ctx->d_imgs, cam, ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc, grho, gu, gth);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    double scal[4];
+    CK(cudaMemcpyAsync(scal, gsc, sizeof scal, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad->d_rho)
+        CK(cudaMemcpyAsync(grad->d_rho, grho, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad->d_u)
+        CK(cudaMemcpyAsync(grad->d_u, gu, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad->d_lnthetae)
+        CK(cudaMemcpyAsync(grad->d_lnthetae, gth, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
+    if (I_out) CK(cudaMemcpyAsync(I_out, ctx->d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long ctr[kCtrCount];
+    CK(cudaMemcpyAsync(ctr, ctx->d_counters, sizeof ctr, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float vjp_ms = 0.f;
+    CK(cudaEventElapsedTime(&vjp_ms, ctx->ev0, ctx->ev1));
+
+    grad->d_inclination = scal[0];
+    grad->d_m_unit = scal[1] / img->m_unit;  // the kernel differentiates with respect to ln M_unit
+    grad->d_r_high = scal[2];
+    grad->d_r_low = scal[3];
+
+    raptor_gpu_stats& s = ctx->stats;
+    memset(&s, 0, sizeof s);
+    s.kernel_ms = vjp_ms;
+    s.device_ms = fwd_ms + vjp_ms;
+    // counters of the adjoint pass (the forward pass takes the same steps)
+    s.rays = (long long)ctr[kCtrRays];
+    s.steps = (long long)ctr[kCtrSteps];
+    s.rt_calls = (long long)ctr[kCtrRtCalls];
+    s.rt_samples = (long long)ctr[kCtrRtSamples];
+    s.n_stepcap = (long long)ctr[kCtrVjpEmit];    // frequencies that emitted
+    s.n_nonfinite = (long long)ctr[kCtrVjpGate];  // terms inside the tau gate
+    (void)fwd_ctr;
+    s.block_size = kVjpBlock;
+    s.grid_blocks = grid;
+    s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if ((long long)ctr[kCtrRays] != b.total_rays)
+        return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "vjp kernel retired %lld rays, expected %lld",
+                        (long long)ctr[kCtrRays], b.total_rays);
+    return RAPTOR_OK;
 }

@@ -66,7 +66,8 @@ class Stats(ctypes.Structure):
                 ("max_ray_steps", ctypes.c_longlong), ("n_stepcap", ctypes.c_longlong),
                 ("n_nonfinite", ctypes.c_longlong), ("kk_max", ctypes.c_double), ("block_size", ctypes.c_int),
                 ("blocks_per_sm", ctypes.c_int), ("refill_interval", ctypes.c_int),
-                ("grid_blocks", ctypes.c_int), ("graph_replayed", ctypes.c_int)]
+                ("grid_blocks", ctypes.c_int), ("graph_replayed", ctypes.c_int),
+                ("device_bytes", ctypes.c_longlong), ("peak_device_bytes", ctypes.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -75,7 +76,7 @@ class Stats(ctypes.Structure):
 class GradC(ctypes.Structure):
     _fields_ = [("d_m_unit", ctypes.c_double), ("d_r_high", ctypes.c_double), ("d_r_low", ctypes.c_double),
                 ("d_inclination", ctypes.c_double), ("d_rho", ctypes.POINTER(ctypes.c_double)),
-                ("d_u", ctypes.POINTER(ctypes.c_double))]
+                ("d_u", ctypes.POINTER(ctypes.c_double)), ("d_lnthetae", ctypes.POINTER(ctypes.c_double))]
 
 
 _LIB = None
@@ -208,11 +209,13 @@ class Engine:
         out = np.empty(img.width * img.height * img.n_freq)
         d_rho = np.zeros(geom.n1 * geom.n2) if want_fields else None
         d_u = np.zeros(geom.n1 * geom.n2) if want_fields else None
-        g = GradC(0, 0, 0, 0, _dp(d_rho), _dp(d_u))
+        d_th = np.zeros(geom.n1 * geom.n2) if want_fields else None
+        g = GradC(0, 0, 0, 0, _dp(d_rho), _dp(d_u), _dp(d_th))
         self._check(self.lib.raptor_gpu_vjp(self.h, ctypes.byref(img), precision, _dp(dldi), _dp(out),
                                             ctypes.byref(g)))
         res = dict(d_m_unit=g.d_m_unit, d_r_high=g.d_r_high, d_r_low=g.d_r_low, d_inclination=g.d_inclination)
         if want_fields:
             res["d_rho"] = d_rho.reshape(geom.n1, geom.n2)
             res["d_u"] = d_u.reshape(geom.n1, geom.n2)
+            res["d_lnthetae"] = d_th.reshape(geom.n1, geom.n2)
         return out, res

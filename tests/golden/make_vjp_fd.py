@@ -1,0 +1,104 @@
+"""Finite-difference gradients of an image loss from the reference build
+(oracle/_ref, IEEE semantics), for checking raptor_gpu_vjp.
+
+    python tests/golden/make_vjp_fd.py [--threads 8]
+
+Configuration (BASELINE configuration 4): 256x256 image, 230 GHz, i = 60 deg,
+a = 0.9375 torus at 256x256, M_unit = 1e19, R_high = R_low = 3, RK4 eps 0.05.
+Loss L = 1/2 sum (O - O_target)^2 over the nu^3-scaled image O, the target
+rendered at M_unit x 1.3, R_high = R_low = 4, i = 62 deg.  Central differences
+with relative step h = 1e-4 on M_unit, R_high, R_low, the inclination, and on
+rho and u of 32 seeded cells inside the torus.  For the four scalars the
+differences at h and h/2 are also Richardson-extrapolated,
+(4 D(h/2) - D(h)) / 3, which removes the O(h^2) truncation error: at h = 1e-4
+the inclination's truncation error alone is ~1e-3 of the derivative.  Writes
+tests/golden/vjp_fd_256.npz.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import ref  # noqa: E402
+from raptor_gb300 import harm, synth  # noqa: E402
+from tests.golden.make_golden import quiet  # noqa: E402
+
+N = 256
+W = H = 256
+FREQ = 230e9
+BASE = dict(m_unit=1e19, r_high=3.0, r_low=3.0, incl=60.0)
+TARGET = dict(m_unit=1.3e19, r_high=4.0, r_low=4.0, incl=62.0)
+REL_H = 1e-4
+N_CELLS = 32
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--threads", type=int, default=0)
+    a = ap.parse_args()
+    tmp = tempfile.mkdtemp(prefix="rgv_", dir="/tmp")
+    d = synth.make_torus(n1=N, n2=N)
+    path = os.path.join(tmp, "t.dump")
+    harm.write_dump(path, d)
+    model = harm.ModelIn(IMG_WIDTH=W, IMG_HEIGHT=H, FREQ_MIN=FREQ, FREQ_MAX=FREQ, STEPSIZE=0.05)
+    pix = np.arange(W * H, dtype=np.int32)
+    lib = ref.load(N, N, "RK4")
+    lib.ref_scale_prim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+
+    def render(prm, scale=None):
+        with quiet():
+            s = ref.RefSession(path, model, prm["m_unit"], prm["incl"], prm["r_high"], prm["r_low"], 0.0,
+                               n1=N, n2=N, workdir=tmp)
+            if scale:
+                assert lib.ref_scale_prim(*scale) == 0
+            img, _ = s.render_pixels(pix, FREQ, a.threads)
+        return img
+
+    target = render(TARGET)
+
+    def loss(prm, scale=None):
+        o = render(prm, scale)
+        return 0.5 * float(np.sum((o - target) ** 2))
+
+    L0 = loss(BASE)
+    fd, rich = {}, {}
+    for key in ("m_unit", "r_high", "r_low", "incl"):
+        diffs = []
+        for rel in (REL_H, REL_H / 2):
+            h = rel * BASE[key]
+            lp = loss(dict(BASE, **{key: BASE[key] + h}))
+            lm = loss(dict(BASE, **{key: BASE[key] - h}))
+            diffs.append((lp - lm) / (2 * h))
+        fd[key] = diffs[0]
+        rich[key] = (4 * diffs[1] - diffs[0]) / 3
+        print(key, fd[key], rich[key], flush=True)
+    rng = np.random.default_rng(2024)
+    cand = np.argwhere(d.prims[0] > 0.2)
+    cells = cand[rng.choice(len(cand), N_CELLS, replace=False)]
+    fd_rho = np.zeros(N_CELLS)
+    fd_u = np.zeros(N_CELLS)
+    for c, (i, j) in enumerate(cells):
+        for q, arr in ((0, fd_rho), (1, fd_u)):
+            v = d.prims[q, i, j]
+            lp = loss(BASE, (q, int(i), int(j), 1 + REL_H))
+            lm = loss(BASE, (q, int(i), int(j), 1 - REL_H))
+            arr[c] = (lp - lm) / (2 * REL_H * v)
+        print("cell", i, j, fd_rho[c], fd_u[c], flush=True)
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "vjp_fd_256.npz"), L0=np.array([L0]),
+                        fd_m_unit=np.array([fd["m_unit"]]), fd_r_high=np.array([fd["r_high"]]),
+                        fd_r_low=np.array([fd["r_low"]]), fd_incl=np.array([fd["incl"]]),
+                        rich_m_unit=np.array([rich["m_unit"]]), rich_r_high=np.array([rich["r_high"]]),
+                        rich_r_low=np.array([rich["r_low"]]), rich_incl=np.array([rich["incl"]]), cells=cells,
+                        fd_rho=fd_rho, fd_u=fd_u, rel_h=np.array([REL_H]))
+
+
+if __name__ == "__main__":
+    main()

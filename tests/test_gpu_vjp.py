@@ -1,0 +1,156 @@
+"""raptor_gpu_vjp against central finite differences: of the engine's own
+FP64 forward render (small case), and of the reference build rerun at
+perturbed parameters (tests/golden/vjp_fd_256.npz, BASELINE configuration 4).
+
+Agreement bar: 1e-3 relative; per-cell gradients 1e-3 of the largest per-cell
+finite difference.  Scalars are compared with Richardson-extrapolated
+differences (4 D(h/2) - D(h)) / 3 at h = 1e-4 relative: the plain central
+difference at that step carries an O(h^2) truncation error of ~1e-3 for the
+inclination (with h 10x smaller the engine's own differences agree with the
+VJP to 1e-6, and to 4e-9 at 100x)."""
+import numpy as np
+import pytest
+
+from tests.parity import load_golden
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-3
+REL_H = 1e-4
+
+
+def _loss(eng, engine, desc, target):
+    img, _ = eng.render(desc, engine.PREC_FP64)
+    return 0.5 * float(np.sum((img - target) ** 2))
+
+
+class Mismatches(list):
+    def check(self, name, got, want, scale=None):
+        scale = abs(want) if scale is None else scale
+        if not abs(got - want) <= TOL * scale:
+            self.append(f"{name}: vjp {got:.6e} vs finite difference {want:.6e}")
+
+
+def test_vjp_against_engine_finite_differences(torus64):
+    from raptor_gb300 import engine
+    eng = engine.Engine()
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    kw = dict(grid=gid, inclination=60.0, m_unit=1e19, r_high=3.0, r_low=3.0)
+    mk = lambda **o: engine.image_desc(32, 32, [230e9], **dict(kw, **o))  # noqa: E731
+    target, _ = eng.render(mk(inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0), engine.PREC_FP64)
+    img, _ = eng.render(mk(), engine.PREC_FP64)
+    _, g = eng.vjp(mk(), img - target, engine.PREC_FP64)
+    bad = Mismatches()
+    for key, attr in (("m_unit", "d_m_unit"), ("r_high", "d_r_high"), ("r_low", "d_r_low"),
+                      ("inclination", "d_inclination")):
+        d = []
+        for rel in (REL_H, REL_H / 2):
+            h = rel * kw[key]
+            lp = _loss(eng, engine, mk(**{key: kw[key] + h}), target)
+            lm = _loss(eng, engine, mk(**{key: kw[key] - h}), target)
+            d.append((lp - lm) / (2 * h))
+        bad.check(key, g[attr], (4 * d[1] - d[0]) / 3)
+    # per-cell fields: cells in the torus body
+    rng = np.random.default_rng(5)
+    cand = np.argwhere(torus64.prims[0] > 0.3)
+    cells = cand[rng.choice(len(cand), 6, replace=False)]
+    fds, gots, names = [], [], []
+    for (i, j) in cells:
+        for q, field in ((0, "d_rho"), (1, "d_u")):
+            pr = torus64.prims.copy()
+            v = pr[q, i, j]
+            pr[q, i, j] = v * (1 + REL_H)
+            eng.upload_grid(torus64.geom, pr, grid_id=gid)
+            lp = _loss(eng, engine, mk(), target)
+            pr[q, i, j] = v * (1 - REL_H)
+            eng.upload_grid(torus64.geom, pr, grid_id=gid)
+            lm = _loss(eng, engine, mk(), target)
+            fds.append((lp - lm) / (2 * REL_H * v))
+            gots.append(g[field][i, j])
+            names.append(f"{field}[{i},{j}]")
+    eng.upload_grid(torus64.geom, torus64.prims, grid_id=gid)
+    scale = max(abs(x) for x in fds)
+    assert scale > 0
+    for n, a, b in zip(names, gots, fds):
+        bad.check(n, a, b, scale)
+    eng.close()
+    assert not bad, "\n".join(bad)
+
+
+def test_vjp_against_reference_finite_differences(torus256):
+    """The reference rerun at perturbed parameters (configuration 4)."""
+    from raptor_gb300 import engine
+    z = load_golden("vjp_fd_256.npz")
+    eng = engine.Engine()
+    gid = eng.upload_grid(torus256.geom, torus256.prims)
+    desc = engine.image_desc(256, 256, [230e9], grid=gid, inclination=60.0, m_unit=1e19, r_high=3.0, r_low=3.0)
+    tdesc = engine.image_desc(256, 256, [230e9], grid=gid, inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0)
+    target, _ = eng.render(tdesc, engine.PREC_FP64)
+    img, _ = eng.render(desc, engine.PREC_FP64)
+    dl = img - target
+    assert 0.5 * np.sum(dl ** 2) == pytest.approx(z["L0"][0], rel=1e-6)
+    _, g = eng.vjp(desc, dl, engine.PREC_FP64)
+    bad = Mismatches()
+    bad.check("M_unit", g["d_m_unit"], z["rich_m_unit"][0])
+    bad.check("R_high", g["d_r_high"], z["rich_r_high"][0])
+    bad.check("R_low", g["d_r_low"], z["rich_r_low"][0])
+    bad.check("inclination", g["d_inclination"], z["rich_incl"][0])
+    cells = z["cells"]
+    scale = max(np.max(np.abs(z["fd_rho"])), np.max(np.abs(z["fd_u"])))
+    for k, (i, j) in enumerate(cells):
+        bad.check(f"rho[{i},{j}]", g["d_rho"][i, j], z["fd_rho"][k], scale)
+        bad.check(f"u[{i},{j}]", g["d_u"][i, j], z["fd_u"][k], scale)
+    assert eng.stats()["rays"] == 256 * 256
+    eng.close()
+    assert not bad, "\n".join(bad)
+
+
+def _dln_thetae_unit_dR(R):
+    """d ln Thetae_unit / d trat of raptor_harm_model.c:266-270 at trat = R."""
+    tg = 0.5 * ((1.0 + 2.0 / 3.0 * (R + 1.0) / (R + 2.0)) + 4.0 / 3.0)
+    return (1.0 / 3.0) / (R + 2.0) ** 2 / (tg - 1.0) - 1.0 / (1.0 + R)
+
+
+def test_vjp_thetae_field_sums_to_temperature_ratio_gradient(torus64):
+    """A uniform factor on Theta_e is a change of T_p/T_e when R_high = R_low
+    (trat = R everywhere), and the bilinear weights of every sample sum to 1,
+    so sum_cells dL/d ln f = (dL/dR_high + dL/dR_low) / (d ln Thetae_unit/dR)."""
+    from raptor_gb300 import engine
+    eng = engine.Engine()
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    R = 3.0
+    desc = engine.image_desc(48, 48, [230e9, 345e9], grid=gid, inclination=60.0, m_unit=1e19, r_high=R, r_low=R)
+    tdesc = engine.image_desc(48, 48, [230e9, 345e9], grid=gid, inclination=62.0, m_unit=1.3e19,
+                              r_high=4.0, r_low=4.0)
+    target, _ = eng.render(tdesc, engine.PREC_FP64)
+    img, _ = eng.render(desc, engine.PREC_FP64)
+    _, g = eng.vjp(desc, img - target, engine.PREC_FP64)
+    eng.close()
+    total = float(np.sum(g["d_lnthetae"]))
+    want = (g["d_r_high"] + g["d_r_low"]) / _dln_thetae_unit_dR(R)
+    assert want != 0.0
+    assert total == pytest.approx(want, rel=1e-9)
+
+
+def test_vjp_mixed_forward(torus64):
+    """precision = mixed: the forward image comes from the FP32-transfer form,
+    the adjoint stays FP64, so the gradients agree with the FP64 VJP to the
+    mixed form's image accuracy."""
+    from raptor_gb300 import engine
+    eng = engine.Engine()
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    desc = engine.image_desc(48, 48, [230e9], grid=gid, inclination=60.0, m_unit=1e19, r_high=3.0, r_low=3.0)
+    tdesc = engine.image_desc(48, 48, [230e9], grid=gid, inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0)
+    target, _ = eng.render(tdesc, engine.PREC_FP64)
+    img, _ = eng.render(desc, engine.PREC_FP64)
+    dl = img - target
+    i64, g64 = eng.vjp(desc, dl, engine.PREC_FP64)
+    i32, g32 = eng.vjp(desc, dl, engine.PREC_MIXED)
+    eng.close()
+    assert np.array_equal(i64, img)
+    assert np.abs(i32 - img).max() <= 1e-4 * np.abs(img).max()
+    for k in ("d_m_unit", "d_r_high", "d_r_low", "d_inclination"):
+        assert g32[k] == pytest.approx(g64[k], rel=1e-3), k
+    for k in ("d_rho", "d_u", "d_lnthetae"):
+        scale = np.abs(g64[k]).max()
+        assert scale > 0
+        assert np.abs(g32[k] - g64[k]).max() <= 1e-3 * scale, k

@@ -290,6 +290,13 @@ def run_differentiable(dev, n_cells=4, reps=2):
                     ("inclination", "d_inclination")):
         fd = fd_scalar(key, 1e-4, key == "inclination")
         scal[key] = {"vjp": g[gk], "fd": fd, "rel_err": abs(g[gk] - fd) / abs(fd)}
+    # the loss is only piecewise smooth in the inclination (clamps, min() in the
+    # step size, cell-index changes along every ray): its difference quotient
+    # reaches the derivative only as h shrinks
+    for rel in (1e-6, 1e-7):
+        fd = fd_scalar("inclination", rel, False)
+        scal[f"inclination_h{rel:g}"] = {"vjp": g["d_inclination"], "fd": fd,
+                                         "rel_err": abs(g["d_inclination"] - fd) / abs(fd)}
     cells = {}
     order = np.argsort(-np.abs(g["d_rho"]).ravel())[:n_cells]
     fd_all, vjp_all = [], []

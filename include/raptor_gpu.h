@@ -46,6 +46,10 @@ extern "C" {
 #define RAPTOR_RK4 4
 #define RAPTOR_RK2 2
 
+/* camera maps (parameters.h:54-55) */
+#define RAPTOR_CAM_LINEAR 0 /* LINEAR_IMPACT_CAM: uniform grid of impact parameters (integrator.c:186-190) */
+#define RAPTOR_CAM_LOG 1    /* LOG_IMPACT_CAM: log-polar grid, x -> radius, y -> angle (integrator.c:191-198) */
+
 typedef struct raptor_gpu_options {
     int device;          /* CUDA device ordinal */
     int block_size;      /* threads per block of the ray kernel; 0 = default/tuned */
@@ -84,6 +88,7 @@ typedef struct raptor_image_desc {
     int grid;                     /* id from raptor_gpu_upload_grid */
     int n_freq;                   /* 1..RAPTOR_MAX_FREQS */
     double freq[RAPTOR_MAX_FREQS]; /* Hz */
+    int camera;                   /* RAPTOR_CAM_LINEAR (0) or RAPTOR_CAM_LOG */
 } raptor_image_desc;
 
 typedef struct raptor_gpu_stats {
@@ -138,7 +143,7 @@ int raptor_gpu_upload_grid(raptor_gpu_ctx *ctx, const double *prims, const rapto
 /* Render n_imgs images in one persistent launch (core.c:97-142 for each).
  * I_out: concatenation over images of intensityfield[W*H][n_freq]
  * (pixel x + y*W, frequency fastest), already multiplied by nu^3 as
- * core.c:136 does.  spectrum_out: [sum over images of n_freq], the plain
+ * core.c:136 does (by nu^3 r dr dtheta / D^2 for RAPTOR_CAM_LOG, core.c:123-133).  spectrum_out: [sum over images of n_freq], the plain
  * pixel sum of core.c:146-150 (the caller applies JANSKY_FACTOR when
  * writing, core.c:177,192,195).  Either output may be NULL. */
 int raptor_gpu_render(raptor_gpu_ctx *ctx, const raptor_image_desc *imgs, int n_imgs, int precision,

@@ -28,7 +28,7 @@ class PortScene(ctypes.Structure):
                 ("inclination", ctypes.c_double), ("stepsize", ctypes.c_double),
                 ("mbh", ctypes.c_double), ("m_unit", ctypes.c_double),
                 ("r_high", ctypes.c_double), ("r_low", ctypes.c_double),
-                ("integrator", ctypes.c_int)]
+                ("integrator", ctypes.c_int), ("camera", ctypes.c_int)]
 
 
 class PortRayStats(ctypes.Structure):
@@ -82,13 +82,13 @@ class Scene:
 
     def __init__(self, geom, prims, width, height, cam_size_x=40.0, cam_size_y=40.0,
                  inclination=60.0, stepsize=0.05, mbh=8.9505e39, m_unit=1e19, r_high=3.0,
-                 r_low=3.0, integrator=4):
+                 r_low=3.0, integrator=4, camera=0):
         self.prims = np.ascontiguousarray(prims, dtype=np.float64)
         assert self.prims.shape == (8, geom.n1, geom.n2)
         self.c = PortScene(geom.n1, geom.n2, geom.startx1, geom.startx2, geom.dx1, geom.dx2,
                            geom.a, geom.hslope, geom.R0, _dp(self.prims), width, height,
                            cam_size_x, cam_size_y, inclination, stepsize, mbh, m_unit,
-                           r_high, r_low, integrator)
+                           r_high, r_low, integrator, camera)
         self.lib = load()
 
     def render(self, freqs, pixels=None, nthreads=0, with_stats=False):

@@ -64,6 +64,7 @@ extern "C" void port_flop_buckets(unsigned long long out[8], int reset)
 #define K_MAX_STEPS 1e5
 #define K_CUTOFF_OUTER (K_RCAM * 1.01)
 #define K_HORIZON_MARG 1e-1
+#define K_SOURCE_DIST 2.6228263e22 /* parameters.h:144 */
 
 typedef struct ray_ctx {
     const port_scene *s;
@@ -585,10 +586,20 @@ static void trace(const ray_ctx *c, int x, int y, const double *freqs, int nf, d
         tau[f] = 0.;
         I[f] = 0.;
     }
-    double stepx = s->cam_size_x / (double)s->width;
-    double stepy = s->cam_size_y / (double)s->height;
-    double alpha = -s->cam_size_x * 0.5 + (x + 0.5) * stepx;
-    double beta = -s->cam_size_y * 0.5 + (y + 0.5) * stepy;
+    double alpha, beta;
+    if (s->camera == 1) {
+        /* LOG_IMPACT_CAM, integrator.c:192-198 */
+        double r_i = exp(log(20.) * (double)(x + 0.5) / ((double)s->width)) - 1.;
+        double theta_i = 2.0 * K_PI * (double)(y + 0.5) / ((double)s->height);
+        alpha = r_i * cos(theta_i);
+        beta = r_i * sin(theta_i);
+    } else {
+        /* LINEAR_IMPACT_CAM, integrator.c:187-190 */
+        double stepx = s->cam_size_x / (double)s->width;
+        double stepy = s->cam_size_y / (double)s->height;
+        alpha = -s->cam_size_x * 0.5 + (x + 0.5) * stepx;
+        beta = -s->cam_size_y * 0.5 + (y + 0.5) * stepy;
+    }
     double ph[8];
     FLOP_SNAP(f_init);
     init_photon(c, alpha, beta, ph);
@@ -711,8 +722,19 @@ int port_render(const port_scene *s, const int *pixels, int n, const double *fre
         int yy = pix / s->width, xx = pix % s->width;
         double I[64];
         trace(&c, xx, yy, freqs, nfreq, I, stats ? &stats[k] : NULL, NULL, 0);
-        for (int f = 0; f < nfreq; f++)
-            out[(size_t)k * nfreq + f] = I[f] * nu3[f];
+        if (s->camera == 1) {
+            /* core.c:123-133 */
+            double r_grav = K_GGRAV * s->mbh / K_CLIGHT / K_CLIGHT;
+            double r_i = exp(log(20.) * (double)(xx + 0.5) / (double)s->width) - 1.;
+            double d_r = r_grav * (r_i + 1.) * log(20.) / (double)s->width;
+            double d_theta = r_grav * 2. * K_PI / (double)s->height;
+            for (int f = 0; f < nfreq; f++)
+                out[(size_t)k * nfreq + f] =
+                    I[f] * nu3[f] * r_i * d_r * d_theta / (K_SOURCE_DIST * K_SOURCE_DIST);
+        } else {
+            for (int f = 0; f < nfreq; f++)
+                out[(size_t)k * nfreq + f] = I[f] * nu3[f];
+        }
     }
     return 0;
 }

@@ -25,6 +25,7 @@ typedef struct port_scene {
     double stepsize;
     double mbh, m_unit, r_high, r_low;
     int integrator; /* 4 = RK4 (integrator.c:13-41), 2 = RK2 (integrator.c:44-70) */
+    int camera;     /* 0 = LINEAR_IMPACT_CAM, 1 = LOG_IMPACT_CAM (parameters.h:54-55) */
 } port_scene;
 
 typedef struct port_ray_stats {
@@ -36,7 +37,8 @@ typedef struct port_ray_stats {
 } port_ray_stats;
 
 /* Render the pixels listed in `pixels` (index x + y*width, core.c:108-109)
- * at nfreq frequencies.  out[k*nfreq + f] = I_f * nu_f^3 (core.c:136).
+ * at nfreq frequencies.  out[k*nfreq + f] = I_f * nu_f^3 (core.c:136), or
+ * I_f nu_f^3 r_i d_r d_theta / D^2 for the log-polar camera (core.c:123-133).
  * stats may be NULL.  nthreads <= 0 uses all OpenMP threads.  Returns 0. */
 int port_render(const port_scene *s, const int *pixels, int n, const double *freqs, int nfreq,
                 double *out, port_ray_stats *stats, int nthreads);

@@ -31,37 +31,39 @@ def sources_present() -> bool:
     return os.path.isfile(os.path.join(REF_SRC_DIR, "integrator.c"))
 
 
-def lib_path(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> str:
-    return os.path.join(HERE, "_ref", f"libraptor_ref_{n1}x{n2}_{rk}_{opt}.so")
+def lib_path(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee", cam: str = "linear") -> str:
+    suffix = "_logcam" if cam == "log" else ""
+    return os.path.join(HERE, "_ref", f"libraptor_ref_{n1}x{n2}_{rk}_{opt}{suffix}.so")
 
 
-def build(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> str:
-    path = lib_path(n1, n2, rk, opt)
+def build(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee", cam: str = "linear") -> str:
+    """cam: "linear" (LINEAR_IMPACT_CAM, the stock camera) or "log" (LOG_IMPACT_CAM)."""
+    path = lib_path(n1, n2, rk, opt, cam)
     if not os.path.exists(path):
         if not sources_present():
             raise FileNotFoundError("reference sources are not present on this machine")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"N1={n1}", f"N2={n2}", f"RK={rk}", f"OPT={opt}",
-                        f"REFDIR={REF_SRC_DIR}"], check=True)
+                        f"CAM={cam}", f"REFDIR={REF_SRC_DIR}"], check=True)
     return path
 
 
-def available(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> bool:
+def available(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee", cam: str = "linear") -> bool:
     """True if a reference library for this grid can be loaded here."""
-    path = lib_path(n1, n2, rk, opt)
+    path = lib_path(n1, n2, rk, opt, cam)
     if not os.path.exists(path) and not sources_present():
         return False
     try:
-        load(n1, n2, rk, opt)
+        load(n1, n2, rk, opt, cam)
         return True
     except OSError:
         return False
 
 
-def load(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee") -> ctypes.CDLL:
-    key = (n1, n2, rk, opt)
+def load(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee", cam: str = "linear") -> ctypes.CDLL:
+    key = (n1, n2, rk, opt, cam)
     if key in _LIBS:
         return _LIBS[key]
-    lib = ctypes.CDLL(build(n1, n2, rk, opt), mode=ctypes.RTLD_LOCAL)
+    lib = ctypes.CDLL(build(n1, n2, rk, opt, cam), mode=ctypes.RTLD_LOCAL)
     D = ctypes.c_double
     P = ctypes.POINTER
     lib.ref_setup.argtypes = [ctypes.c_char_p, ctypes.c_char_p, D, D, D, D, D]
@@ -86,7 +88,7 @@ class RefSession:
 
     def __init__(self, dump_path: str, model, m_unit: float, inclination: float,
                  r_high: float, r_low: float, time_init: float = 0.0, rk: str = "RK4", opt: str = "ieee",
-                 n1: int | None = None, n2: int | None = None, workdir: str | None = None):
+                 n1: int | None = None, n2: int | None = None, workdir: str | None = None, cam: str = "linear"):
         from raptor_gb300.harm import read_dump
         if n1 is None:
             with open(dump_path) as f:
@@ -94,7 +96,7 @@ class RefSession:
             n1, n2 = int(head[1]), int(head[2])
         self.n1, self.n2 = n1, n2
         self.model = model
-        self.lib = load(n1, n2, rk, opt)
+        self.lib = load(n1, n2, rk, opt, cam)
         self._tmp = tempfile.mkdtemp(prefix="rgo_", dir=workdir or "/tmp")
         self.model_path = os.path.join(self._tmp, "model.in")
         model.write(self.model_path)

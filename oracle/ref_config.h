@@ -12,6 +12,8 @@
  *                                  of images larger than 1000x1000
  *                                  (core.c:76,81-83), so it is raised to
  *                                  at least W*H
+ *   LOG_IMPACT_CAM / LINEAR_IMPACT_CAM  parameters.h:54-55, swapped when
+ *                                  REF_LOG_CAM is defined
  *
  * num_indices (parameters.h:215) stays 1: transfer is independent per
  * frequency (radiative_transfer.c:71-98), so the oracle runs one
@@ -41,4 +43,10 @@
 #define N2 (REF_N2)
 #undef maxsize
 #define maxsize (REF_MAXSIZE)
+#ifdef REF_LOG_CAM
+#undef LOG_IMPACT_CAM
+#define LOG_IMPACT_CAM (1)
+#undef LINEAR_IMPACT_CAM
+#define LINEAR_IMPACT_CAM (0)
+#endif
 #endif

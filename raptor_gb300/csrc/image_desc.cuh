@@ -12,6 +12,9 @@ constexpr double kRcam = 1.e4;                 // parameters.h:163
 constexpr double kCutoffOuter = kRcam * 1.01;  // parameters.h:184
 constexpr int kMaxOrder = 100;                 // parameters.h:170
 constexpr double kMaxSteps = 1e5;              // parameters.h:182
+constexpr double kSourceDist = 2.6228263e22;   // parameters.h:144, cm
+constexpr double kTwoPi = 6.283185307179586;   // 2.0 * M_PI, exact
+constexpr int kCamLog = 1;                     // RAPTOR_CAM_LOG
 
 // cgs constants, constants.h:16-29 and j_nu.c:15
 constexpr double kECharge = 4.8032068e-10;
@@ -47,6 +50,12 @@ struct DevImage {
     double freq[kMaxFreqs];
     double nu3[kMaxFreqs];        // freq^3 (core.c:136)
     double rg_over_nu[kMaxFreqs]; // R_g / freq (radiative_transfer.c:88)
+    // log-polar camera (integrator.c:191-198, core.c:123-133)
+    int camera;                   // 0 linear, 1 log-polar
+    double ln20;                  // log(20.)
+    double rgrav;                 // R_GRAV, cm (utilities.c:20)
+    double dtheta_px;             // R_GRAV 2 pi / H
+    double dist2;                 // source_dist^2 (parameters.h:144)
 };
 
 // Per-step record of one traced ray (the analogue of the reference's GEOD

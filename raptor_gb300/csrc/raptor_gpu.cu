@@ -84,6 +84,8 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "n_freq %d out of range 1..%d", d.n_freq, RAPTOR_MAX_FREQS);
     if (d.integrator != RAPTOR_RK4 && d.integrator != RAPTOR_RK2)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "integrator %d is neither RK4 (4) nor RK2 (2)", d.integrator);
+    if (d.camera != RAPTOR_CAM_LINEAR && d.camera != RAPTOR_CAM_LOG)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "camera %d is neither linear (0) nor log-polar (1)", d.camera);
     if (!finite_all({d.cam_size_x, d.cam_size_y, d.inclination, d.mbh, d.m_unit, d.r_high, d.r_low, d.stepsize}) ||
         !(d.stepsize > 0) || !(d.mbh > 0) || !(d.m_unit > 0))
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "non-finite or non-positive image parameter");
@@ -164,6 +166,12 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
     im.inv_stepsize = 1.0 / d.stepsize;
     im.cutoff_inner = (1. + sqrt(1. - a * a)) * (1. + 1e-1);
     const double Rg = kGGrav * d.mbh / kC / kC;
+    // log-polar camera constants (integrator.c:192-198, core.c:123-133, utilities.c:20)
+    im.camera = d.camera;
+    im.ln20 = log(20.);
+    im.rgrav = Rg;
+    im.dtheta_px = Rg * 2. * M_PI / (double)d.height;
+    im.dist2 = kSourceDist * kSourceDist;
     for (int f = 0; f < d.n_freq; ++f) {
         im.freq[f] = d.freq[f];
         im.nu3[f] = pow(d.freq[f], 3.);

@@ -58,17 +58,50 @@ __device__ __forceinline__ CamT<double> camera_of(const DevImage& im) {
                         im.gu03,   im.gu33,  im.gu22,       im.xcam[2], im.k2fac};
 }
 
+// Output factor of a pixel (core.c:121-137): the image holds I nu^3 for the
+// linear camera and I nu^3 r_i d_r d_theta / D^2 for the log-polar one,
+// multiplied in the reference's order.
+struct PixelScale {
+    double r_i = 0.0, d_r = 0.0;
+};
+
+__device__ __forceinline__ PixelScale pixel_scale(const DevImage& im, int x) {
+    PixelScale p;
+    if (im.camera == kCamLog) {
+        p.r_i = exp(__ddiv_rn(__dmul_rn(im.ln20, x + 0.5), (double)im.width)) - 1.0;
+        p.d_r = __ddiv_rn(__dmul_rn(__dmul_rn(im.rgrav, p.r_i + 1.0), im.ln20), (double)im.width);
+    }
+    return p;
+}
+
+__device__ __forceinline__ double scale_output(const DevImage& im, const PixelScale& ps, double v, int f) {
+    double o = v * im.nu3[f];
+    if (im.camera == kCamLog)
+        o = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(o, ps.r_i), ps.d_r), im.dtheta_px), im.dist2);
+    return o;
+}
+
 // Initial photon (metric.c:650-727, GRmath.c:135-184, newtonraphson.c:76-97);
 // the pixel-independent part lives in DevImage / CamT.
 template <class R>
 __device__ __forceinline__ void init_photon(const DevImage& im, const CamT<R>& cam, int x, int yy, R y[8],
                                             double& beta) {
-    // Impact parameters with the multiply and the add rounded separately, as
-    // the reference computes them (integrator.c:190-191, C99 without FMA
-    // contraction): on the middle row of an odd-height image beta is then
-    // exactly 0, and sign(beta) = 0 selects k_theta = 0 (metric.c:669).
-    const double alpha = __dadd_rn(-im.half_x, __dmul_rn(x + 0.5, im.stepx));
-    beta = __dadd_rn(-im.half_y, __dmul_rn(yy + 0.5, im.stepy));
+    // Impact parameters with every operation rounded separately, as the
+    // reference computes them (C99 without FMA contraction): on the middle
+    // row of an odd-height linear image beta is then exactly 0, and
+    // sign(beta) = 0 selects k_theta = 0 (metric.c:669).
+    double alpha;
+    if (im.camera == kCamLog) {  // integrator.c:192-198
+        const double r_i = exp(__ddiv_rn(__dmul_rn(im.ln20, x + 0.5), (double)im.width)) - 1.0;
+        const double th = __ddiv_rn(__dmul_rn(kTwoPi, yy + 0.5), (double)im.height);
+        double sn, cs;
+        sincos(th, &sn, &cs);
+        alpha = r_i * cs;
+        beta = r_i * sn;
+    } else {  // integrator.c:187-190
+        alpha = __dadd_rn(-im.half_x, __dmul_rn(x + 0.5, im.stepx));
+        beta = __dadd_rn(-im.half_y, __dmul_rn(yy + 0.5, im.stepy));
+    }
     const R ll = -alpha * cam.sin_mu;
     const R qq = beta * beta + cam.mu0sq * (alpha * alpha - 1.0);
     const double sg = (beta < 0.0) ? -1.0 : ((beta > 0.0) ? 1.0 : 0.0);
@@ -291,15 +324,16 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
                     if (tr.out && s.rid == tr.ray) trace_record<NF, MIXED>(tr, s, dl, event);
                 }
                 if (done) {
-                    // write intensityfield[pix][f] * nu^3 (core.c:136)
+                    // write intensityfield[pix][f] * nu^3 (core.c:121-137)
                     double* o = out + im->out_offset + (long long)s.pix * im->nfreq;
+                    const PixelScale ps = pixel_scale(*im, s.pix % im->width);
 #pragma unroll
                     for (int f = 0; f < NF; ++f) {
                         if (f >= im->nfreq) break;
                         double v;
                         if constexpr (MIXED) v = ((double)s.If[f] + (double)s.Ic[f]) * kE2C;
                         else v = s.I[f];
-                        o[f] = v * im->nu3[f];
+                        o[f] = scale_output(*im, ps, v, f);
                     }
                     n_steps += (unsigned long long)s.steps;
                     n_rays += 1;

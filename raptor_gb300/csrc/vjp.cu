@@ -247,6 +247,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
         init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
         MksPointT<D1> p;
         mks_point(y[1], y[2], im.geo, p);
+        const PixelScale ps = pixel_scale(im, pix % im.width);
         double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dI[NF][4];
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
@@ -258,8 +259,9 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             for (int q = 0; q < 4; ++q) dtg[f][q] = dI[f][q] = 0.0;
             if (f < im.nfreq) {
                 const long long o = (long long)pix * im.nfreq + f;
-                Itot[f] = fwd[o] / im.nu3[f];
-                w[f] = dLdO[o] * im.nu3[f];
+                const double dOdI = scale_output(im, ps, 1.0, f);
+                Itot[f] = fwd[o] / dOdI;
+                w[f] = dLdO[o] * dOdI;
             }
         }
         int steps = 0, turns = 0, stop = 0;

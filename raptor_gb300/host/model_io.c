@@ -81,6 +81,15 @@ int raptor_read_model(int argc, char **argv, raptor_model *m, char *err, size_t 
         snprintf(err, errlen, "RAPTOR_INT_METHOD must be RK4 or RK2");
         return -1;
     }
+    const char *cam = env_or("RAPTOR_CAMERA", "linear");
+    if (!strcasecmp(cam, "linear"))
+        m->camera = RAPTOR_CAM_LINEAR;
+    else if (!strcasecmp(cam, "log"))
+        m->camera = RAPTOR_CAM_LOG;
+    else {
+        snprintf(err, errlen, "RAPTOR_CAMERA must be linear or log");
+        return -1;
+    }
     const char *pr = env_or("RAPTOR_PRECISION", "fp64");
     if (!strcasecmp(pr, "fp64"))
         m->precision = RAPTOR_PREC_FP64;
@@ -135,10 +144,14 @@ void raptor_set_constants(const raptor_model *m, double a, raptor_units *u)
     double Z2 = pow(3. * a * a + Z1 * Z1, 0.5);
     double retro = a < 0. ? 1. : -1.;
     u->R_ISCO = 3. + Z2 + retro * pow((3. - Z1) * (3. + Z1 + 2. * Z2), 0.5);
-    /* LINEAR_IMPACT_CAM pixel solid angle, utilities.c:32-42 */
-    double d_x = m->CAM_SIZE_X * u->R_GRAV, d_y = m->CAM_SIZE_Y * u->R_GRAV;
-    double delta_x = d_x / SOURCE_DIST, delta_y = d_y / SOURCE_DIST;
-    double pixsize = (delta_x / (double)m->IMG_WIDTH) * (delta_y / (double)m->IMG_HEIGHT);
+    /* pixel solid angle, utilities.c:32-42: LINEAR_IMPACT_CAM from the
+     * camera size; LOG_IMPACT_CAM folds it into the image (core.c:123-133) */
+    double pixsize = 1.;
+    if (m->camera == RAPTOR_CAM_LINEAR) {
+        double d_x = m->CAM_SIZE_X * u->R_GRAV, d_y = m->CAM_SIZE_Y * u->R_GRAV;
+        double delta_x = d_x / SOURCE_DIST, delta_y = d_y / SOURCE_DIST;
+        pixsize = (delta_x / (double)m->IMG_WIDTH) * (delta_y / (double)m->IMG_HEIGHT);
+    }
     u->JANSKY_FACTOR = 1.e23 * pixsize;
 }
 

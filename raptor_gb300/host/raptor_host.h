@@ -9,6 +9,7 @@
  *   RAPTOR_INT_METHOD   RK4 (default) or RK2        parameters.h:189
  *   RAPTOR_NUM_INDICES  frequencies, 1..8 (def. 1) parameters.h:215
  *   RAPTOR_PRECISION    fp64 (default) or mixed
+ *   RAPTOR_CAMERA       linear (default) or log     parameters.h:54-55
  *   RAPTOR_DEVICE       CUDA device ordinal (default 0)
  *   RAPTOR_OUTPUT_DIR   output folder (default "output", core.c:157)
  */
@@ -36,6 +37,7 @@ typedef struct raptor_model {
     double INCLINATION, R_HIGH, R_LOW, TIME_INIT;
     /* engine settings (environment) */
     int num_indices, integrator, precision, device;
+    int camera; /* RAPTOR_CAM_LINEAR or RAPTOR_CAM_LOG (parameters.h:54-55) */
     char output_dir[256];
 } raptor_model;
 

@@ -6,8 +6,9 @@
  *
  * Differences from the reference, all deliberate: every pixel is rendered
  * (the reference drops pixels past index 1e6, core.c:81-83); errors return
- * a non-zero exit status instead of continuing; the integrator and the
- * number of frequencies are run-time settings (raptor_host.h). */
+ * a non-zero exit status instead of continuing; the integrator, the
+ * camera map and the number of frequencies are run-time settings
+ * (raptor_host.h). */
 #define _POSIX_C_SOURCE 200809L
 #include <stdio.h>
 #include <stdlib.h>
@@ -53,6 +54,7 @@ static int calculate_image_gpu(const raptor_model *m, const raptor_dump *d, cons
         img.r_low = m->R_LOW;
         img.stepsize = m->STEPSIZE;
         img.integrator = m->integrator;
+        img.camera = m->camera;
         img.grid = gid;
         img.n_freq = m->num_indices;
         for (int f = 0; f < m->num_indices; f++)

@@ -58,6 +58,13 @@ def quiet():
         os.close(saved[1])
 
 
+# log-polar camera images on the 256x256 torus: name, W, H, inclination, frequency, integrator
+LOGCAM_IMAGES = [
+    ("log_i60_rk4", 64, 48, 60.0, 230e9, "RK4"),
+    ("log_i17_rk2", 40, 33, 17.0, 345e9, "RK2"),
+]
+
+
 def prim_checksum(prims):
     return np.array([np.sum(np.abs(p), dtype=np.float64) for p in prims])
 
@@ -69,11 +76,11 @@ def torus_and_dump(n, tmp, **kw):
     return d, path
 
 
-def ref_image(dump_path, n, w, h, incl, freq, rk, eps, m_unit, rh, rl, pixels=None, threads=0):
+def ref_image(dump_path, n, w, h, incl, freq, rk, eps, m_unit, rh, rl, pixels=None, threads=0, cam="linear"):
     model = harm.ModelIn(MBH=8.9505e39, M_UNIT=m_unit, IMG_WIDTH=w, IMG_HEIGHT=h, CAM_SIZE_X=40.0,
                          CAM_SIZE_Y=40.0, FREQ_MIN=freq, FREQ_MAX=freq, STEPSIZE=eps)
     with quiet():
-        s = ref.RefSession(dump_path, model, m_unit, incl, rh, rl, 0.0, rk=rk, n1=n, n2=n)
+        s = ref.RefSession(dump_path, model, m_unit, incl, rh, rl, 0.0, rk=rk, n1=n, n2=n, cam=cam)
         if pixels is None:
             img, spec, dt = s.render_serial(freq)
             return img, spec, dt
@@ -156,26 +163,26 @@ def kats(dump_path, n):
                 kat_fluid_X=fx, kat_fluid=fluid, kat_fluid_ok=fok)
 
 
-def ref_output_files(dump, img, spec):
-    """The reference's own output_files (core.c:154-200) for the 32x32 image,
-    run in a scratch directory with relative file names, copied to
-    tests/golden/ref_output/."""
+def ref_output_files(dump, img, spec, w=32, h=32, cam="linear", dst_name="ref_output"):
+    """The reference's own output_files (core.c:154-200) for a w x h image of
+    the 64x64 torus, run in a scratch directory with relative file names,
+    copied to tests/golden/<dst_name>/."""
     import shutil
     tmp = tempfile.mkdtemp(prefix="rgo_out_", dir="/tmp")
     harm.write_dump(os.path.join(tmp, "torus64.dump"), dump)
-    model = harm.ModelIn(IMG_WIDTH=32, IMG_HEIGHT=32, FREQ_MIN=230e9, FREQ_MAX=230e9, STEPSIZE=0.05)
+    model = harm.ModelIn(IMG_WIDTH=w, IMG_HEIGHT=h, FREQ_MIN=230e9, FREQ_MAX=230e9, STEPSIZE=0.05)
     cwd = os.getcwd()
     os.chdir(tmp)
     try:
-        lib = ref.load(64, 64, "RK4")
+        lib = ref.load(64, 64, "RK4", cam=cam)
         lib.ref_output_files.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_double, ctypes.c_double]
         with quiet():
-            ref.RefSession("torus64.dump", model, 1e19, 60.0, 3.0, 3.0, 1.0, n1=64, n2=64, workdir=tmp)
+            ref.RefSession("torus64.dump", model, 1e19, 60.0, 3.0, 3.0, 1.0, n1=64, n2=64, workdir=tmp, cam=cam)
             field = np.ascontiguousarray(img, dtype=np.float64)
             lib.ref_output_files(field.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), spec, 230e9)
     finally:
         os.chdir(cwd)
-    dst = os.path.join(OUT, "ref_output")
+    dst = os.path.join(OUT, dst_name)
     os.makedirs(dst, exist_ok=True)
     for fn in os.listdir(os.path.join(tmp, "output")):
         shutil.copy(os.path.join(tmp, "output", fn), os.path.join(dst, fn))
@@ -186,8 +193,31 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--parts", default="small,256,logcam",
+                    help="comma list of fixture groups to write: small, 256, logcam")
     a = ap.parse_args()
+    parts = set(a.parts.split(","))
     tmp = tempfile.mkdtemp(prefix="rgg_", dir="/tmp")
+
+    if "logcam" in parts:
+        # the log-polar camera (LOG_IMPACT_CAM build): stock serial calculate_image,
+        # whose post-scale (core.c:123-133) is part of what is pinned
+        d256, p256 = torus_and_dump(256, tmp)
+        out = dict(prim_checksum=prim_checksum(d256.prims))
+        for (name, w, h, incl, freq, rk) in LOGCAM_IMAGES:
+            img, spec, dt = ref_image(p256, 256, w, h, incl, freq, rk, 0.05, 1e19, 3.0, 3.0, cam="log")
+            out[f"{name}_img"] = img
+            out[f"{name}_spec"] = np.array([spec])
+            out[f"{name}_params"] = np.array([w, h, incl, freq, 4 if rk == "RK4" else 2])
+            print(f"{name}: {dt:.2f} s, flux {spec:.6e}", flush=True)
+        out["names"] = np.array([c[0] for c in LOGCAM_IMAGES])
+        np.savez_compressed(os.path.join(OUT, "logcam_g256.npz"), **out)
+        # the reference's output files of a 32x24 log-polar image of the 64x64 torus
+        d64, p64 = torus_and_dump(64, tmp)
+        img, spec, _ = ref_image(p64, 64, 32, 24, 60.0, 230e9, "RK4", 0.05, 1e19, 3.0, 3.0, cam="log")
+        ref_output_files(d64, img, spec, w=32, h=24, cam="log", dst_name="ref_output_logcam")
+    if "small" not in parts:
+        return
 
     # small grid: several images through the stock serial calculate_image
     d64, p64 = torus_and_dump(64, tmp)
@@ -205,6 +235,8 @@ def main():
     np.savez_compressed(os.path.join(OUT, "small_g64.npz"), **res)
     ref_output_files(d64, res["g64_i60_rk4_img"], res["g64_i60_rk4_spec"][0])
 
+    if "256" not in parts:
+        return
     # the 100x100 image on the 256x256 torus (RK4, eps 0.05, i = 60, 230 GHz)
     d256, p256 = torus_and_dump(256, tmp)
     img, spec, dt = ref_image(p256, 256, 100, 100, 60.0, 230e9, "RK4", 0.05, 1e19, 3.0, 3.0)

@@ -1,7 +1,9 @@
 """The drop-in host program end to end on the GPU: the reference's command
 line, model.in and HARM dump in, the reference's output files out, compared
 with files the reference itself wrote for the same image
-(tests/golden/ref_output, 32x32, i = 60, 230 GHz, 64x64 torus)."""
+(tests/golden/ref_output: 32x32, i = 60, 230 GHz, 64x64 torus;
+tests/golden/ref_output_logcam: the same through a LOG_IMPACT_CAM build,
+32x24)."""
 import os
 import subprocess
 
@@ -12,16 +14,16 @@ from raptor_gb300 import harm
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-GOLD = os.path.join(ROOT, "tests", "golden", "ref_output")
 
-
-def test_host_program_reproduces_reference_files(tmp_path, torus64):
+@pytest.mark.parametrize("gold_name,camera", [("ref_output", "linear"), ("ref_output_logcam", "log")])
+def test_host_program_reproduces_reference_files(tmp_path, torus64, gold_name, camera):
     from raptor_gb300 import build
+    GOLD = os.path.join(ROOT, "tests", "golden", gold_name)
     exe = build.build_host()
     assert exe
     harm.write_dump(tmp_path / "torus64.dump", torus64)
     harm.ModelIn.read(os.path.join(GOLD, "model.in")).write(tmp_path / "model.in")
-    env = dict(os.environ, RAPTOR_INT_METHOD="RK4", RAPTOR_PRECISION="fp64")
+    env = dict(os.environ, RAPTOR_INT_METHOD="RK4", RAPTOR_PRECISION="fp64", RAPTOR_CAMERA=camera)
     r = subprocess.run([exe, "model.in", "torus64.dump", "1e19", "60", "3", "3", "1"], cwd=tmp_path, env=env,
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]

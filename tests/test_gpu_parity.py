@@ -63,6 +63,22 @@ def test_fp64_matches_reference_100x100_on_256(eng, torus256):
     assert spec[0] == pytest.approx(g["spec"][0], rel=1e-6)
 
 
+@pytest.mark.parametrize("name", ["log_i60_rk4", "log_i17_rk2"])
+def test_log_camera_matches_reference(eng, torus256, name):
+    """LOG_IMPACT_CAM: log-polar impact parameters and the r dr dtheta / D^2
+    output scale; FP64 at the parity bar, mixed form within its flux bar."""
+    from raptor_gb300 import engine
+    g = load_golden("logcam_g256.npz")
+    w, h, incl, freq, rk = g[f"{name}_params"]
+    d = engine.image_desc(int(w), int(h), [freq], grid=_grid(eng, torus256), inclination=incl,
+                          integrator=int(rk), camera=engine.CAM_LOG)
+    img, spec = eng.render(d, engine.PREC_FP64)
+    assert_fp64_parity(img, g[f"{name}_img"], name)
+    assert spec[0] == pytest.approx(g[f"{name}_spec"][0], rel=1e-6)
+    _, spec_m = eng.render(d, engine.PREC_MIXED)
+    assert spec_m[0] == pytest.approx(g[f"{name}_spec"][0], rel=FLUX_RTOL_MIXED)
+
+
 def test_fp64_matches_port_and_step_counts(eng, torus64):
     """Step and sample counters agree with the oracle's, ray by ray in sum."""
     from oracle import port

@@ -1,13 +1,19 @@
 """raptor_gpu_vjp against central finite differences: of the engine's own
 FP64 forward render (small case), and of the reference build rerun at
-perturbed parameters (tests/golden/vjp_fd_256.npz, BASELINE configuration 4).
+perturbed parameters (tests/golden/vjp_fd_256.npz: 256x256 image of the
+256x256 torus, loss to a target at M_unit x 1.3, R = 4, i = 62 deg).
 
 Agreement bar: 1e-3 relative; per-cell gradients 1e-3 of the largest per-cell
-finite difference.  Scalars are compared with Richardson-extrapolated
-differences (4 D(h/2) - D(h)) / 3 at h = 1e-4 relative: the plain central
-difference at that step carries an O(h^2) truncation error of ~1e-3 for the
-inclination (with h 10x smaller the engine's own differences agree with the
-VJP to 1e-6, and to 4e-9 at 100x)."""
+finite difference.  M_unit, R_high and R_low are compared with
+Richardson-extrapolated differences (4 D(h/2) - D(h)) / 3 at h = 1e-4
+relative.  The image loss is only piecewise smooth in the inclination (clamps,
+the min() of the step size and cell-index changes along 65,536 rays), so its
+difference quotient at h = 1e-4 sits 0.7 % from the derivative on the 256x256
+image and converges to it only as h shrinks (0.26 % at 1e-5, 2e-5 at 1e-6,
+2e-8 at 1e-7 with the engine's own differences): the inclination gradient is
+checked against the reference's difference at h = 1e-7, and the reference's
+difference at h = 1e-4 is matched by the engine's own (a check of the forward
+sensitivity, not of the VJP)."""
 import numpy as np
 import pytest
 
@@ -93,7 +99,17 @@ def test_vjp_against_reference_finite_differences(torus256):
     bad.check("M_unit", g["d_m_unit"], z["rich_m_unit"][0])
     bad.check("R_high", g["d_r_high"], z["rich_r_high"][0])
     bad.check("R_low", g["d_r_low"], z["rich_r_low"][0])
-    bad.check("inclination", g["d_inclination"], z["rich_incl"][0])
+    bad.check("inclination", g["d_inclination"], z["fd_incl_1e-07"][0])
+    # the engine's own difference quotient at h = 1e-4 against the reference's
+    h = 1e-4 * 60.0
+    op, _ = eng.render(engine.image_desc(256, 256, [230e9], grid=gid, inclination=60.0 + h, m_unit=1e19,
+                                         r_high=3.0, r_low=3.0), engine.PREC_FP64)
+    om, _ = eng.render(engine.image_desc(256, 256, [230e9], grid=gid, inclination=60.0 - h, m_unit=1e19,
+                                         r_high=3.0, r_low=3.0), engine.PREC_FP64)
+    fd_engine = 0.5 * np.sum((op - om) * (op + om - 2 * target)) / (2 * h)
+    if not abs(fd_engine - z["fd_incl"][0]) <= 1e-6 * abs(z["fd_incl"][0]):
+        bad.append(f"inclination difference quotient at h=1e-4: engine {fd_engine:.9e} "
+                   f"vs reference {z['fd_incl'][0]:.9e}")
     cells = z["cells"]
     scale = max(np.max(np.abs(z["fd_rho"])), np.max(np.abs(z["fd_u"])))
     for k, (i, j) in enumerate(cells):

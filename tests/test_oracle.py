@@ -115,3 +115,19 @@ def test_port_vs_reference_fresh_seed(tmp_path):
     sc = port.Scene(d.geom, d.prims, 20, 20, inclination=75.0, m_unit=2e19, r_high=5.0, r_low=2.0)
     out, _ = sc.render([345e9])
     assert_fp64_parity(out[:, 0], img, "fresh seed")
+
+
+@pytest.mark.parametrize("name", ["log_i60_rk4", "log_i17_rk2"])
+def test_port_matches_reference_log_camera(torus256, name):
+    """LOG_IMPACT_CAM build of the reference (parameters.h:54-55): log-polar
+    impact parameters (integrator.c:192-198) and the r dr dtheta / D^2
+    post-scale of calculate_image (core.c:123-133)."""
+    from oracle import port
+    g = load_golden("logcam_g256.npz")
+    from tests.golden.make_golden import prim_checksum
+    np.testing.assert_allclose(prim_checksum(torus256.prims), g["prim_checksum"], rtol=1e-12)
+    w, h, incl, freq, rk = g[f"{name}_params"]
+    sc = port.Scene(torus256.geom, torus256.prims, int(w), int(h), inclination=incl, integrator=int(rk), camera=1)
+    out, _ = sc.render([freq])
+    assert_fp64_parity(out[:, 0], g[f"{name}_img"], name)
+    np.testing.assert_allclose(out[:, 0].sum(), g[f"{name}_spec"][0], rtol=1e-6)

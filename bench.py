@@ -379,13 +379,14 @@ def run_engine(args, rank, world, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    forms = ((engine.PREC_FP64, "fp64"), (engine.PREC_MIXED, "mixed"), (engine.PREC_MIXED_DF, "mixed_df"))
     for _ in range(args.warmup):
-        render_resident(engine.PREC_FP64)
-        render_resident(engine.PREC_MIXED)
+        for prec, _name in forms:
+            render_resident(prec)
 
     results = {}
     with Clocks(dev) as clk:
-        for prec, name in ((engine.PREC_FP64, "fp64"), (engine.PREC_MIXED, "mixed")):
+        for prec, name in forms:
             if barrier:
                 barrier()
             dev_ms, ker_ms, stats = [], [], None
@@ -402,9 +403,13 @@ def run_engine(args, rank, world, local):
     # images of both forms for the mixed-vs-FP64 error report
     img64, spec64 = eng.render(desc, engine.PREC_FP64)
     imgmx, specmx = eng.render(desc, engine.PREC_MIXED)
+    imgdf, specdf = eng.render(desc, engine.PREC_MIXED_DF)
+    kk_df = eng.stats()["kk_max"]
     nz = img64 != 0
     pix_err = np.abs(imgmx[nz] - img64[nz]) / np.abs(img64[nz])
     flux_err = abs(specmx[0] - spec64[0]) / spec64[0]
+    pix_err_df = np.abs(imgdf[nz] - img64[nz]) / np.abs(img64[nz])
+    flux_err_df = abs(specdf[0] - spec64[0]) / spec64[0]
 
     # end to end through the C ABI with host buffers: grid upload (pinned) + render + image read-back
     try:
@@ -436,9 +441,11 @@ def run_engine(args, rank, world, local):
     st = results["fp64"]["stats"]
     t_fp64 = maxed(float(np.mean(results["fp64"]["device_ms"])))
     t_mixed = maxed(float(np.mean(results["mixed"]["device_ms"])))
+    t_mixed_df = maxed(float(np.mean(results["mixed_df"]["device_ms"])))
     t_e2e = maxed(float(np.mean(e2e_ms))) if e2e_ms else None
     e2e_h2d = int(dump.prims.nbytes + e2e_stats["h2d_bytes"])  # grid upload + descriptors
     k_fp64 = float(np.mean(results["fp64"]["kernel_ms"]))
+    k_df = float(np.mean(results["mixed_df"]["kernel_ms"]))
     from raptor_gb300 import workload
     flop = workload.image_flops(st["rays"], st["steps"], st["rt_samples"], 1, rk4=True)
     achieved = flop / (k_fp64 * 1e-3) / 1e12
@@ -466,8 +473,8 @@ def run_engine(args, rank, world, local):
                  "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"]),
                  "path": "raptor_gpu_upload_grid (pinned host prims) + raptor_gpu_render (host image out)"}
                 if t_e2e is not None else None),
-        # timed loop, per render of each form: L2 flush, ray kernel, spectrum kernel
-        "gpu_launches": 3 * 2 * args.steps,
+        # timed loop, per render of each of the three forms: L2 flush, ray kernel, spectrum kernel
+        "gpu_launches": 3 * 3 * args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value if peak.value > 0 else None, "traffic": None,
                      "peak_source": "measured DFMA loop on this GPU (MEASURED_PEAKS.json has no FP64 figure); "
@@ -481,6 +488,16 @@ def run_engine(args, rank, world, local):
                      "launch": [st["block_size"], st["blocks_per_sm"], st["refill_interval"]]},
             "mixed": {"ms_per_image": t_mixed, "speedup_vs_fp64": t_fp64 / t_mixed, "flux_err_vs_fp64": flux_err,
                       "pixel_err_median": float(np.median(pix_err)), "pixel_err_max": float(np.max(pix_err))},
+            "mixed_df": {"ms_per_image": t_mixed_df, "speedup_vs_fp64": t_fp64 / t_mixed_df,
+                         "flux_err_vs_fp64": flux_err_df, "pixel_err_median": float(np.median(pix_err_df)),
+                         "pixel_err_max": float(np.max(pix_err_df)), "kk_max": kk_df,
+                         "geodesic": "double-float (FP32 pairs, 48-bit significand)",
+                         "kernel_ms": k_df,
+                         # the same algorithmic FLOP count as the FP64 form, per second of the DF kernel
+                         "algorithmic_tflops": flop / (k_df * 1e-3) / 1e12,
+                         "vs_fp64_dfma_peak": (flop / (k_df * 1e-3) / 1e12) / peak.value if peak.value > 0 else None,
+                         "launch": [results["mixed_df"]["stats"][k] for k in
+                                    ("block_size", "blocks_per_sm", "refill_interval")]},
             "vjp": vjp,
             "batch": batch,
         },

@@ -41,6 +41,9 @@ extern "C" {
 /* arithmetic forms */
 #define RAPTOR_PREC_FP64 0  /* everything FP64, the reference's arithmetic */
 #define RAPTOR_PREC_MIXED 1 /* FP64 geodesic + metric, FP32 fluid/emission/transfer */
+#define RAPTOR_PREC_MIXED_DF 2 /* geodesic + metric in double-float (pairs of FP32, 48-bit
+                                  significand) on the FP32 pipes, transfer as RAPTOR_PREC_MIXED;
+                                  not for trace_ray */
 
 /* integrators (parameters.h:186-189) */
 #define RAPTOR_RK4 4
@@ -179,8 +182,7 @@ int raptor_gpu_trace_ray(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
  * layout and nu^3 scaling as I_out), returns dL/d(M_UNIT, R_HIGH, R_LOW,
  * INCLINATION) and, if the pointers are set, the per-cell gradients on the
  * image's grid.  precision selects the form of the forward render whose image
- * the adjoint uses (RAPTOR_PREC_FP64 or RAPTOR_PREC_MIXED); the adjoint pass
- * itself runs in FP64.  I_out receives the forward image (may be NULL).
+ * the adjoint uses (any of the three); the adjoint pass itself runs in FP64.  I_out receives the forward image (may be NULL).
  * No counterpart in the reference, which has no derivatives. */
 int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
                    const double *dL_dI, double *I_out, raptor_grad *grad);

@@ -79,9 +79,11 @@ int ctx_fail(raptor_gpu_ctx* ctx, int code, const char* fmt, ...);
 int ensure_buffer(raptor_gpu_ctx* ctx, void** ptr, size_t* cap, size_t bytes);
 int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, raptor::DevImage& im);
 int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs, Batch& b);
-RayLaunchFn pick_ray_kernel(int nf, bool mixed, const void** fn);
+// form: RAPTOR_PREC_FP64, RAPTOR_PREC_MIXED or RAPTOR_PREC_MIXED_DF
+RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn);
+RayLaunchFn pick_ray_kernel_df(int nf, const void** fn);
 LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn);
-LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, RayLaunchFn fn, const void* fnp);
-int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, long long rb, long long re,
+LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunchFn fn, const void* fnp);
+int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, int form, long long rb, long long re,
                    const LaunchShape& ls, RayLaunchFn fn, bool timed, raptor::TraceSpec tr = {-1, nullptr, 0});
 int collect_stats(raptor_gpu_ctx* ctx, bool timed);

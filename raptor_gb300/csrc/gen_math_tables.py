@@ -1,11 +1,14 @@
-"""Generate math_tables.inc: the tables of the table-driven FP64 exp and
-sincospi in fp64_math.cuh, each entry correctly rounded to double.
+"""Generate the tables of the table-driven exp and sincospi:
+math_tables.inc (fp64_math.cuh, each entry correctly rounded to double) and
+df_tables.inc (df64.cuh, each entry as an unevaluated pair hi + lo of FP32
+numbers, hi the value rounded to FP32 and lo the remainder rounded to FP32).
 
     python raptor_gb300/csrc/gen_math_tables.py
 
 Values are computed with Python's decimal module at 50 significant digits
-(Taylor series), then rounded once to the nearest double."""
+(Taylor series), then rounded."""
 import os
+import struct
 from decimal import Decimal, getcontext
 
 getcontext().prec = 50
@@ -41,7 +44,60 @@ def dsincos(x):
             return s, c
 
 
+def f32(x):
+    """Round a Decimal to the nearest FP32 value (through an exact double
+    near it; a double-rounding tie changes hi by one ulp and lo absorbs it)."""
+    return struct.unpack("f", struct.pack("f", float(x)))[0]
+
+
+def split(x):
+    hi = f32(x)
+    lo = f32(x - Decimal(hi))
+    return hi, lo
+
+
+def ffmt(v):
+    return f"{v!r}f" if v != 0 else "0.0f"
+
+
+def write_df_tables(here):
+    lines = ["// Generated by gen_math_tables.py - do not edit.", "",
+             "// 2^(j/64) as (hi, lo) FP32 pairs, j = 0..63", "__device__ const float2 kExp2TableDF[64] = {"]
+    for j in range(64):
+        hi, lo = split(dexp(LN2 * j / 64))
+        lines.append(f"    {{{ffmt(hi)}, {ffmt(lo)}}},")
+    lines.append("};")
+    lines += ["", "// (sin hi, sin lo, cos hi, cos lo) of pi n/128, n = 0..255",
+              "__device__ const float4 kSinCosPiTableDF[256] = {"]
+    for n in range(256):
+        s, c = dsincos(PI * n / 128)
+        sh, sl = split(s)
+        ch, cl = split(c)
+        lines.append(f"    {{{ffmt(sh)}, {ffmt(sl)}, {ffmt(ch)}, {ffmt(cl)}}},")
+    lines.append("};")
+    # constants: pi, ln2/64 split for Cody-Waite reduction, 1/6
+    pih, pil = split(PI)
+    l2 = LN2 / 64
+    # L1 with 12 significant bits so that n * L1 is exact for |n| < 2^12
+    e = 0
+    while Decimal(2) ** (e + 1) <= l2:
+        e += 1
+    while Decimal(2) ** e > l2:
+        e -= 1
+    q = Decimal(2) ** (e - 11)
+    L1 = (l2 / q).to_integral_value(rounding="ROUND_FLOOR") * q
+    L2 = f32(l2 - L1)
+    L3 = f32(l2 - L1 - Decimal(L2))
+    sxh, sxl = split(Decimal(1) / 6)
+    lines += ["", f"constexpr float kPiDFhi = {ffmt(pih)}, kPiDFlo = {ffmt(pil)};",
+              f"constexpr float kLn2by64_1 = {ffmt(f32(L1))};  // 12 significant bits",
+              f"constexpr float kLn2by64_2 = {ffmt(L2)}, kLn2by64_3 = {ffmt(L3)};",
+              f"constexpr float kSixthDFhi = {ffmt(sxh)}, kSixthDFlo = {ffmt(sxl)};"]
+    open(os.path.join(here, "df_tables.inc"), "w").write("\n".join(lines) + "\n")
+
+
 def main():
+    write_df_tables(os.path.dirname(os.path.abspath(__file__)))
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "math_tables.inc")
     lines = ["// Generated by gen_math_tables.py - do not edit.", "",
              "// 2^(j/64), j = 0..63", "__device__ const double kExp2Table[64] = {"]

@@ -56,6 +56,13 @@ struct DevImage {
     double rgrav;                 // R_GRAV, cm (utilities.c:20)
     double dtheta_px;             // R_GRAV 2 pi / H
     double dist2;                 // source_dist^2 (parameters.h:144)
+    // FP32 copies of the transfer sample's constants (mixed forms)
+    float ne_unit_f, b_unit_f, inv_b_unit_f, r_high_f, r_low_f;
+    float freq_f[kMaxFreqs], rg_over_nu_f[kMaxFreqs];
+    // DF copies of the geodesic's constants (mixed-DF form)
+    GeoDF geo_df;
+    DF inv_stepsize_df, cutoff_inner_df;
+    DF startx1_df, startx2_df, stopx1_df, stopx2_df, idx1_df, idx2_df;
 };
 
 // Per-step record of one traced ray (the analogue of the reference's GEOD

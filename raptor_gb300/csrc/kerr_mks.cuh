@@ -14,11 +14,14 @@
 // products U^j U^k), which moves results by rounding only.
 //
 // Everything is templated on the scalar type R: double for the forward
-// kernels, Dual<N> (dual.cuh) for the forward-mode tangents of the adjoint.
+// kernels, Dual<N> (dual.cuh) for the forward-mode tangents of the adjoint,
+// DF (df64.cuh) for the mixed-DF form; and on the constants' type G: Geo
+// (FP64) or GeoDF.
 #pragma once
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include "df_type.cuh"
 #include "fp64_math.cuh"
 
 namespace raptor {
@@ -44,8 +47,8 @@ struct MksPointT {
 };
 using MksPoint = MksPointT<double>;
 
-template <class R>
-__device__ __forceinline__ void mks_point(R x1, R x2, const Geo& g, MksPointT<R>& p) {
+template <class R, class G>
+__device__ __forceinline__ void mks_point(R x1, R x2, const G& g, MksPointT<R>& p) {
     p.rp = fast_exp(x1);
     p.r = g.R0 + p.rp;
     fast_sincospi(2.0 * x2, &p.s2x, &p.c2x);
@@ -61,9 +64,9 @@ __device__ __forceinline__ void mks_point(R x1, R x2, const Geo& g, MksPointT<R>
 
 // d^2 x^i / d lambda^2 = -Gamma^i_jk U^j U^k  (integrator.c:126-146 with the
 // MKS connection of metric.c:538-638).
-template <class R>
-__device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const Geo& g, const R U[4], R A[4]) {
-    const double a = g.a, a2 = g.a2;
+template <class R, class G>
+__device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g, const R U[4], R A[4]) {
+    const auto a = g.a, a2 = g.a2;
     const R r = p.r, r2 = r * r;
     const R rp = p.rp, rp2 = rp * rp;
     const R thp = CUDART_PI * fma(g.one_m_h, p.c2x, 1.0);
@@ -152,10 +155,10 @@ struct MetricUUT {
 using MetricDD = MetricDDT<double>;
 using MetricUU = MetricUUT<double>;
 
-template <class R>
-__device__ __forceinline__ void mks_metric(const MksPointT<R>& p, const Geo& g, MetricDDT<R>& d, MetricUUT<R>& u) {
+template <class R, class G>
+__device__ __forceinline__ void mks_metric(const MksPointT<R>& p, const G& g, MetricDDT<R>& d, MetricUUT<R>& u) {
     const R r = p.r;
-    const double a = g.a;
+    const auto a = g.a;
     const R s2 = p.s * p.s;
     const R irho2 = p.iS;
     const R rfac = r - g.R0;

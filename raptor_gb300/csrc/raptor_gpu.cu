@@ -176,7 +176,26 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
         im.freq[f] = d.freq[f];
         im.nu3[f] = pow(d.freq[f], 3.);
         im.rg_over_nu[f] = Rg / d.freq[f];
+        im.freq_f[f] = (float)im.freq[f];
+        im.rg_over_nu_f[f] = (float)im.rg_over_nu[f];
     }
+    im.ne_unit_f = (float)im.Ne_unit;
+    im.b_unit_f = (float)im.B_unit;
+    im.inv_b_unit_f = (float)im.inv_B_unit;
+    im.r_high_f = (float)im.r_high;
+    im.r_low_f = (float)im.r_low;
+    // DF copies for the mixed-DF geodesic
+    im.geo_df = GeoDF{df_const(im.geo.a),       df_const(im.geo.a2),      df_const(im.geo.hslope),
+                      df_const(im.geo.R0),      df_const(im.geo.one_m_h), df_const(im.geo.th_coef),
+                      df_const(im.geo.half_1mh)};
+    im.inv_stepsize_df = df_const(im.inv_stepsize);
+    im.cutoff_inner_df = df_const(im.cutoff_inner);
+    im.startx1_df = df_const(im.startx1);
+    im.startx2_df = df_const(im.startx2);
+    im.stopx1_df = df_const(im.stopx1);
+    im.stopx2_df = df_const(im.stopx2);
+    im.idx1_df = df_const(im.idx1);
+    im.idx2_df = df_const(im.idx2);
     return RAPTOR_OK;
 }
 
@@ -378,7 +397,9 @@ static void launch_ray(const LaunchShape& ls, cudaStream_t st, const DevImage* i
     ray_kernel<NF, MIXED><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
 }
 
-RayLaunchFn pick_ray_kernel(int nf, bool mixed, const void** fn) {
+RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn) {
+    if (form == RAPTOR_PREC_MIXED_DF) return pick_ray_kernel_df(nf, fn);
+    const bool mixed = form == RAPTOR_PREC_MIXED;
     // one instantiation per frequency-count bucket so tau/I stay in registers
 #define PICK(NF)                                                        \
     if (nf <= NF) {                                                     \
@@ -463,7 +484,7 @@ LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn) {
 
 // Enqueue the whole render (counters reset, ray kernel, spectrum) on the
 // context stream; used directly and under stream capture.
-int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, long long rb, long long re,
+int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, int form, long long rb, long long re,
                    const LaunchShape& ls, RayLaunchFn fn, bool timed, TraceSpec tr) {
     if (timed) CK(cudaEventRecord(ctx->evA, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_counters, 0, kCtrCount * sizeof(unsigned long long), ctx->stream));
@@ -510,11 +531,11 @@ int collect_stats(raptor_gpu_ctx* ctx, bool timed) {
 // buffers it touches - and relaunched while the signature repeats; the
 // per-image descriptors are uploaded before every launch, so their contents
 // (angles, frequencies, units, grids of the same size) may change freely.
-int graph_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, const LaunchShape& ls, RayLaunchFn fn,
+int graph_render(raptor_gpu_ctx* ctx, const Batch& b, int form, const LaunchShape& ls, RayLaunchFn fn,
                  bool* replayed) {
     char key[512];
     snprintf(key, sizeof key, "%d|%lld|%lld|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p", b.n, b.total_rays, b.out_len,
-             b.spec_len, b.max_nf, (int)mixed, ls.grid, ls.block, ls.refill, (void*)fn, (void*)ctx->d_imgs,
+             b.spec_len, b.max_nf, form, ls.grid, ls.block, ls.refill, (void*)fn, (void*)ctx->d_imgs,
              (void*)ctx->d_out, (void*)ctx->d_spec, (void*)ctx->d_spec_map, (void*)ctx->d_counters);
     *replayed = ctx->graph_exec && ctx->graph_key == key;
     if (!*replayed) {
@@ -524,7 +545,7 @@ int graph_render(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, const LaunchSh
         }
         cudaGraph_t graph = nullptr;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_render(ctx, b, mixed, 0, b.total_rays, ls, fn, false);
+        const int rc = enqueue_render(ctx, b, form, 0, b.total_rays, ls, fn, false);
         cudaError_t ec = cudaStreamEndCapture(ctx->stream, &graph);
         if (rc) {
             if (graph) cudaGraphDestroy(graph);
@@ -553,7 +574,7 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     if (!ctx) return RAPTOR_ERR_INVALID;
     ctx->err[0] = 0;
     auto t0 = std::chrono::steady_clock::now();
-    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED)
+    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED && precision != RAPTOR_PREC_MIXED_DF)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "precision %d unknown", precision);
     CK(cudaSetDevice(ctx->device));
     cudaGetLastError();  // a failed earlier call must not fail this one
@@ -563,15 +584,15 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     long long rb = ray_begin < 0 ? 0 : ray_begin;
     long long re = ray_count < 0 ? b.total_rays : std::min(b.total_rays, rb + ray_count);
     if (rb > b.total_rays) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "ray range starts past the batch");
-    const bool mixed = precision == RAPTOR_PREC_MIXED;
+    const int form = precision;
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, mixed, &fnp);
-    LaunchShape ls = choose_shape(ctx, b, mixed, fn, fnp);
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, form, &fnp);
+    LaunchShape ls = choose_shape(ctx, b, form, fn, fnp);
     bool replayed = false;
     if (ctx->opt.use_graph && rb == 0 && re == b.total_rays) {
-        rc = graph_render(ctx, b, mixed, ls, fn, &replayed);
+        rc = graph_render(ctx, b, form, ls, fn, &replayed);
     } else {
-        rc = enqueue_render(ctx, b, mixed, rb, re, ls, fn, true);
+        rc = enqueue_render(ctx, b, form, rb, re, ls, fn, true);
     }
     if (rc) return rc;
     size_t d2h = 0;
@@ -633,12 +654,12 @@ extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc
     if (rc) return rc;
     CK(cudaMemsetAsync(ctx->d_trace, 0, bytes, ctx->stream));
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision == RAPTOR_PREC_MIXED, &fnp);
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp);
     LaunchShape ls = default_shape(ctx, fnp);
     ls.grid = 1;
     ls.block = 32;
     TraceSpec tr{pixel, ctx->d_trace, max_records};
-    rc = enqueue_render(ctx, b, precision == RAPTOR_PREC_MIXED, pixel, pixel + 1, ls, fn, true, tr);
+    rc = enqueue_render(ctx, b, precision, pixel, pixel + 1, ls, fn, true, tr);
     if (rc) return rc;
     CK(cudaMemcpyAsync(records, ctx->d_trace, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

@@ -134,8 +134,8 @@ __device__ __forceinline__ R step_size(const DevImage& im, const R y[8]) {
     return -fmax(1.0 / (i1 + i2 + i3), 1e-12);
 }
 
-template <class R>
-__device__ __forceinline__ void rhs(const MksPointT<R>& p, const Geo& g, const R ys[8], R f[8]) {
+template <class R, class G>
+__device__ __forceinline__ void rhs(const MksPointT<R>& p, const G& g, const R ys[8], R f[8]) {
     f[0] = ys[4];
     f[1] = ys[5];
     f[2] = ys[6];
@@ -149,8 +149,8 @@ __device__ __forceinline__ void rhs(const MksPointT<R>& p, const Geo& g, const R
 // Stages 2-4 run as one rolled loop: the stage body (point transcendentals,
 // 40 Christoffels, contraction) is large, and one copy of it instead of
 // three keeps the kernel's hot loop inside the instruction cache.
-template <class R>
-__device__ __forceinline__ void rk4_step(const Geo& g, R y[8], MksPointT<R>& p, R dt) {
+template <class R, class G>
+__device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R dt) {
     R acc[8], ys[8], f[8];
     rhs(p, g, y, f);
 #pragma unroll
@@ -164,8 +164,9 @@ __device__ __forceinline__ void rk4_step(const Geo& g, R y[8], MksPointT<R>& p, 
         MksPointT<R> qp;
         mks_point(ys[1], ys[2], g, qp);
         rhs(qp, g, ys, f);
-        const double wacc = (q == 3) ? 1.0 : 2.0;   // k2, k3 count twice
-        const double wnext = (q == 1) ? 0.5 : 1.0;  // stage weights 1/2, 1/2, 1
+        using W = typename StageWeight<R>::type;
+        const W wacc = (q == 3) ? W(1.0) : W(2.0);   // k2, k3 count twice
+        const W wnext = (q == 1) ? W(0.5) : W(1.0);  // stage weights 1/2, 1/2, 1
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const R d = dt * f[i];
@@ -178,9 +179,46 @@ __device__ __forceinline__ void rk4_step(const Geo& g, R y[8], MksPointT<R>& p, 
     mks_point(y[1], y[2], g, p);
 }
 
+// The same RK4 step with all four stages and the end point's evaluation in
+// one rolled loop, so the stage body (point transcendentals, Christoffels,
+// contraction) exists once.  Same operations in the same order as rk4_step.
+// For the double-float state, where each operation is about ten FP32
+// instructions, the single copy keeps the hot loop from stalling on
+// instruction fetch.
+template <class R, class G>
+__device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>& p, R dt) {
+    using W = typename StageWeight<R>::type;
+    R acc[8], ys[8], f[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) ys[i] = y[i];
+    MksPointT<R> qp = p;
+#pragma unroll 1
+    for (int q = 0;; ++q) {
+        if (q > 0) mks_point(ys[1], ys[2], g, qp);
+        if (q == 4) break;
+        rhs(qp, g, ys, f);
+        const W wacc = (q == 1 || q == 2) ? W(2.0) : W(1.0);  // k2, k3 count twice
+        const W wnext = (q < 2) ? W(0.5) : W(1.0);           // stage weights 1/2, 1/2, 1
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const R d = dt * f[i];
+            acc[i] = (q == 0) ? d : acc[i] + d * wacc;
+            ys[i] = y[i] + d * wnext;
+        }
+        if (q == 3) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                y[i] = y[i] + 1.0 / 6.0 * acc[i];
+                ys[i] = y[i];
+            }
+        }
+    }
+    p = qp;
+}
+
 // RK2 midpoint step (integrator.c:44-70).
-template <class R>
-__device__ __forceinline__ void rk2_step(const Geo& g, R y[8], MksPointT<R>& p, R dt) {
+template <class R, class G>
+__device__ __forceinline__ void rk2_step(const G& g, R y[8], MksPointT<R>& p, R dt) {
     R ys[8], f[8];
     rhs(p, g, y, f);
 #pragma unroll

@@ -1,0 +1,275 @@
+// The mixed-DF form: the geodesic (RK steps, step size, point
+// transcendentals, Christoffels, the sample's metric) in double-float
+// arithmetic (df64.cuh, 48-bit significand on the FP32 pipes), the transfer
+// sample in FP32 with compensated sums exactly as the mixed form's.
+//
+// Same loop as ray_kernel (ray_kernel.cuh, integrator.c:149-289): the
+// persistent grid, the ray queue with warp-aggregated refills, termination,
+// theta-turn limit and transfer gating.  FP64 is used only per ray: the
+// camera set-up (init_photon), the output write and the k.k drift.
+#include <cuda_runtime.h>
+
+#include "df64.cuh"
+#include "engine_internal.h"
+#include "ray_kernel.cuh"
+
+namespace raptor {
+namespace {
+
+template <int NF>
+struct RayStateDF {
+    DF y[8];
+    MksPointT<DF> p;
+    float thdot_prev;
+    long long rid;
+    int bsign, steps, turns, stop, img, pix;
+    float tf[NF], tc[NF], If[NF], Ic[NF];
+};
+
+// stepsize (integrator.c:109-122), as step_size in ray_kernel.cuh
+__device__ __forceinline__ DF step_size_df(const DevImage& im, const DF y[8]) {
+    const float t = 1.e-40f;
+    const DF m2 = fmin(y[2], 1.0 - y[2]);
+    const DF i1 = add_f(fabs(y[5]), t) * im.inv_stepsize_df;
+    const DF i2 = add_f(fabs(y[6]), t) * im.inv_stepsize_df / m2;
+    const DF i3 = add_f(fabs(y[7]), t) * im.inv_stepsize_df;
+    return -fmax(1.0 / (i1 + i2 + i3), df_const(1e-12));
+}
+
+// mks_point (kerr_mks.cuh) for DF states, with the two sincospi evaluations
+// (of 2 x2, then of theta / pi) through one copy of the code.
+__device__ __forceinline__ void mks_point(DF x1, DF x2, const GeoDF& g, MksPointT<DF>& p) {
+    p.rp = fast_exp(x1);
+    p.r = g.R0 + p.rp;
+    DF arg = 2.0 * x2, sv, cv;
+#pragma unroll 1
+    for (int k = 0;; ++k) {
+        fast_sincospi(arg, &sv, &cv);
+        if (k == 1) break;
+        p.s2x = sv;
+        p.c2x = cv;
+        // theta = pi x2 + (1-h)/2 sin(2 pi x2) (metric.c:98), as theta / pi
+        arg = fma(g.th_coef, sv, x2);
+    }
+    p.s = sv;
+    p.c = cv;
+    const DF Sg = fma(p.r, p.r, g.a2 * p.c * p.c);
+    const DF thp = CUDART_PI * fma(g.one_m_h, p.c2x, 1.0);
+    p.iS = 1.0 / Sg;
+    p.irp = 1.0 / p.rp;
+    p.ithp = 1.0 / thp;
+    p.isn = 1.0 / p.s;
+}
+
+// The sample's metric (metric.c:94-137, 207-231 as mks_metric) in FP32 from
+// the point's leading parts: it only feeds the FP32 fluid and tetrad
+// projection.
+__device__ __forceinline__ MetricT<float> metric_f32(const MksPointT<DF>& p, const GeoDF& gd) {
+    const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
+    const float r = p.r.hi, s = p.s.hi, c = p.c.hi, irho2 = p.iS.hi;
+    const float s2 = s * s;
+    const float rfac = r - R0;
+    const float hfac = 3.14159265f * fmaf(gd.one_m_h.hi, p.c2x.hi, 1.0f);
+    const float rho2 = fmaf(r, r, a2 * c * c);
+    const float z = 2.0f * r * irho2;
+    const float ir = (R0 == 0.0f) ? p.irp.hi : 1.0f / r;
+    MetricT<float> g;
+    g.d00 = -1.0f + z;
+    g.d01 = z * rfac;
+    g.d03 = -a * z * s2;
+    g.d11 = (1.0f + z) * rfac * rfac;
+    g.d13 = -a * s2 * (1.0f + z) * rfac;
+    g.d22 = rho2 * hfac * hfac;
+    g.d33 = s2 * (rho2 + a2 * s2 * (1.0f + z));
+    g.u00 = -1.0f - z;
+    g.u01 = 2.0f * irho2;
+    g.u11 = irho2 * (r * (r - 2.0f) + a2) * (ir * ir);
+    g.u13 = a * irho2 * ir;
+    g.u22 = irho2 * (p.ithp.hi * p.ithp.hi);
+    g.u33 = irho2 * (p.isn.hi * p.isn.hi);
+    return g;
+}
+
+// trunc toward zero of hi + lo (the reference's (int) cast in Xtoij)
+__device__ __forceinline__ int df_trunc(DF t) {
+    int i = (int)t.hi;
+    if ((float)i == t.hi) {
+        if (t.hi > 0.0f && t.lo < 0.0f) i -= 1;
+        else if (t.hi < 0.0f && t.lo > 0.0f) i += 1;
+    }
+    return i;
+}
+
+// One transfer sample: Xtoij (grmhd.c:46-71) from the DF position, the
+// metric in FP32, the rest as the mixed form's FP32 sample.
+template <int NF>
+__device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], const MksPointT<DF>& p, float adl,
+                                             float (&tau)[NF], float (&tauc)[NF], float (&I)[NF],
+                                             float (&Ic)[NF]) {
+    const MetricT<float> g = metric_f32(p, im.geo_df);
+    const DF t1 = (y[1] - im.startx1_df) * im.idx1_df - 0.5;
+    const DF t2 = (y[2] - im.startx2_df) * im.idx2_df - 0.5;
+    int i = df_trunc(t1), j = df_trunc(t2);
+    float d1, d2;
+    if (i < 0) { i = 0; d1 = 0.0f; }
+    else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = 1.0f; }
+    else d1 = add_f(t1, (float)-i).hi;
+    if (j < 0) { j = 0; d2 = 0.0f; }
+    else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = 1.0f; }
+    else d2 = add_f(t2, (float)-j).hi;
+    float v[8];
+    interp_prims_at(im.cells32, im.n2, i * im.n2 + j, d1, d2, v);
+    const float k[4] = {y[4].hi, y[5].hi, y[6].hi, y[7].hi};
+    return rt_sample_fp32_core<NF>(im, g, v, k, [&](int f) { return adl * im.rg_over_nu_f[f]; }, tau, tauc, I,
+                                   Ic);
+}
+
+// 4 blocks of 128 (16 warps) per SM: the DF arithmetic is FP32-latency bound,
+// and 16 warps at 128 registers (a few hundred bytes of spills) ran 1.4x
+// faster than 8 warps at 196 registers without spills (1024x1024 image).
+#ifndef RAPTOR_RAY_DF_MIN_BLOCKS
+#define RAPTOR_RAY_DF_MIN_BLOCKS 4
+#endif
+
+template <int NF>
+__global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
+    ray_kernel_df(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
+                  unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval) {
+    const int lane = threadIdx.x & 31;
+    RayStateDF<NF> s;
+    bool active = false, live = true;
+    const DevImage* im = imgs;
+    unsigned long long n_steps = 0, n_rt_calls = 0, n_rt_samples = 0, n_rays = 0, n_cap = 0, n_nan = 0;
+    unsigned long long max_steps = 0;
+    double kk_max = 0.0;
+    const DF cut_outer = df_const(kCutoffOuter);
+
+    while (true) {
+        const unsigned need = __ballot_sync(kFull, !active && live);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (!active && live) {
+                const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
+                if (rid < ray_end) {
+                    s.img = find_image(imgs, n_imgs, rid);
+                    im = imgs + s.img;
+                    s.pix = (int)(rid - im->ray_begin);
+                    s.rid = rid;
+                    // camera set-up in FP64 (once per ray), then the DF state
+                    double y0[8], beta;
+                    init_photon(*im, camera_of(*im), s.pix % im->width, s.pix / im->width, y0, beta);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) s.y[i] = df_const(y0[i]);
+                    s.bsign = (beta < 0.0) ? -1 : ((beta > 0.0) ? 1 : 0);
+                    mks_point(s.y[1], s.y[2], im->geo_df, s.p);
+                    s.steps = 0;
+                    s.turns = 0;
+                    s.stop = 0;
+                    s.thdot_prev = 0.0f;
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
+                    }
+                    active = true;
+                } else {
+                    live = false;
+                }
+            }
+        }
+        if (!__any_sync(kFull, active)) break;
+        if (active) {
+            for (int it = 0; it < refill_interval; ++it) {
+                // while-condition of integrator.c:228-229
+                const DF r = s.p.rp;
+                bool done = !(r < cut_outer && r > im->cutoff_inner_df && s.steps < (int)kMaxSteps && !s.stop);
+                if (!done) {
+                    // theta turning points (integrator.c:243-247)
+                    const float th = s.y[6].hi;
+                    if (((s.thdot_prev < 0.0f && th > 0.0f) || (s.thdot_prev > 0.0f && th < 0.0f)) && s.steps > 2)
+                        s.turns += 1;
+                    s.thdot_prev = th;
+                    if ((s.bsign < 0 && s.turns > kMaxOrder) || (s.bsign > 0 && s.turns > kMaxOrder + 1)) s.stop = 1;
+                    const DF dl = step_size_df(*im, s.y);
+                    if (im->integrator == 2) rk2_step(im->geo_df, s.y, s.p, dl);
+                    else rk4_step_rolled(im->geo_df, s.y, s.p, dl);
+                    s.steps += 1;
+                    if (s.y[1] > im->stopx1_df && s.y[5].hi < 0.0f) {
+                        done = true;  // escaped outward (integrator.c:271-272)
+                    } else if (s.y[1] < im->stopx1_df && s.y[1] > im->startx1_df && s.y[2] > im->startx2_df &&
+                               s.y[2] < im->stopx2_df) {
+                        ++n_rt_calls;
+                        const bool sampled = rt_sample_df<NF>(*im, s.y, s.p, -dl.hi, s.tf, s.tc, s.If, s.Ic);
+                        n_rt_samples += sampled ? 1 : 0;
+                    }
+                }
+                if (done) {
+                    double* o = out + im->out_offset + (long long)s.pix * im->nfreq;
+                    const PixelScale ps = pixel_scale(*im, s.pix % im->width);
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        if (f >= im->nfreq) break;
+                        o[f] = scale_output(*im, ps, ((double)s.If[f] + (double)s.Ic[f]) * kE2C, f);
+                    }
+                    n_steps += (unsigned long long)s.steps;
+                    n_rays += 1;
+                    if ((double)s.steps >= kMaxSteps) ++n_cap;
+                    if (!(s.p.rp.hi == s.p.rp.hi) || !isfinite(s.y[5].hi)) ++n_nan;
+                    max_steps = max(max_steps, (unsigned long long)s.steps);
+                    // k.k drift in FP64 at the final state (once per ray)
+                    double yd[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) yd[i] = df_to_double(s.y[i]);
+                    MksPoint pd;
+                    mks_point(yd[1], yd[2], im->geo, pd);
+                    const double kk = null_drift(pd, im->geo, yd);
+                    if (kk == kk) kk_max = fmax(kk_max, kk);
+                    active = false;
+                    break;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_steps += __shfl_xor_sync(kFull, n_steps, o);
+        n_rt_calls += __shfl_xor_sync(kFull, n_rt_calls, o);
+        n_rt_samples += __shfl_xor_sync(kFull, n_rt_samples, o);
+        n_rays += __shfl_xor_sync(kFull, n_rays, o);
+        n_cap += __shfl_xor_sync(kFull, n_cap, o);
+        n_nan += __shfl_xor_sync(kFull, n_nan, o);
+        max_steps = max(max_steps, __shfl_xor_sync(kFull, max_steps, o));
+        kk_max = fmax(kk_max, __shfl_xor_sync(kFull, kk_max, o));
+    }
+    if (lane == 0) {
+        atomicAdd(&counters[kCtrSteps], n_steps);
+        atomicAdd(&counters[kCtrRtCalls], n_rt_calls);
+        atomicAdd(&counters[kCtrRtSamples], n_rt_samples);
+        atomicAdd(&counters[kCtrRays], n_rays);
+        atomicAdd(&counters[kCtrStepCap], n_cap);
+        atomicAdd(&counters[kCtrNonFinite], n_nan);
+        atomicMax(&counters[kCtrMaxSteps], max_steps);
+        atomicMax(&counters[kCtrKkMax], (unsigned long long)__double_as_longlong(kk_max));
+    }
+}
+
+template <int NF>
+void launch_ray_df(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b, long long e,
+                   unsigned long long* ctr, double* out, TraceSpec) {
+    ray_kernel_df<NF><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill);
+}
+
+}  // namespace
+}  // namespace raptor
+
+using namespace raptor;
+
+RayLaunchFn pick_ray_kernel_df(int nf, const void** fn) {
+    if (nf <= 1) { *fn = (const void*)ray_kernel_df<1>; return launch_ray_df<1>; }
+    if (nf <= 2) { *fn = (const void*)ray_kernel_df<2>; return launch_ray_df<2>; }
+    if (nf <= 4) { *fn = (const void*)ray_kernel_df<4>; return launch_ray_df<4>; }
+    *fn = (const void*)ray_kernel_df<8>;
+    return launch_ray_df<8>;
+}

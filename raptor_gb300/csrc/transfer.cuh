@@ -65,19 +65,23 @@ __device__ __forceinline__ void load_cell(const float* __restrict__ c, float v[8
 // Bilinear interpolation of all eight primitives, coefficient order of
 // raptor_harm_model.c:213-216 and term order of grmhd.c:38-41.
 template <class T>
-__device__ __forceinline__ void interp_prims(const T* __restrict__ cells, int n2, const CellCoef& cc,
-                                             T v[8]) {
-    const T d1 = (T)cc.d1, d2 = (T)cc.d2;
+__device__ __forceinline__ void interp_prims_at(const T* __restrict__ cells, int n2, int base, T d1, T d2,
+                                                T v[8]) {
     const T c0 = (T(1) - d1) * (T(1) - d2), c1 = (T(1) - d1) * d2;
     const T c2 = d1 * (T(1) - d2), c3 = d1 * d2;
     T a[8], b[8], e[8], f[8];
-    const T* p = cells + (size_t)cc.base * 8;
+    const T* p = cells + (size_t)base * 8;
     load_cell(p, a);
     load_cell(p + 8, b);
     load_cell(p + (size_t)n2 * 8, e);
     load_cell(p + (size_t)n2 * 8 + 8, f);
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = a[q] * c0 + b[q] * c1 + e[q] * c2 + f[q] * c3;
+}
+template <class T>
+__device__ __forceinline__ void interp_prims(const T* __restrict__ cells, int n2, const CellCoef& cc,
+                                             T v[8]) {
+    interp_prims_at(cells, n2, cc.base, (T)cc.d1, (T)cc.d2, v);
 }
 
 template <class T>
@@ -225,28 +229,21 @@ __device__ __forceinline__ void neumaier_add(float& s, float& c, float x) {
     s = t;
 }
 
-template <int NF>
-__device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double y[8], const MksPoint& p,
-                                               double adl, float (&tau)[NF], float (&tauc)[NF],
-                                               float (&I)[NF], float (&Ic)[NF]) {
-    MetricDD gd;
-    MetricUU gu;
-    mks_metric(p, im.geo, gd, gu);
-    const MetricT<float> g = metric_cast<float>(gd, gu);
-    const CellCoef cc = cell_coef(im, y[1], y[2]);
-    float v[8];
-    interp_prims(im.cells32, im.n2, cc, v);
+// The FP32 sample from the metric, the interpolated primitives and the
+// photon wave vector in FP32.  dlf_of(f) gives |d lambda| R_g / nu_f.
+template <int NF, class DlfOf>
+__device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const MetricT<float>& g, const float v[8],
+                                                    const float k[4], DlfOf dlf_of, float (&tau)[NF],
+                                                    float (&tauc)[NF], float (&I)[NF], float (&Ic)[NF]) {
     Fluid<float> fl;
-    if (!fluid_from_prims(v, g, (float)im.Ne_unit, (float)im.B_unit, (float)im.r_high, (float)im.r_low, fl))
-        return false;
-    const float k[4] = {(float)y[4], (float)y[5], (float)y[6], (float)y[7]};
+    if (!fluid_from_prims(v, g, im.ne_unit_f, im.b_unit_f, im.r_high_f, im.r_low_f, fl)) return false;
     float kd[4];
     lowerT(g, k, kd);
     const float* U = fl.ucon;
     const float* Bc = fl.bcon;
     const float kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
     float pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) /
-                  (fabsf(kU) * (fl.B * (float)im.inv_B_unit));
+                  (fabsf(kU) * (fl.B * im.inv_b_unit_f));
     if (fabsf(pitch) > 1.0f) pitch /= fabsf(pitch);
     const float sth = sqrtf(1.0f - pitch * pitch);
     const float nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
@@ -259,10 +256,10 @@ __device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double 
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
         if (f >= im.nfreq) break;
-        float nup = -kU * (float)im.freq[f];
+        float nup = -kU * im.freq_f[f];
         if (nup <= 0.0f) nup = 1.0f;
         if (!(emits && nup != 1.0f)) continue;
-        const float dlf = (float)(adl * im.rg_over_nu[f]);
+        const float dlf = dlf_of(f);
         const float X = nup / nus;
         const float cb = cbrtf(X);
         const float sq = sqrtf(X) + 1.8877486f * sqrtf(cb);
@@ -275,6 +272,23 @@ __device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double 
         if (t < 6.9077553f && !(t < 0.0f)) neumaier_add(I[f], Ic[f], dI);
     }
     return true;
+}
+
+// Mixed form: metric and cell coefficients from the FP64 geodesic state.
+template <int NF>
+__device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double y[8], const MksPoint& p,
+                                               double adl, float (&tau)[NF], float (&tauc)[NF],
+                                               float (&I)[NF], float (&Ic)[NF]) {
+    MetricDD gd;
+    MetricUU gu;
+    mks_metric(p, im.geo, gd, gu);
+    const MetricT<float> g = metric_cast<float>(gd, gu);
+    const CellCoef cc = cell_coef(im, y[1], y[2]);
+    float v[8];
+    interp_prims(im.cells32, im.n2, cc, v);
+    const float k[4] = {(float)y[4], (float)y[5], (float)y[6], (float)y[7]};
+    return rt_sample_fp32_core<NF>(im, g, v, k, [&](int f) { return (float)(adl * im.rg_over_nu[f]); }, tau,
+                                   tauc, I, Ic);
 }
 
 }  // namespace raptor

@@ -26,10 +26,10 @@ using raptor::TraceSpec;
 
 namespace {
 
-std::string signature(const raptor_gpu_ctx* ctx, const Batch& b, bool mixed) {
+std::string signature(const raptor_gpu_ctx* ctx, const Batch& b, int form) {
     char k[384];
     const int size_class = (int)std::log2((double)std::max<long long>(b.total_rays, 1));
-    snprintf(k, sizeof k, "%s|%s|nf%d|2^%d", ctx->device_name, mixed ? "mixed" : "fp64", b.max_nf, size_class);
+    snprintf(k, sizeof k, "%s|%s|nf%d|2^%d", ctx->device_name, form == RAPTOR_PREC_MIXED_DF ? "mixed_df" : (form == RAPTOR_PREC_MIXED ? "mixed" : "fp64"), b.max_nf, size_class);
     std::string s(k);
     for (char& c : s)
         if (c == ' ') c = '_';
@@ -59,11 +59,11 @@ void save_file_cache(const std::string& key, const LaunchShape& ls) {
 
 }  // namespace
 
-LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, bool mixed, RayLaunchFn fn, const void* fnp) {
+LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunchFn fn, const void* fnp) {
     LaunchShape base = default_shape(ctx, fnp);
     if (!ctx->opt.autotune) return base;
     load_file_cache(ctx);
-    const std::string key = signature(ctx, b, mixed);
+    const std::string key = signature(ctx, b, form);
     auto it = ctx->tuned.find(key);
     if (it != ctx->tuned.end()) {
         LaunchShape ls = it->second;

@@ -57,20 +57,22 @@ __device__ __forceinline__ D6 lift(const D1& a) {
     return r;
 }
 
-template <int NF>
-struct SampleTerms {
-    D6 S[NF], dtau[NF];
+// The frequency-independent part of one transfer sample, as value + six
+// tangents: the same arithmetic as rt_sample_fp64 (get_fluid_params
+// raptor_harm_model.c:190-290, pitch_angle radiative_transfer.c:32-47,
+// j_nu.c:130-153, 188-200) up to the frequency loop.
+struct SampleCommon {
+    D6 kU;        // k_mu u^mu
+    D6 nus;       // nu_s
+    D6 pre;       // n_e sqrt(2) pi nu_s / (3 K2), the first factors of j
+    D6 kT;        // k_B T
+    D6 adl;       // |d lambda|
     double dlnth_du;  // d ln Theta_e / d u_s
-    bool emit[NF], poison[NF];
+    bool emits;
 };
 
-// One transfer sample as value + six tangents: the same arithmetic as
-// rt_sample_fp64 (get_fluid_params raptor_harm_model.c:190-290,
-// pitch_angle radiative_transfer.c:32-47, j_nu.c:130-153, 188-200), split
-// into the per-frequency terms S and delta of the tau / I recurrence.
-template <int NF>
-__device__ bool sample_terms(const DevImage& im, const D1& x1, const D1& x2, const D1 k1[4], const MksPointT<D1>& p,
-                             const D1& adl1, CellCoef& cc, SampleTerms<NF>& out) {
+__device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, const D1 k1[4], const MksPointT<D1>& p,
+                              const D1& adl1, CellCoef& cc, SampleCommon& out) {
     MetricDDT<D1> gd1;
     MetricUUT<D1> gu1;
     mks_metric(p, im.geo, gd1, gu1);
@@ -120,42 +122,41 @@ __device__ bool sample_terms(const DevImage& im, const D1& x1, const D1& x2, con
     lowerT(g, k, kd);
     const D6* U = fl.ucon;
     const D6* Bc = fl.bcon;
-    const D6 kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    D6 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(kU) * fl.B / B_unit);
+    out.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
+    D6 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * fl.B / B_unit);
     if (fabs(pitch.v) > 1.0) pitch = D6(pitch.v > 0 ? 1.0 : -1.0);
     const D6 s2 = 1.0 - pitch * pitch;
     const D6 sth = s2.v > 0.0 ? sqrt(s2) : D6(0.0);
     const D6 nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
-    const D6 nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
-    const bool emits = (fabs(sth.v) >= 1.e-10) && (fl.thetae.v > 1e-4);
+    out.nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
+    out.emits = (fabs(sth.v) >= 1.e-10) && (fl.thetae.v > 1e-4);
     const D6 K2 = 2.0 * fl.thetae * fl.thetae;
-    const D6 T = fl.thetae * (kEMass * kC * kC / kBoltz);
-    const D6 adl = lift(adl1);
-#pragma unroll
-    for (int fi = 0; fi < NF; ++fi) {
-        out.emit[fi] = false;
-        out.poison[fi] = false;
-        if (fi >= im.nfreq) break;
-        D6 nup = -kU * im.freq[fi];
-        if (nup.v <= 0.0) nup = D6(1.0);
-        const D6 dlf = adl * im.rg_over_nu[fi];
-        if (emits && nup.v != 1.0) {
-            const D6 X = nup / nus;
-            const D6 cb = cbrt(X);
-            const D6 sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);
-            const D6 jn = fl.ne * (1.4142135623730951 * CUDART_PI) * nus / (3.0 * K2) * (sq * sq) * exp(-cb) * kE2C;
-            const D6 Bnu = 2.0 * nup * nup * nup / (kC * kC) / (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
-            const D6 an = jn * kE2CH / Bnu / kE2C;
-            out.dtau[fi] = nup * an * dlf;
-            out.S[fi] = jn / (nup * nup) * dlf;
-            out.emit[fi] = true;
-        } else {
-            const double Bnu = 2.0 * nup.v * nup.v * nup.v / (kC * kC) * 1.0 /
-                               (exp(kPlanck * nup.v / (kBoltz * T.v)) - 1.0);
-            out.poison[fi] = !(Bnu != 0.0);  // the primal's 0/0 (transfer.cuh)
-        }
-    }
+    out.pre = fl.ne * (1.4142135623730951 * CUDART_PI) * out.nus / (3.0 * K2);
+    out.kT = kBoltz * (fl.thetae * (kEMass * kC * kC / kBoltz));
+    out.adl = lift(adl1);
     return true;
+}
+
+// The terms S and delta of the tau / I recurrence at frequency fi.
+// Returns 1 if the frequency emits, 2 where the primal's tau turns NaN
+// (0/0 in a with B_nu underflowed, transfer.cuh), else 0.
+__device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommon& sc, int fi, D6& S, D6& dtau) {
+    D6 nup = -sc.kU * im.freq[fi];
+    if (nup.v <= 0.0) nup = D6(1.0);
+    if (sc.emits && nup.v != 1.0) {
+        const D6 dlf = sc.adl * im.rg_over_nu[fi];
+        const D6 X = nup / sc.nus;
+        const D6 cb = cbrt(X);
+        const D6 sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);
+        const D6 jn = sc.pre * (sq * sq) * exp(-cb) * kE2C;
+        const D6 Bnu = 2.0 * nup * nup * nup / (kC * kC) / (exp(kPlanck * nup / sc.kT) - 1.0);
+        const D6 an = jn * kE2CH / Bnu / kE2C;
+        dtau = nup * an * dlf;
+        S = jn / (nup * nup) * dlf;
+        return 1;
+    }
+    const double Bnu = 2.0 * nup.v * nup.v * nup.v / (kC * kC) * 1.0 / (exp(kPlanck * nup.v / sc.kT.v) - 1.0);
+    return !(Bnu != 0.0) ? 2 : 0;
 }
 
 // Inclination-dependent camera constants with their tangent per degree.
@@ -248,7 +249,9 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
         MksPointT<D1> p;
         mks_point(y[1], y[2], im.geo, p);
         const PixelScale ps = pixel_scale(im, pix % im.width);
-        double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dI[NF][4];
+        // per frequency: tau, the forward I, the part of I accumulated so far,
+        // dL/dI and d tau / d(scalars); dIw = sum over frequencies of dL/dI dI/d(scalars)
+        double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dIw[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
             tau[f] = 0.0;
@@ -256,7 +259,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             Itot[f] = 0.0;
             w[f] = 0.0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) dtg[f][q] = dI[f][q] = 0.0;
+            for (int q = 0; q < 4; ++q) dtg[f][q] = 0.0;
             if (f < im.nfreq) {
                 const long long o = (long long)pix * im.nfreq + f;
                 const double dOdI = scale_output(im, ps, 1.0, f);
@@ -279,19 +282,19 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             if (y[1].v > im.stopx1 && y[5].v < 0.0) break;
             if (y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2) {
                 ++n_calls;
-                SampleTerms<NF> st;
+                SampleCommon sc;
                 CellCoef cc;
                 const D1 k1[4] = {y[4], y[5], y[6], y[7]};
-                if (sample_terms<NF>(im, y[1], y[2], k1, p, fabs(dl), cc, st)) {
+                if (sample_common(im, y[1], y[2], k1, p, fabs(dl), cc, sc)) {
                     ++n_samples;
                     double Gr = 0.0, Gt = 0.0;
 #pragma unroll
                     for (int f = 0; f < NF; ++f) {
                         if (f >= im.nfreq) break;
-                        if (st.emit[f]) {
+                        D6 S, dt;
+                        const int kind = sample_freq(im, sc, f, S, dt);
+                        if (kind == 1) {
                             ++n_emit;
-                            const D6& S = st.S[f];
-                            const D6& dt = st.dtau[f];
                             tau[f] += dt.v;
 #pragma unroll
                             for (int q = 0; q < 4; ++q) dtg[f][q] += dt.d[gdir(q)];
@@ -305,15 +308,16 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                             }
                             if (gate) {
                                 ++n_gate;
+                                const double we = w[f] * e;
 #pragma unroll
-                                for (int q = 0; q < 4; ++q) dI[f][q] += e * (S.d[gdir(q)] - S.v * dtg[f][q]);
+                                for (int q = 0; q < 4; ++q) dIw[q] += we * (S.d[gdir(q)] - S.v * dtg[f][q]);
                                 Ipart[f] += S.v * e;
                             }
-                        } else if (st.poison[f]) {
+                        } else if (kind == 2) {
                             tau[f] = __longlong_as_double(0x7ff8000000000000ll);
                         }
                     }
-                    const double Gu = Gt * st.dlnth_du;
+                    const double Gu = Gt * sc.dlnth_du;
                     if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
                         const double w0 = (1.0 - cc.d1) * (1.0 - cc.d2), w1 = (1.0 - cc.d1) * cc.d2;
                         const double w2 = cc.d1 * (1.0 - cc.d2), w3 = cc.d1 * cc.d2;
@@ -335,10 +339,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             }
         }
 #pragma unroll
-        for (int f = 0; f < NF; ++f)
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (isfinite(dI[f][q])) acc[q] += w[f] * dI[f][q];
+        for (int q = 0; q < 4; ++q)
+            if (isfinite(dIw[q])) acc[q] += dIw[q];
         atomicAdd(&counters[kCtrSteps], (unsigned long long)steps);
         atomicAdd(&counters[kCtrRays], 1ull);
     }
@@ -375,9 +377,8 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     if (!ctx) return RAPTOR_ERR_INVALID;
     ctx->err[0] = 0;
     if (!img || !dL_dI || !grad) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: null image, dL_dI or grad");
-    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED)
-        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: precision %d is neither FP64 (0) nor mixed (1)", precision);
-    const bool mixed = precision == RAPTOR_PREC_MIXED;
+    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED && precision != RAPTOR_PREC_MIXED_DF)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: precision %d unknown", precision);
     auto t0 = std::chrono::steady_clock::now();
     CK(cudaSetDevice(ctx->device));
     cudaGetLastError();
@@ -390,9 +391,9 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
 
     // forward render (its image is the I of the suffix identity)
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, mixed, &fnp);
-    LaunchShape ls = choose_shape(ctx, b, mixed, fn, fnp);
-    rc = enqueue_render(ctx, b, mixed, 0, b.total_rays, ls, fn, true);
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp);
+    LaunchShape ls = choose_shape(ctx, b, precision, fn, fnp);
+    rc = enqueue_render(ctx, b, precision, 0, b.total_rays, ls, fn, true);
     if (rc) return rc;
 
     const size_t nout = (size_t)b.out_len;
@@ -416,6 +417,7 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     if (b.max_nf <= 1) { vfn = launch_vjp<1>; kp = (const void*)vjp_kernel<1>; }
     else if (b.max_nf <= 2) { vfn = launch_vjp<2>; kp = (const void*)vjp_kernel<2>; }
     else if (b.max_nf <= 4) { vfn = launch_vjp<4>; kp = (const void*)vjp_kernel<4>; }
+    else if (b.max_nf <= 5) { vfn = launch_vjp<5>; kp = (const void*)vjp_kernel<5>; }
     else { vfn = launch_vjp<8>; kp = (const void*)vjp_kernel<8>; }
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
     const int grid = ctx->num_sms * std::max(occ, 1);

@@ -22,6 +22,7 @@ RAPTOR_MAX_FREQS = 8
 RAPTOR_MAX_GRIDS = 16
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_MIXED_DF = 2
 RK4 = 4
 RK2 = 2
 CAM_LINEAR = 0

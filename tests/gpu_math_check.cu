@@ -8,6 +8,7 @@
 #include <cmath>
 #include <vector>
 
+#include "df64.cuh"
 #include "fp64_math.cuh"
 
 __global__ void eval(const double* x, int n, double* out) {
@@ -22,6 +23,27 @@ __global__ void eval(const double* x, int n, double* out) {
     out[6 * i + 3] = s1;
     out[6 * i + 4] = c0;
     out[6 * i + 5] = c1;
+}
+
+// The double-float (hi + lo FP32 pairs) exp and sincospi of df64.cuh, and
+// DF division, against CUDA's FP64 functions; relative errors.
+__global__ void eval_df(const double* x, int n, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xe = fabs(x[i]) * (10.0 / 30.0);  // x1 = ln r in [0, 10]
+    const raptor::DF de = raptor::df_const(xe);
+    const raptor::DF ds = raptor::df_const(x[i] * (1.0 / 14.0));  // [-2.1, 2.1]
+    raptor::DF s0, c0;
+    raptor::fast_sincospi(ds, &s0, &c0);
+    double s1, c1;
+    sincospi(raptor::df_to_double(ds), &s1, &c1);
+    const double e1 = exp(raptor::df_to_double(de));
+    const raptor::DF q = de / ds;
+    out[4 * i + 0] = fabs(raptor::df_to_double(raptor::fast_exp(de)) - e1) / e1;
+    out[4 * i + 1] = fabs(raptor::df_to_double(s0) - s1);
+    out[4 * i + 2] = fabs(raptor::df_to_double(c0) - c1);
+    const double qd = raptor::df_to_double(de) / raptor::df_to_double(ds);
+    out[4 * i + 3] = fabs(raptor::df_to_double(q) - qd) / fabs(qd);
 }
 
 static double ulps(double a, double b) {
@@ -58,7 +80,17 @@ int main() {
         abs_s = fmax(abs_s, fabs(o[6 * i + 2] - o[6 * i + 3]));
         abs_c = fmax(abs_c, fabs(o[6 * i + 4] - o[6 * i + 5]));
     }
-    printf("exp_ulp %g sin_ulp %g cos_ulp %g sin_abs %g cos_abs %g err %s\n", me, ms, mc, abs_s, abs_c,
-           cudaGetErrorString(cudaGetLastError()));
+    eval_df<<<(n + 255) / 256, 256>>>(dx, n, dout);
+    cudaMemcpy(o.data(), dout, 4 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+    double df_e = 0, df_s = 0, df_c = 0, df_q = 0;
+    for (int i = 0; i < n; ++i) {
+        df_e = fmax(df_e, o[4 * i]);
+        df_s = fmax(df_s, o[4 * i + 1]);
+        df_c = fmax(df_c, o[4 * i + 2]);
+        if (std::isfinite(o[4 * i + 3])) df_q = fmax(df_q, o[4 * i + 3]);
+    }
+    printf("exp_ulp %g sin_ulp %g cos_ulp %g sin_abs %g cos_abs %g df_exp_rel %g df_sin_abs %g df_cos_abs %g "
+           "df_div_rel %g err %s\n",
+           me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, cudaGetErrorString(cudaGetLastError()));
     return 0;
 }

@@ -1,6 +1,9 @@
 """The engine's table-driven FP64 exp and sincospi (csrc/fp64_math.cuh)
 against CUDA's exp and sincospi, on the GPU: <= 2 ulp, and sin/cos within
-2.3e-16 absolute near their zeros (where ulp counts are meaningless)."""
+2.3e-16 absolute near their zeros (where ulp counts are meaningless).  The
+double-float versions (csrc/df64.cuh) against the same FP64 functions:
+exp, sin and cos within 2e-14 (a few units of the 48-bit significand), the
+division (one correction step, ~2^-45) within 5e-14."""
 import os
 import subprocess
 
@@ -21,3 +24,6 @@ def test_fast_math_against_cuda(tmp_path):
     assert vals["err"] == "no"
     assert float(vals["exp_ulp"]) <= 2
     assert float(vals["sin_abs"]) <= 2.3e-16 and float(vals["cos_abs"]) <= 2.3e-16
+    assert float(vals["df_exp_rel"]) <= 2e-14
+    assert float(vals["df_sin_abs"]) <= 2e-14 and float(vals["df_cos_abs"]) <= 2e-14
+    assert float(vals["df_div_rel"]) <= 5e-14

@@ -106,6 +106,37 @@ def test_mixed_flux_within_1e4(eng, torus256):
     assert np.median(err) < 1e-4
 
 
+@pytest.mark.parametrize("integrator", [4, 2])
+def test_mixed_df_against_fp64_and_reference(eng, torus256, integrator):
+    """Mixed-DF form (double-float geodesic on the FP32 pipes, FP32 transfer):
+    total flux within the mixed form's 1e-4 of the reference; the image
+    agrees with the FP64 form pixel by pixel as closely as the mixed form
+    does (its error is the FP32 transfer's, not the geodesic's), and the
+    geodesic itself follows the FP64 one: same step and sample counts to
+    0.1 %, the same null-condition drift."""
+    from raptor_gb300 import engine
+    g = load_golden("img100_g256.npz")
+    gid = _grid(eng, torus256)
+    params = np.array(g["params"])
+    params[4] = integrator
+    desc = _desc(params, gid)
+    i64, s64 = eng.render(desc, engine.PREC_FP64)
+    st64 = eng.stats()
+    imx, smx = eng.render(desc, engine.PREC_MIXED)
+    idf, sdf = eng.render(desc, engine.PREC_MIXED_DF)
+    stdf = eng.stats()
+    if integrator == 4:
+        assert abs(sdf[0] - g["spec"][0]) / g["spec"][0] <= FLUX_RTOL_MIXED
+    assert abs(sdf[0] - s64[0]) / s64[0] <= FLUX_RTOL_MIXED
+    err_df = pixel_errors(idf, i64)
+    err_mx = pixel_errors(imx, i64)
+    assert np.median(err_df) <= 2 * np.median(err_mx) + 1e-7
+    assert abs(stdf["steps"] - st64["steps"]) <= 1e-3 * st64["steps"]
+    assert abs(stdf["rt_samples"] - st64["rt_samples"]) <= 1e-3 * st64["rt_samples"]
+    assert stdf["rays"] == i64.size and stdf["n_nonfinite"] == 0
+    assert stdf["kk_max"] <= 1.01 * st64["kk_max"] + 1e-12
+
+
 def test_deterministic(eng, torus64):
     from raptor_gb300 import engine
     gid = _grid(eng, torus64)
@@ -189,3 +220,5 @@ def test_1024_on_512_against_reference(eng, incl):
     assert abs(spec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= 1e-6
     mimg, mspec = eng.render(desc, engine.PREC_MIXED)
     assert abs(mspec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= FLUX_RTOL_MIXED
+    _, dspec = eng.render(desc, engine.PREC_MIXED_DF)
+    assert abs(dspec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= FLUX_RTOL_MIXED

@@ -95,8 +95,10 @@ int raptor_read_model(int argc, char **argv, raptor_model *m, char *err, size_t 
         m->precision = RAPTOR_PREC_FP64;
     else if (!strcasecmp(pr, "mixed"))
         m->precision = RAPTOR_PREC_MIXED;
+    else if (!strcasecmp(pr, "mixed_df"))
+        m->precision = RAPTOR_PREC_MIXED_DF;
     else {
-        snprintf(err, errlen, "RAPTOR_PRECISION must be fp64 or mixed");
+        snprintf(err, errlen, "RAPTOR_PRECISION must be fp64, mixed or mixed_df");
         return -1;
     }
     m->device = atoi(env_or("RAPTOR_DEVICE", "0"));

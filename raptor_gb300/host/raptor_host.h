@@ -8,7 +8,7 @@
  * compile time are environment variables here:
  *   RAPTOR_INT_METHOD   RK4 (default) or RK2        parameters.h:189
  *   RAPTOR_NUM_INDICES  frequencies, 1..8 (def. 1) parameters.h:215
- *   RAPTOR_PRECISION    fp64 (default) or mixed
+ *   RAPTOR_PRECISION    fp64 (default), mixed or mixed_df
  *   RAPTOR_CAMERA       linear (default) or log     parameters.h:54-55
  *   RAPTOR_DEVICE       CUDA device ordinal (default 0)
  *   RAPTOR_OUTPUT_DIR   output folder (default "output", core.c:157)

@@ -65,6 +65,13 @@ LOGCAM_IMAGES = [
 ]
 
 
+# one image per dump of the batched configuration: name, W, H, inclination, frequency, integrator, M_unit
+BATCH_DUMP_IMAGES = [
+    ("a05_i120_345", 48, 40, 120.0, 345e9, "RK4", 3e18),
+    ("a09375_i25_86", 40, 48, 25.0, 86e9, "RK4", 5e19),
+]
+
+
 def prim_checksum(prims):
     return np.array([np.sum(np.abs(p), dtype=np.float64) for p in prims])
 
@@ -193,11 +200,29 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--parts", default="small,256,logcam",
-                    help="comma list of fixture groups to write: small, 256, logcam")
+    ap.add_argument("--parts", default="small,256,logcam,batchdumps",
+                    help="comma list of fixture groups to write: small, 256, logcam, batchdumps")
     a = ap.parse_args()
     parts = set(a.parts.split(","))
     tmp = tempfile.mkdtemp(prefix="rgg_", dir="/tmp")
+
+    if "batchdumps" in parts:
+        # the two dumps of the batched configuration (a = 0.5 and a = 0.9375,
+        # their own seeds), one image each with batch-like parameters
+        from raptor_gb300 import workloads
+        out = {}
+        for k, d in enumerate(workloads.batch_dumps(256)):
+            path = os.path.join(tmp, f"batch{k}.dump")
+            harm.write_dump(path, d)
+            name, w, h, incl, freq, rk, mu = BATCH_DUMP_IMAGES[k]
+            img, spec, dt = ref_image(path, 256, w, h, incl, freq, rk, 0.05, mu, 3.0, 3.0)
+            out[f"{name}_img"] = img
+            out[f"{name}_spec"] = np.array([spec])
+            out[f"{name}_params"] = np.array([w, h, incl, freq, 4 if rk == "RK4" else 2, 0.05, mu, 3.0, 3.0])
+            out[f"{name}_prim_checksum"] = prim_checksum(d.prims)
+            print(f"{name}: {dt:.2f} s, flux {spec:.6e}", flush=True)
+        out["names"] = np.array([c[0] for c in BATCH_DUMP_IMAGES])
+        np.savez_compressed(os.path.join(OUT, "batch_dumps_g256.npz"), **out)
 
     if "logcam" in parts:
         # the log-polar camera (LOG_IMPACT_CAM build): stock serial calculate_image,

@@ -79,6 +79,24 @@ def test_log_camera_matches_reference(eng, torus256, name):
     assert spec_m[0] == pytest.approx(g[f"{name}_spec"][0], rel=FLUX_RTOL_MIXED)
 
 
+@pytest.mark.parametrize("k,name", [(0, "a05_i120_345"), (1, "a09375_i25_86")])
+def test_batch_dumps_match_reference(eng, k, name):
+    """The batched configuration's two dumps (a = 0.5 and a = 0.9375), one
+    reference image each: FP64 at the parity bar; both mixed forms within
+    the flux bar."""
+    from raptor_gb300 import engine, workloads
+    g = load_golden("batch_dumps_g256.npz")
+    d = workloads.batch_dumps(256)[k]
+    gid = _grid(eng, d)
+    desc = _desc(g[f"{name}_params"], gid)
+    img, spec = eng.render(desc, engine.PREC_FP64)
+    assert_fp64_parity(img, g[f"{name}_img"], name)
+    assert spec[0] == pytest.approx(g[f"{name}_spec"][0], rel=1e-6)
+    for prec in (engine.PREC_MIXED, engine.PREC_MIXED_DF):
+        _, sm = eng.render(desc, prec)
+        assert sm[0] == pytest.approx(g[f"{name}_spec"][0], rel=FLUX_RTOL_MIXED), prec
+
+
 def test_fp64_matches_port_and_step_counts(eng, torus64):
     """Step and sample counters agree with the oracle's, ray by ray in sum."""
     from oracle import port

@@ -131,3 +131,20 @@ def test_port_matches_reference_log_camera(torus256, name):
     out, _ = sc.render([freq])
     assert_fp64_parity(out[:, 0], g[f"{name}_img"], name)
     np.testing.assert_allclose(out[:, 0].sum(), g[f"{name}_spec"][0], rtol=1e-6)
+
+
+@pytest.mark.parametrize("k,name", [(0, "a05_i120_345"), (1, "a09375_i25_86")])
+def test_port_matches_reference_batch_dumps(k, name):
+    """The two dumps of the batched configuration (a = 0.5 and a = 0.9375 with
+    their own seeds): one image each, M_unit 3e18 (optically thin) and 5e19
+    (optically thick at 86 GHz)."""
+    from oracle import port
+    from raptor_gb300 import workloads
+    from tests.golden.make_golden import prim_checksum
+    g = load_golden("batch_dumps_g256.npz")
+    d = workloads.batch_dumps(256)[k]
+    np.testing.assert_allclose(prim_checksum(d.prims), g[f"{name}_prim_checksum"], rtol=1e-12)
+    sc, freq = _scene(d, g[f"{name}_params"])
+    out, _ = sc.render([freq])
+    assert_fp64_parity(out[:, 0], g[f"{name}_img"], name)
+    np.testing.assert_allclose(out[:, 0].sum(), g[f"{name}_spec"][0], rtol=1e-6)

@@ -182,8 +182,10 @@ def workload_config():
 
 def run_vjp_config4(reps=3):
     """Adjoint configuration: 256x256 image of the 256x256 torus, loss = L2
-    distance to a target at M_unit x 1.3, R = 4, i = 62 deg.  Reports the
-    FP64 forward and VJP (forward pass + adjoint pass) device times."""
+    distance to a target at M_unit x 1.3, R = 4, i = 62 deg.  Reports, for
+    the FP64 form and for the mixed-DF form, the forward and VJP (forward
+    pass + adjoint pass) device times; the mixed-DF gradients are compared
+    with the FP64 ones."""
     from raptor_gb300 import engine, synth
     d = synth.make_torus(n1=256, n2=256)
     eng = engine.Engine()
@@ -191,17 +193,24 @@ def run_vjp_config4(reps=3):
     desc = engine.image_desc(256, 256, [FREQ], grid=gid, inclination=60.0)
     target, _ = eng.render(engine.image_desc(256, 256, [FREQ], grid=gid, inclination=62.0, m_unit=1.3e19,
                                              r_high=4.0, r_low=4.0), engine.PREC_FP64)
-    fwd, vjp, grads = [], [], None
-    for _ in range(reps):
-        img, _ = eng.render(desc, engine.PREC_FP64)
-        fwd.append(eng.stats()["device_ms"])
-        _, grads = eng.vjp(desc, img - target, engine.PREC_FP64)
-        vjp.append(eng.stats()["device_ms"])
+    keys = ("d_m_unit", "d_r_high", "d_r_low", "d_inclination")
+    out = {"config": "256x256 image, 256x256 torus, i=60, 230 GHz; loss to target at M_unit*1.3, R=4, i=62"}
+    grads = {}
+    for prec, name in ((engine.PREC_FP64, "fp64"), (engine.PREC_MIXED_DF, "mixed_df")):
+        fwd, vjp = [], []
+        for _ in range(reps):
+            img, _ = eng.render(desc, prec)
+            fwd.append(eng.stats()["device_ms"])
+            _, grads[name] = eng.vjp(desc, img - target, prec)
+            vjp.append(eng.stats()["device_ms"])
+        f, v = min(fwd), min(vjp)
+        out[name] = {"fwd_ms": f, "vjp_ms": v, "ratio": v / f, "grad": {k: grads[name][k] for k in keys}}
+    out["mixed_df"]["grad_rel_diff_vs_fp64"] = {
+        k: abs(grads["mixed_df"][k] - grads["fp64"][k]) / abs(grads["fp64"][k]) for k in keys}
     eng.close()
-    f, v = min(fwd), min(vjp)
-    return {"config": "256x256 image, 256x256 torus, i=60, 230 GHz; loss to target at M_unit*1.3, R=4, i=62",
-            "fwd_ms": f, "vjp_ms": v, "ratio": v / f,
-            "grad": {k: grads[k] for k in ("d_m_unit", "d_r_high", "d_r_low", "d_inclination")}}
+    # the FP64 numbers stay at the top level
+    out.update(fwd_ms=out["fp64"]["fwd_ms"], vjp_ms=out["fp64"]["vjp_ms"], ratio=out["fp64"]["ratio"])
+    return out
 
 
 def run_batch_config3(dev):
@@ -273,6 +282,15 @@ def run_differentiable(dev, n_cells=4, reps=2):
         adj_ms.append(st["kernel_ms"])
         vjp_ms.append(st["device_ms"])
     peak = eng.stats()["peak_device_bytes"]
+    # the same with the mixed-DF forward and its adjoint
+    fwd_df, adj_df, vjp_df = [], [], []
+    for _ in range(reps):
+        eng.render(mk(), engine.PREC_MIXED_DF)
+        fwd_df.append(eng.stats()["device_ms"])
+        _, gdf = eng.vjp(mk(), dl, engine.PREC_MIXED_DF)
+        st = eng.stats()
+        adj_df.append(st["kernel_ms"])
+        vjp_df.append(st["device_ms"])
 
     # finite differences of the FP64 forward
     def fd_scalar(key, rel, richardson):
@@ -289,17 +307,20 @@ def run_differentiable(dev, n_cells=4, reps=2):
     for key, gk in (("m_unit", "d_m_unit"), ("r_high", "d_r_high"), ("r_low", "d_r_low"),
                     ("inclination", "d_inclination")):
         fd = fd_scalar(key, 1e-4, key == "inclination")
-        scal[key] = {"vjp": g[gk], "fd": fd, "rel_err": abs(g[gk] - fd) / abs(fd)}
+        scal[key] = {"vjp": g[gk], "fd": fd, "rel_err": abs(g[gk] - fd) / abs(fd),
+                     "vjp_df": gdf[gk], "rel_err_df": abs(gdf[gk] - fd) / abs(fd)}
     # the loss is only piecewise smooth in the inclination (clamps, min() in the
     # step size, cell-index changes along every ray): its difference quotient
     # reaches the derivative only as h shrinks
     for rel in (1e-6, 1e-7):
         fd = fd_scalar("inclination", rel, False)
         scal[f"inclination_h{rel:g}"] = {"vjp": g["d_inclination"], "fd": fd,
-                                         "rel_err": abs(g["d_inclination"] - fd) / abs(fd)}
+                                         "rel_err": abs(g["d_inclination"] - fd) / abs(fd),
+                                         "vjp_df": gdf["d_inclination"],
+                                         "rel_err_df": abs(gdf["d_inclination"] - fd) / abs(fd)}
     cells = {}
     order = np.argsort(-np.abs(g["d_rho"]).ravel())[:n_cells]
-    fd_all, vjp_all = [], []
+    fd_all, vjp_all, vjp_all_df = [], [], []
     for flat in order:
         i, j = divmod(int(flat), d.geom.n2)
         for q, field in ((0, "d_rho"), (1, "d_u")):
@@ -312,13 +333,16 @@ def run_differentiable(dev, n_cells=4, reps=2):
             eng.upload_grid(d.geom, pr, grid_id=gid)
             om, _ = eng.render(mk(), engine.PREC_FP64)
             fd = _loss_delta(op, om, target) / (2e-4 * v)
-            cells[f"{field}[{i},{j}]"] = {"vjp": float(g[field][i, j]), "fd": fd}
+            cells[f"{field}[{i},{j}]"] = {"vjp": float(g[field][i, j]), "vjp_df": float(gdf[field][i, j]),
+                                          "fd": fd}
             fd_all.append(fd)
             vjp_all.append(float(g[field][i, j]))
+            vjp_all_df.append(float(gdf[field][i, j]))
     eng.upload_grid(d.geom, d.prims, grid_id=gid)
     fd_s = time.perf_counter() - t0
     scale = max(abs(x) for x in fd_all)
     cell_err = max(abs(a - b) for a, b in zip(vjp_all, fd_all)) / scale
+    cell_err_df = max(abs(a - b) for a, b in zip(vjp_all_df, fd_all)) / scale
     # uniform Theta_e factor = change of T_p/T_e at R_high = R_low = R
     R = base["r_high"]
     tg = 0.5 * ((1.0 + 2.0 / 3.0 * (R + 1.0) / (R + 2.0)) + 4.0 / 3.0)
@@ -335,6 +359,10 @@ def run_differentiable(dev, n_cells=4, reps=2):
                    "forward": "mixed", "adjoint": "fp64 (forward-mode tangents + suffix identity, no checkpoints)"},
         "forward_ms": f, "adjoint_kernel_ms": a, "vjp_total_ms": v, "adjoint_over_forward": a / f,
         "vjp_total_over_forward": v / f, "peak_device_bytes": peak,
+        "mixed_df": {"forward_ms": min(fwd_df), "adjoint_kernel_ms": min(adj_df), "vjp_total_ms": min(vjp_df),
+                     "vjp_total_over_forward": min(vjp_df) / min(fwd_df),
+                     "adjoint": "double-float geodesic and tangent, FP32 dual sample",
+                     "cell_max_err_over_scale": cell_err_df},
         "grad_values": int(3 * d.geom.n1 * d.geom.n2 + 4),
         "fd": {"scalars": scal, "cells": cells, "cell_max_err_over_scale": cell_err,
                "thetae_field_sum": th_sum, "thetae_sum_identity": th_want,

@@ -29,7 +29,7 @@ LIB = os.path.join(LIBDIR, "libraptor_gpu.so")
 BENCH_LIB = os.path.join(LIBDIR, "libraptor_benchutil.so")
 HOST_BIN = os.path.join(LIBDIR, "raptor_gb300")
 
-CU_SOURCES = ["raptor_gpu.cu", "tuner.cu", "vjp.cu", "noalloc.cu", "ray_kernel_df.cu"]
+CU_SOURCES = ["raptor_gpu.cu", "tuner.cu", "vjp.cu", "noalloc.cu", "ray_kernel_df.cu", "vjp_df.cu"]
 HOST_SOURCES = ["raptor_main.c", "harm_io.c", "model_io.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -121,6 +121,10 @@ __device__ __forceinline__ DF fma(DF a, DF b, double c) { return a * b + c; }
 // ----------------------------------------------------------- comparisons
 __device__ __forceinline__ bool operator<(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool operator>(DF a, DF b) { return b < a; }
+__device__ __forceinline__ bool operator<=(DF a, DF b) { return !(b < a); }
+__device__ __forceinline__ bool operator>=(DF a, DF b) { return !(a < b); }
+__device__ __forceinline__ bool operator==(DF a, DF b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(DF a, DF b) { return !(a == b); }
 __device__ __forceinline__ bool operator==(DF a, double c) {
     const DF k = df_const(c);
     return a.hi == k.hi && a.lo == k.lo;

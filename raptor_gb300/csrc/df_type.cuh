@@ -20,6 +20,17 @@ __host__ __device__ __forceinline__ DF df_const(double c) {
     return DF{h, (float)(c - (double)h)};
 }
 
+// A plain double constant as scalar type T (dual.cuh): a cast, or the DF
+// split for DF.
+template <class T>
+__host__ __device__ inline T scalar_cast(double x) {
+    return (T)x;
+}
+template <>
+__host__ __device__ inline DF scalar_cast<DF>(double x) {
+    return df_const(x);
+}
+
 // Geo (kerr_mks.cuh) with DF fields
 struct GeoDF {
     DF a, a2, hslope, R0;

@@ -4,8 +4,9 @@
 // dI/d delta_k = -(I - I_<k) with the forward image's I, forward-mode
 // tangents for the four scalars, per-cell atomic scatter), in GB300's fast
 // arithmetic:
-//  * the geodesic and its inclination tangent as Dual<1, DF> through the
-//    same templated code as every other form (step size, rolled RK4, point
+//  * the geodesic as DF with its inclination tangent in FP32 (Dual<1, DF,
+//    float>; the tangent needs ~1e-5, not the path's 1e-14) through the same
+//    templated code as every other form (step size, rolled RK4, point
 //    transcendentals, Christoffels), so the path is ray_kernel_df's;
 //  * the sample as Dual<6, float>, the FP32 transfer of the mixed forms
 //    (rt_sample_fp32_core: emissivity without e2_c, absorptivity through
@@ -21,13 +22,13 @@
 namespace raptor {
 namespace {
 
-using DD1 = Dual<1, DF>;
+using DD1 = Dual<1, DF, float>;  // DF value, FP32 inclination tangent
 using F1 = Dual<1, float>;
 using F6 = Dual<6, float>;
 
 __device__ __forceinline__ F1 to_f1(const DD1& x) {
     F1 r(x.v.hi);
-    r.d[0] = x.d[0].hi;
+    r.d[0] = x.d[0];
     return r;
 }
 __device__ __forceinline__ F6 liftf(const F1& a) {
@@ -97,10 +98,10 @@ __device__ bool sample_common_f(const DevImage& im, const DD1 y[8], const MksPoi
     F6 d1(0.0f), d2(0.0f);
     if (i < 0) i = 0;
     else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F6(1.0f); }
-    else { d1 = F6(add_f(t1, (float)-i).hi); d1.d[kDirIncl] = y[1].d[0].hi * im.idx1_df.hi; }
+    else { d1 = F6(add_f(t1, (float)-i).hi); d1.d[kDirIncl] = y[1].d[0] * im.idx1_df.hi; }
     if (j < 0) j = 0;
     else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F6(1.0f); }
-    else { d2 = F6(add_f(t2, (float)-j).hi); d2.d[kDirIncl] = y[2].d[0].hi * im.idx2_df.hi; }
+    else { d2 = F6(add_f(t2, (float)-j).hi); d2.d[kDirIncl] = y[2].d[0] * im.idx2_df.hi; }
     out.base = i * im.n2 + j;
     out.d1 = d1.v;
     out.d2 = d2.v;
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         s.y[i] = DD1(df_const(y0[i].v));
-                        s.y[i].d[0] = df_const(y0[i].d[0]);
+                        s.y[i].d[0] = (float)y0[i].d[0];
                     }
                     s.bsign = (beta < 0.0) ? -1 : ((beta > 0.0) ? 1 : 0);
                     mks_point(s.y[1], s.y[2], im.geo_df, s.p);

@@ -228,6 +228,12 @@ def run_batch_config3(dev):
     g_eng.render(descs, engine.PREC_FP64)
     wall_batch = (time.perf_counter() - t0) * 1e3
     st = g_eng.stats()
+    # the same batch in the mixed-DF form (its own tuned shape and graph)
+    g_eng.render(descs, engine.PREC_MIXED_DF)
+    t0 = time.perf_counter()
+    g_eng.render(descs, engine.PREC_MIXED_DF)
+    wall_df = (time.perf_counter() - t0) * 1e3
+    st_df = g_eng.stats()
     p_eng = engine.Engine(device=dev)
     for d in dumps:
         p_eng.upload_grid(d.geom, d.prims)
@@ -243,7 +249,11 @@ def run_batch_config3(dev):
             "launch": [st["block_size"], st["blocks_per_sm"], st["refill_interval"]],
             "batched_device_ms": st["device_ms"], "batched_wall_ms": wall_batch,
             "sequential_device_ms": seq_dev, "sequential_wall_ms": wall_seq,
-            "speedup_wall": wall_seq / wall_batch, "rays_per_s": st["rays"] / (st["device_ms"] * 1e-3)}
+            "speedup_wall": wall_seq / wall_batch, "rays_per_s": st["rays"] / (st["device_ms"] * 1e-3),
+            "mixed_df": {"batched_device_ms": st_df["device_ms"], "batched_wall_ms": wall_df,
+                         "graph_replayed": st_df["graph_replayed"],
+                         "launch": [st_df["block_size"], st_df["blocks_per_sm"], st_df["refill_interval"]],
+                         "rays_per_s": st_df["rays"] / (st_df["device_ms"] * 1e-3)}}
 
 
 def _loss_delta(op, om, target):
@@ -545,12 +555,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", choices=("1024", "profile", "differentiable"), default="1024",
+    ap.add_argument("--workload", choices=("1024", "profile", "differentiable", "adjoint"), default="1024",
                     help="profile: a 256x256 image on a 256x256 torus, render timings only (for ncu captures); "
-                         "differentiable: the 2048x2048 5-frequency forward + VJP with finite-difference checks")
+                         "differentiable: the 2048x2048 5-frequency forward + VJP with finite-difference checks; "
+                         "adjoint: the 256x256 adjoint configuration alone (FP64 and mixed-DF VJP)")
     args = ap.parse_args()
     if args.workload == "differentiable":
         print(json.dumps(run_differentiable(dist_env()[2])), flush=True)
+        return
+    if args.workload == "adjoint":
+        print(json.dumps(run_vjp_config4(reps=args.steps)), flush=True)
         return
     if args.workload == "profile":
         global W, H, GRID_N

@@ -204,175 +204,145 @@ CamT<D1> camera_tangent(const DevImage& im, double inclination, double a, double
     return c;
 }
 
-template <int NF>
-struct AdjState64 {
-    D1 y[8];
-    MksPointT<D1> p;
-    double beta, thdot_prev;
-    int steps, turns, stop, pix;
-    // per frequency: tau, the forward I, the part of I accumulated so far,
-    // dL/dI and d tau / d(scalars); dIw = sum over frequencies of dL/dI dI/d(scalars)
-    double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dIw[4];
-};
-
-// Lanes take a new ray from the queue every refill_interval steps (as the
-// forward kernel does), so a warp is not held by its longest ray.
+// One lane runs its ray to the end before taking the next: with the FP64
+// duals' register footprint, keeping a ray's state across lane refills (as
+// the mixed-DF adjoint does) spilled more and ran slower (5-frequency
+// 2048x2048: 14.5 s against 11.7 s).
 template <int NF>
 __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-               double* __restrict__ g_th, int refill_interval) {
+               double* __restrict__ g_th) {
     const DevImage& im = *imp;
     const int lane = threadIdx.x & 31;
     const long long nrays = (long long)im.width * im.height;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
-    AdjState64<NF> s;
-    bool active = false, live = true;
+    unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0;
+    bool live = true;
     while (true) {
-        const unsigned need = __ballot_sync(kFull, !active && live);
-        if (need) {
-            const int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
-            base = __shfl_sync(kFull, base, leader);
-            if (!active && live) {
-                const long long rid = (long long)(base + __popc(need & ((1u << lane) - 1u)));
-                if (rid < nrays) {
-                    s.pix = (int)rid;
-                    init_photon(im, cam, s.pix % im.width, s.pix / im.width, s.y, s.beta);
-                    mks_point(s.y[1], s.y[2], im.geo, s.p);
-                    const PixelScale ps = pixel_scale(im, s.pix % im.width);
+        const unsigned want = __ballot_sync(kFull, live);
+        if (!want) break;
+        const int leader = __ffs(want) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(want));
+        base = __shfl_sync(kFull, base, leader);
+        long long rid = -1;
+        if (live) {
+            rid = (long long)(base + __popc(want & ((1u << lane) - 1u)));
+            if (rid >= nrays) {
+                live = false;
+                rid = -1;
+            }
+        }
+        if (rid < 0) continue;
+
+        const int pix = (int)rid;
+        D1 y[8];
+        double beta;
+        init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
+        MksPointT<D1> p;
+        mks_point(y[1], y[2], im.geo, p);
+        const PixelScale ps = pixel_scale(im, pix % im.width);
+        // per frequency: tau, the forward I, the part of I accumulated so far,
+        // dL/dI and d tau / d(scalars); dIw = sum over frequencies of dL/dI dI/d(scalars)
+        double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dIw[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            tau[f] = 0.0;
+            Ipart[f] = 0.0;
+            Itot[f] = 0.0;
+            w[f] = 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dtg[f][q] = 0.0;
+            if (f < im.nfreq) {
+                const long long o = (long long)pix * im.nfreq + f;
+                const double dOdI = scale_output(im, ps, 1.0, f);
+                Itot[f] = fwd[o] / dOdI;
+                w[f] = dLdO[o] * dOdI;
+            }
+        }
+        int steps = 0, turns = 0, stop = 0;
+        double thdot_prev = 0.0;
+        while (true) {
+            const double r = p.rp.v;
+            if (!(r < kCutoffOuter && r > im.cutoff_inner && (double)steps < kMaxSteps && !stop)) break;
+            if (thdot_prev * y[6].v < 0.0 && steps > 2) turns += 1;
+            thdot_prev = y[6].v;
+            if ((beta < 0.0 && turns > kMaxOrder) || (beta > 0.0 && turns > kMaxOrder + 1)) stop = 1;
+            const D1 dl = step_size(im, y);
+            if (im.integrator == 2) rk2_step(im.geo, y, p, dl);
+            else rk4_step(im.geo, y, p, dl);
+            steps += 1;
+            if (y[1].v > im.stopx1 && y[5].v < 0.0) break;
+            if (y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2) {
+                ++n_calls;
+                SampleCommon sc;
+                CellCoef cc;
+                const D1 k1[4] = {y[4], y[5], y[6], y[7]};
+                if (sample_common(im, y[1], y[2], k1, p, fabs(dl), cc, sc)) {
+                    ++n_samples;
+                    double Gr = 0.0, Gt = 0.0;
 #pragma unroll
                     for (int f = 0; f < NF; ++f) {
-                        s.tau[f] = 0.0;
-                        s.Ipart[f] = 0.0;
-                        s.Itot[f] = 0.0;
-                        s.w[f] = 0.0;
+                        if (f >= im.nfreq) break;
+                        D6 S, dt;
+                        const int kind = sample_freq(im, sc, f, S, dt);
+                        if (kind == 1) {
+                            ++n_emit;
+                            tau[f] += dt.v;
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) s.dtg[f][q] = 0.0;
-                        if (f < im.nfreq) {
-                            const long long o = (long long)s.pix * im.nfreq + f;
-                            const double dOdI = scale_output(im, ps, 1.0, f);
-                            s.Itot[f] = fwd[o] / dOdI;
-                            s.w[f] = dLdO[o] * dOdI;
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) s.dIw[q] = 0.0;
-                    s.steps = 0;
-                    s.turns = 0;
-                    s.stop = 0;
-                    s.thdot_prev = 0.0;
-                    active = true;
-                } else {
-                    live = false;
-                }
-            }
-        }
-        if (!__any_sync(kFull, active)) break;
-        if (!active) continue;
-        for (int it = 0; it < refill_interval; ++it) {
-            const double r = s.p.rp.v;
-            bool done = !(r < kCutoffOuter && r > im.cutoff_inner && (double)s.steps < kMaxSteps && !s.stop);
-            if (!done) {
-                if (s.thdot_prev * s.y[6].v < 0.0 && s.steps > 2) s.turns += 1;
-                s.thdot_prev = s.y[6].v;
-                if ((s.beta < 0.0 && s.turns > kMaxOrder) || (s.beta > 0.0 && s.turns > kMaxOrder + 1)) s.stop = 1;
-                const D1 dl = step_size(im, s.y);
-                if (im.integrator == 2) rk2_step(im.geo, s.y, s.p, dl);
-                else rk4_step(im.geo, s.y, s.p, dl);
-                s.steps += 1;
-                if (s.y[1].v > im.stopx1 && s.y[5].v < 0.0) {
-                    done = true;
-                } else if (s.y[1].v < im.stopx1 && s.y[1].v > im.startx1 && s.y[2].v > im.startx2 &&
-                           s.y[2].v < im.stopx2) {
-                    ++n_calls;
-                    SampleCommon sc;
-                    CellCoef cc;
-                    const D1 k1[4] = {s.y[4], s.y[5], s.y[6], s.y[7]};
-                    if (sample_common(im, s.y[1], s.y[2], k1, s.p, fabs(dl), cc, sc)) {
-                        ++n_samples;
-                        double Gr = 0.0, Gt = 0.0;
-#pragma unroll
-                        for (int f = 0; f < NF; ++f) {
-                            if (f >= im.nfreq) break;
-                            D6 S, dt;
-                            const int kind = sample_freq(im, sc, f, S, dt);
-                            if (kind == 1) {
-                                ++n_emit;
-                                s.tau[f] += dt.v;
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) s.dtg[f][q] += dt.d[gdir(q)];
-                                const double e = exp(-s.tau[f]);
-                                const bool gate = s.tau[f] < 6.907755278982137 && !(s.tau[f] < 0.0);
-                                const double suffix = s.Itot[f] - s.Ipart[f];
-                                const double eS = gate ? e : 0.0;
-                                if (suffix != 0.0 || gate) {
-                                    Gr += s.w[f] * (eS * S.d[kDirRho] - suffix * dt.d[kDirRho]);
-                                    Gt += s.w[f] * (eS * S.d[kDirU] - suffix * dt.d[kDirU]);
-                                }
-                                if (gate) {
-                                    ++n_gate;
-                                    const double we = s.w[f] * e;
-#pragma unroll
-                                    for (int q = 0; q < 4; ++q) s.dIw[q] += we * (S.d[gdir(q)] - S.v * s.dtg[f][q]);
-                                    s.Ipart[f] += S.v * e;
-                                }
-                            } else if (kind == 2) {
-                                s.tau[f] = __longlong_as_double(0x7ff8000000000000ll);
+                            for (int q = 0; q < 4; ++q) dtg[f][q] += dt.d[gdir(q)];
+                            const double e = exp(-tau[f]);
+                            const bool gate = tau[f] < 6.907755278982137 && !(tau[f] < 0.0);
+                            const double suffix = Itot[f] - Ipart[f];
+                            const double eS = gate ? e : 0.0;
+                            if (suffix != 0.0 || gate) {
+                                Gr += w[f] * (eS * S.d[kDirRho] - suffix * dt.d[kDirRho]);
+                                Gt += w[f] * (eS * S.d[kDirU] - suffix * dt.d[kDirU]);
                             }
+                            if (gate) {
+                                ++n_gate;
+                                const double we = w[f] * e;
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) dIw[q] += we * (S.d[gdir(q)] - S.v * dtg[f][q]);
+                                Ipart[f] += S.v * e;
+                            }
+                        } else if (kind == 2) {
+                            tau[f] = __longlong_as_double(0x7ff8000000000000ll);
                         }
-                        const double Gu = Gt * sc.dlnth_du;
-                        if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
-                            const double w0 = (1.0 - cc.d1) * (1.0 - cc.d2), w1 = (1.0 - cc.d1) * cc.d2;
-                            const double w2 = cc.d1 * (1.0 - cc.d2), w3 = cc.d1 * cc.d2;
-                            const long long c = cc.base, cn = cc.base + im.n2;
-                            atomicAdd(&g_rho[c], Gr * w0);
-                            atomicAdd(&g_rho[c + 1], Gr * w1);
-                            atomicAdd(&g_rho[cn], Gr * w2);
-                            atomicAdd(&g_rho[cn + 1], Gr * w3);
-                            atomicAdd(&g_u[c], Gu * w0);
-                            atomicAdd(&g_u[c + 1], Gu * w1);
-                            atomicAdd(&g_u[cn], Gu * w2);
-                            atomicAdd(&g_u[cn + 1], Gu * w3);
-                            atomicAdd(&g_th[c], Gt * w0);
-                            atomicAdd(&g_th[c + 1], Gt * w1);
-                            atomicAdd(&g_th[cn], Gt * w2);
-                            atomicAdd(&g_th[cn + 1], Gt * w3);
-                        }
+                    }
+                    const double Gu = Gt * sc.dlnth_du;
+                    if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
+                        const double w0 = (1.0 - cc.d1) * (1.0 - cc.d2), w1 = (1.0 - cc.d1) * cc.d2;
+                        const double w2 = cc.d1 * (1.0 - cc.d2), w3 = cc.d1 * cc.d2;
+                        const long long c = cc.base, cn = cc.base + im.n2;
+                        atomicAdd(&g_rho[c], Gr * w0);
+                        atomicAdd(&g_rho[c + 1], Gr * w1);
+                        atomicAdd(&g_rho[cn], Gr * w2);
+                        atomicAdd(&g_rho[cn + 1], Gr * w3);
+                        atomicAdd(&g_u[c], Gu * w0);
+                        atomicAdd(&g_u[c + 1], Gu * w1);
+                        atomicAdd(&g_u[cn], Gu * w2);
+                        atomicAdd(&g_u[cn + 1], Gu * w3);
+                        atomicAdd(&g_th[c], Gt * w0);
+                        atomicAdd(&g_th[c + 1], Gt * w1);
+                        atomicAdd(&g_th[cn], Gt * w2);
+                        atomicAdd(&g_th[cn + 1], Gt * w3);
                     }
                 }
             }
-            if (done) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (isfinite(s.dIw[q])) acc[q] += s.dIw[q];
-                n_steps += (unsigned long long)s.steps;
-                n_rays += 1;
-                active = false;
-                break;
-            }
         }
-    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        n_steps += __shfl_xor_sync(kFull, n_steps, o);
-        n_rays += __shfl_xor_sync(kFull, n_rays, o);
-        n_calls += __shfl_xor_sync(kFull, n_calls, o);
-        n_samples += __shfl_xor_sync(kFull, n_samples, o);
-        n_emit += __shfl_xor_sync(kFull, n_emit, o);
-        n_gate += __shfl_xor_sync(kFull, n_gate, o);
+        for (int q = 0; q < 4; ++q)
+            if (isfinite(dIw[q])) acc[q] += dIw[q];
+        atomicAdd(&counters[kCtrSteps], (unsigned long long)steps);
+        atomicAdd(&counters[kCtrRays], 1ull);
     }
-    if (lane == 0) {
-        atomicAdd(&counters[kCtrSteps], n_steps);
-        atomicAdd(&counters[kCtrRays], n_rays);
-        atomicAdd(&counters[kCtrRtCalls], n_calls);
-        atomicAdd(&counters[kCtrRtSamples], n_samples);
-        atomicAdd(&counters[kCtrVjpEmit], n_emit);
-        atomicAdd(&counters[kCtrVjpGate], n_gate);
-    }
+    atomicAdd(&counters[kCtrRtCalls], n_calls);
+    atomicAdd(&counters[kCtrRtSamples], n_samples);
+    atomicAdd(&counters[kCtrVjpEmit], n_emit);
+    atomicAdd(&counters[kCtrVjpGate], n_gate);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         double v = acc[q];
@@ -385,8 +355,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 template <int NF>
 void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                 const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                int refill) {
-    vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
+                int) {
+    vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt);
 }
 
 VjpLaunchFn pick_vjp_fp64(int nf, const void** fn) {

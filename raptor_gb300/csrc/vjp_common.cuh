@@ -16,7 +16,7 @@ constexpr int kDirIncl = 0, kDirRho = 1, kDirU = 2, kDirLnM = 3, kDirRh = 4, kDi
 __host__ __device__ __forceinline__ int gdir(int q) { return q == 0 ? kDirIncl : q + 2; }
 
 constexpr int kVjpBlock = 128;
-constexpr int kVjpRefill = 8;  // geodesic steps between lane refills of the adjoint kernels
+constexpr int kVjpRefill = 8;  // geodesic steps between lane refills of the mixed-DF adjoint
 
 // Launch of the adjoint pass: grid blocks of kVjpBlock threads on stream st
 // for image im (device pointer), camera constants with their inclination

@@ -111,6 +111,8 @@ typedef struct raptor_gpu_stats {
     int graph_replayed;
     long long device_bytes;      /* device memory the context holds now */
     long long peak_device_bytes; /* the most it has held */
+    long long vjp_terms;         /* raptor_gpu_vjp: (sample, frequency) terms that emitted */
+    long long vjp_gated_terms;   /* raptor_gpu_vjp: of those, inside the tau < ln 1000 gate */
 } raptor_gpu_stats;
 
 /* Gradients of a scalar loss L(I) of the output image, given dL/dI. */
@@ -164,7 +166,9 @@ int raptor_gpu_render_range(raptor_gpu_ctx *ctx, const raptor_image_desc *imgs, 
 long long raptor_gpu_output_size(const raptor_image_desc *imgs, int n_imgs);
 long long raptor_gpu_spectrum_size(const raptor_image_desc *imgs, int n_imgs);
 
-/* Statistics of the last render or VJP on this context. */
+/* Statistics of the last render or VJP on this context (for a VJP: the
+ * adjoint pass's counters; kernel_ms is the adjoint pass, device_ms forward
+ * plus adjoint). */
 int raptor_gpu_get_stats(const raptor_gpu_ctx *ctx, raptor_gpu_stats *out);
 
 /* Per-step record of one ray, the engine's form of the reference's GEOD

@@ -512,6 +512,8 @@ int collect_stats(raptor_gpu_ctx* ctx, bool timed) {
     s.n_stepcap = (long long)c[kCtrStepCap];
     s.n_nonfinite = (long long)c[kCtrNonFinite];
     s.max_ray_steps = (long long)c[kCtrMaxSteps];
+    s.vjp_terms = 0;  // render statistics: no adjoint terms
+    s.vjp_gated_terms = 0;
     double kk;
     memcpy(&kk, &c[kCtrKkMax], sizeof kk);
     s.kk_max = kk;

@@ -463,8 +463,8 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     s.steps = (long long)ctr[kCtrSteps];
     s.rt_calls = (long long)ctr[kCtrRtCalls];
     s.rt_samples = (long long)ctr[kCtrRtSamples];
-    s.n_stepcap = (long long)ctr[kCtrVjpEmit];    // frequencies that emitted
-    s.n_nonfinite = (long long)ctr[kCtrVjpGate];  // terms inside the tau gate
+    s.vjp_terms = (long long)ctr[kCtrVjpEmit];
+    s.vjp_gated_terms = (long long)ctr[kCtrVjpGate];
     (void)fwd_ctr;
     s.block_size = kVjpBlock;
     s.grid_blocks = grid;

@@ -70,7 +70,8 @@ class Stats(ctypes.Structure):
                 ("n_nonfinite", ctypes.c_longlong), ("kk_max", ctypes.c_double), ("block_size", ctypes.c_int),
                 ("blocks_per_sm", ctypes.c_int), ("refill_interval", ctypes.c_int),
                 ("grid_blocks", ctypes.c_int), ("graph_replayed", ctypes.c_int),
-                ("device_bytes", ctypes.c_longlong), ("peak_device_bytes", ctypes.c_longlong)]
+                ("device_bytes", ctypes.c_longlong), ("peak_device_bytes", ctypes.c_longlong),
+                ("vjp_terms", ctypes.c_longlong), ("vjp_gated_terms", ctypes.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

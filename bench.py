@@ -22,6 +22,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -52,7 +53,9 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+        # the samples go to RAPTOR_ARTIFACT_DIR when set, else to a scratch file
+        out_dir = os.environ.get("RAPTOR_ARTIFACT_DIR") or tempfile.mkdtemp(prefix="raptor_clocks_")
+        self.path = os.path.join(out_dir, f"clocks_rank{device}.csv")
 
     def __enter__(self):
         try:
@@ -112,7 +115,6 @@ def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, re
     sess = None
     if ref.available(GRID_N, GRID_N, opt="stock"):
         try:
-            import tempfile
             from raptor_gb300 import harm
             from tests.golden.make_golden import quiet
             tmp = tempfile.mkdtemp(prefix="rgb_", dir="/tmp")

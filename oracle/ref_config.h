@@ -6,7 +6,7 @@
  * switches that the reference only offers as #defines:
  *
  *   int_method  parameters.h:189  RK2 in the stock build; RK4 for the
- *                                  configurations this engine is judged on
+ *                                  benchmark configurations
  *   N1, N2      parameters.h:76-77 grid size of the dump being read
  *   maxsize     parameters.h:52   image buffer; 1e6 silently drops pixels
  *                                  of images larger than 1000x1000

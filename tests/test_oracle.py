@@ -97,9 +97,12 @@ def test_camera_angle_root(torus64, small):
     assert th == pytest.approx(np.arccos(np.cos(np.radians(60.0))), abs=1e-14)
 
 
-@pytest.mark.skipif(not os.path.isfile(os.path.join(os.environ.get("RAPTOR_REFERENCE_DIR", "/root/reference"),
-                                                    "integrator.c")),
-                    reason="reference sources not present on this machine")
+def _reference_sources():
+    from oracle import ref
+    return ref.sources_present()
+
+
+@pytest.mark.skipif(not _reference_sources(), reason="reference sources not present on this machine")
 def test_port_vs_reference_fresh_seed(tmp_path):
     """Port against the reference build on a torus the fixtures never saw."""
     from oracle import port, ref

@@ -82,7 +82,7 @@ int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs
 // form: RAPTOR_PREC_FP64, RAPTOR_PREC_MIXED or RAPTOR_PREC_MIXED_DF
 RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn);
 RayLaunchFn pick_ray_kernel_df(int nf, const void** fn);
-LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn);
+LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn, int form);
 LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunchFn fn, const void* fnp);
 int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, int form, long long rb, long long re,
                    const LaunchShape& ls, RayLaunchFn fn, bool timed, raptor::TraceSpec tr = {-1, nullptr, 0});

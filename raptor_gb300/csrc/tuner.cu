@@ -60,7 +60,7 @@ void save_file_cache(const std::string& key, const LaunchShape& ls) {
 }  // namespace
 
 LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunchFn fn, const void* fnp) {
-    LaunchShape base = default_shape(ctx, fnp);
+    LaunchShape base = default_shape(ctx, fnp, form);
     if (!ctx->opt.autotune) return base;
     load_file_cache(ctx);
     const std::string key = signature(ctx, b, form);

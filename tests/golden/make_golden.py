@@ -72,6 +72,20 @@ BATCH_DUMP_IMAGES = [
 ]
 
 
+# images of the R0 = 0.3 dump: name, W, H, inclination, frequency, integrator
+R0_IMAGES = [
+    ("r0_i50_rk4", 32, 28, 50.0, 230e9, "RK4"),
+    ("r0_i130_rk2", 24, 24, 130.0, 345e9, "RK2"),
+]
+
+
+def r0_dump():
+    """The 64x64 torus with its header's R0 set to 0.3."""
+    import dataclasses
+    d = synth.make_torus(n1=64, n2=64)
+    return dataclasses.replace(d, geom=dataclasses.replace(d.geom, R0=0.3))
+
+
 def prim_checksum(prims):
     return np.array([np.sum(np.abs(p), dtype=np.float64) for p in prims])
 
@@ -200,11 +214,29 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--parts", default="small,256,logcam,batchdumps",
-                    help="comma list of fixture groups to write: small, 256, logcam, batchdumps")
+    ap.add_argument("--parts", default="small,256,logcam,batchdumps,r0",
+                    help="comma list of fixture groups to write: small, 256, logcam, batchdumps, r0")
     a = ap.parse_args()
     parts = set(a.parts.split(","))
     tmp = tempfile.mkdtemp(prefix="rgg_", dir="/tmp")
+
+    if "r0" in parts:
+        # a non-zero MKS radial offset: the 64x64 torus's cells read under a
+        # header with R0 = 0.3 (r = R0 + exp(x1) in the metric and the
+        # connection, metric.c:94-137,538-638); the inputs need not be a
+        # physical solution for parity, only the same on both sides
+        d64 = r0_dump()
+        path = os.path.join(tmp, "torus64_r0.dump")
+        harm.write_dump(path, d64)
+        out = dict(prim_checksum=prim_checksum(d64.prims), R0=np.array([d64.geom.R0]))
+        for (name, w, h, incl, freq, rk) in R0_IMAGES:
+            img, spec, dt = ref_image(path, 64, w, h, incl, freq, rk, 0.05, 1e19, 3.0, 3.0)
+            out[f"{name}_img"] = img
+            out[f"{name}_spec"] = np.array([spec])
+            out[f"{name}_params"] = np.array([w, h, incl, freq, 4 if rk == "RK4" else 2, 0.05, 1e19, 3.0, 3.0])
+            print(f"{name}: {dt:.2f} s, flux {spec:.6e}", flush=True)
+        out["names"] = np.array([c[0] for c in R0_IMAGES])
+        np.savez_compressed(os.path.join(OUT, "r0_g64.npz"), **out)
 
     if "batchdumps" in parts:
         # the two dumps of the batched configuration (a = 0.5 and a = 0.9375,

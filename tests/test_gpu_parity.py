@@ -97,6 +97,23 @@ def test_batch_dumps_match_reference(eng, k, name):
         assert sm[0] == pytest.approx(g[f"{name}_spec"][0], rel=FLUX_RTOL_MIXED), prec
 
 
+@pytest.mark.parametrize("name", ["r0_i50_rk4", "r0_i130_rk2"])
+def test_nonzero_r0_matches_reference(eng, name):
+    """R0 = 0.3 in the dump header (r = R0 + exp(x1)): FP64 at the parity bar,
+    both mixed forms within the flux bar."""
+    from raptor_gb300 import engine
+    from tests.golden.make_golden import r0_dump
+    g = load_golden("r0_g64.npz")
+    d = r0_dump()
+    desc = _desc(g[f"{name}_params"], _grid(eng, d))
+    img, spec = eng.render(desc, engine.PREC_FP64)
+    assert_fp64_parity(img, g[f"{name}_img"], name)
+    assert spec[0] == pytest.approx(g[f"{name}_spec"][0], rel=1e-6)
+    for prec in (engine.PREC_MIXED, engine.PREC_MIXED_DF):
+        _, sm = eng.render(desc, prec)
+        assert sm[0] == pytest.approx(g[f"{name}_spec"][0], rel=FLUX_RTOL_MIXED), prec
+
+
 def test_fp64_matches_port_and_step_counts(eng, torus64):
     """Step and sample counters agree with the oracle's, ray by ray in sum."""
     from oracle import port

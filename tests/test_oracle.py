@@ -151,3 +151,17 @@ def test_port_matches_reference_batch_dumps(k, name):
     out, _ = sc.render([freq])
     assert_fp64_parity(out[:, 0], g[f"{name}_img"], name)
     np.testing.assert_allclose(out[:, 0].sum(), g[f"{name}_spec"][0], rtol=1e-6)
+
+
+@pytest.mark.parametrize("name", ["r0_i50_rk4", "r0_i130_rk2"])
+def test_port_matches_reference_nonzero_r0(name):
+    """A non-zero MKS radial offset (R0 = 0.3 in the dump header): r = R0 +
+    exp(x1) in the metric and connection (metric.c:94-137, 538-638)."""
+    from tests.golden.make_golden import prim_checksum, r0_dump
+    g = load_golden("r0_g64.npz")
+    d = r0_dump()
+    assert d.geom.R0 == g["R0"][0]
+    np.testing.assert_allclose(prim_checksum(d.prims), g["prim_checksum"], rtol=1e-12)
+    sc, freq = _scene(d, g[f"{name}_params"])
+    out, _ = sc.render([freq])
+    assert_fp64_parity(out[:, 0], g[f"{name}_img"], name)

@@ -222,8 +222,13 @@ def test_range_render_is_a_slice(eng, torus64):
 def test_invalid_arguments_are_rejected(eng, torus64):
     from raptor_gb300 import engine
     gid = _grid(eng, torus64)
+    for bad_grid in (-1, 16):  # outside 0..RAPTOR_MAX_GRIDS-1
+        with pytest.raises(engine.EngineError):
+            eng.render(engine.image_desc(4, 4, [230e9], grid=bad_grid))
     with pytest.raises(engine.EngineError):
-        eng.render(engine.image_desc(4, 4, [230e9], grid=gid + 5))
+        eng.render(engine.image_desc(4, 4, [230e9], grid=gid, camera=7))
+    with pytest.raises(engine.EngineError):
+        eng.render(engine.image_desc(4, 4, [230e9], grid=gid), 3)  # unknown precision
     with pytest.raises(engine.EngineError):
         eng.render(engine.image_desc(4, 4, [230e9], grid=gid, integrator=3))
     with pytest.raises(engine.EngineError):

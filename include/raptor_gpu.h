@@ -42,8 +42,7 @@ extern "C" {
 #define RAPTOR_PREC_FP64 0  /* everything FP64, the reference's arithmetic */
 #define RAPTOR_PREC_MIXED 1 /* FP64 geodesic + metric, FP32 fluid/emission/transfer */
 #define RAPTOR_PREC_MIXED_DF 2 /* geodesic + metric in double-float (pairs of FP32, 48-bit
-                                  significand) on the FP32 pipes, transfer as RAPTOR_PREC_MIXED;
-                                  not for trace_ray */
+                                  significand) on the FP32 pipes, transfer as RAPTOR_PREC_MIXED */
 
 /* integrators (parameters.h:186-189) */
 #define RAPTOR_RK4 4

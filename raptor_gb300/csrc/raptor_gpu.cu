@@ -643,7 +643,7 @@ extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc
     ctx->err[0] = 0;
     if (!img || !records || !n_records || max_records <= 0)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "trace_ray: null output or non-positive max_records");
-    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED)
+    if (precision != RAPTOR_PREC_FP64 && precision != RAPTOR_PREC_MIXED && precision != RAPTOR_PREC_MIXED_DF)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "precision %d unknown", precision);
     if (pixel < 0 || (long long)pixel >= (long long)img->width * img->height)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "pixel %d outside the %dx%d image", pixel, img->width, img->height);

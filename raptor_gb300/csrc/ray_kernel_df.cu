@@ -127,6 +127,24 @@ __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], 
 // 4 blocks of 128 (16 warps) per SM: the DF arithmetic is FP32-latency bound,
 // and 16 warps at 128 registers (a few hundred bytes of spills) ran 1.4x
 // faster than 8 warps at 196 registers without spills (1024x1024 image).
+// Per-step record of the traced ray (the layout of trace_record in
+// ray_kernel.cuh), the DF state written as doubles.
+template <int NF>
+__device__ __forceinline__ void trace_record_df(const TraceSpec& tr, const RayStateDF<NF>& s, double dl, int event) {
+    if (s.steps >= tr.cap) return;
+    double* r = tr.out + (long long)s.steps * kTraceWidth;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r[i] = df_to_double(s.y[i]);
+    r[8] = dl;
+    r[9] = (double)s.tf[0] + (double)s.tc[0];
+    r[10] = ((double)s.If[0] + (double)s.Ic[0]) * kE2C;
+    r[11] = s.steps;
+    r[12] = s.turns;
+    r[13] = event;
+    r[14] = s.stop;
+    r[15] = 0.0;
+}
+
 #ifndef RAPTOR_RAY_DF_MIN_BLOCKS
 #define RAPTOR_RAY_DF_MIN_BLOCKS 4
 #endif
@@ -134,7 +152,8 @@ __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], 
 template <int NF>
 __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
     ray_kernel_df(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
-                  unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval) {
+                  unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval,
+                  TraceSpec tr) {
     const int lane = threadIdx.x & 31;
     RayStateDF<NF> s;
     bool active = false, live = true;
@@ -174,6 +193,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
                         s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
                     }
                     active = true;
+                    if (tr.out && rid == tr.ray) trace_record_df<NF>(tr, s, 0.0, 0);
                 } else {
                     live = false;
                 }
@@ -196,14 +216,18 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
                     if (im->integrator == 2) rk2_step(im->geo_df, s.y, s.p, dl);
                     else rk4_step_rolled(im->geo_df, s.y, s.p, dl);
                     s.steps += 1;
+                    int event = 0;
                     if (s.y[1] > im->stopx1_df && s.y[5].hi < 0.0f) {
                         done = true;  // escaped outward (integrator.c:271-272)
+                        event = 3;
                     } else if (s.y[1] < im->stopx1_df && s.y[1] > im->startx1_df && s.y[2] > im->startx2_df &&
                                s.y[2] < im->stopx2_df) {
                         ++n_rt_calls;
                         const bool sampled = rt_sample_df<NF>(*im, s.y, s.p, -dl.hi, s.tf, s.tc, s.If, s.Ic);
                         n_rt_samples += sampled ? 1 : 0;
+                        event = sampled ? 2 : 1;
                     }
+                    if (tr.out && s.rid == tr.ray) trace_record_df<NF>(tr, s, df_to_double(dl), event);
                 }
                 if (done) {
                     double* o = out + im->out_offset + (long long)s.pix * im->nfreq;
@@ -257,8 +281,8 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
 
 template <int NF>
 void launch_ray_df(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b, long long e,
-                   unsigned long long* ctr, double* out, TraceSpec) {
-    ray_kernel_df<NF><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill);
+                   unsigned long long* ctr, double* out, TraceSpec tr) {
+    ray_kernel_df<NF><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
 }
 
 }  // namespace

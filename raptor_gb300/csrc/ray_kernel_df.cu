@@ -36,29 +36,9 @@ __device__ __forceinline__ DF step_size_df(const DevImage& im, const DF y[8]) {
     return -fmax(1.0 / (i1 + i2 + i3), df_const(1e-12));
 }
 
-// mks_point (kerr_mks.cuh) for DF states, with the two sincospi evaluations
-// (of 2 x2, then of theta / pi) through one copy of the code.
+// mks_point for DF states: the rolled form (kerr_mks.cuh)
 __device__ __forceinline__ void mks_point(DF x1, DF x2, const GeoDF& g, MksPointT<DF>& p) {
-    p.rp = fast_exp(x1);
-    p.r = g.R0 + p.rp;
-    DF arg = 2.0 * x2, sv, cv;
-#pragma unroll 1
-    for (int k = 0;; ++k) {
-        fast_sincospi(arg, &sv, &cv);
-        if (k == 1) break;
-        p.s2x = sv;
-        p.c2x = cv;
-        // theta = pi x2 + (1-h)/2 sin(2 pi x2) (metric.c:98), as theta / pi
-        arg = fma(g.th_coef, sv, x2);
-    }
-    p.s = sv;
-    p.c = cv;
-    const DF Sg = fma(p.r, p.r, g.a2 * p.c * p.c);
-    const DF thp = CUDART_PI * fma(g.one_m_h, p.c2x, 1.0);
-    p.iS = 1.0 / Sg;
-    p.irp = 1.0 / p.rp;
-    p.ithp = 1.0 / thp;
-    p.isn = 1.0 / p.s;
+    mks_point_rolled(x1, x2, g, p);
 }
 
 // The sample's metric (metric.c:94-137, 207-231 as mks_metric) in FP32 from

@@ -26,6 +26,11 @@ using DD1 = Dual<1, DF, float>;  // DF value, FP32 inclination tangent
 using F1 = Dual<1, float>;
 using F6 = Dual<6, float>;
 
+// mks_point for the dual DF state: the rolled form (kerr_mks.cuh)
+__device__ __forceinline__ void mks_point(DD1 x1, DD1 x2, const GeoDF& g, MksPointT<DD1>& p) {
+    mks_point_rolled(x1, x2, g, p);
+}
+
 __device__ __forceinline__ F1 to_f1(const DD1& x) {
     F1 r(x.v.hi);
     r.d[0] = x.d[0];
@@ -184,7 +189,14 @@ struct AdjState {
     float tau[NF], Ipart[NF], Itot[NF], w[NF];
     float dtg[NF][4];
     float dIw[4];
+    int wexp;  // w[f] holds dL/dI_f * 2^-wexp; the ray's gradient terms are scaled back by 2^wexp
 };
+
+// 2^e as a double for e in [-1022, 1023] (built from the exponent field).
+__device__ __forceinline__ double pow2_double(int e) {
+    e = min(max(e, -1022), 1023);
+    return __longlong_as_double((long long)(e + 1023) << 52);
+}
 
 #ifndef RAPTOR_VJP_DF_MIN_BLOCKS
 #define RAPTOR_VJP_DF_MIN_BLOCKS 2
@@ -227,6 +239,19 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                     s.bsign = (beta < 0.0) ? -1 : ((beta > 0.0) ? 1 : 0);
                     mks_point(s.y[1], s.y[2], im.geo_df, s.p);
                     const PixelScale ps = pixel_scale(im, px);
+                    // The loss weights dL/dO * dO/dI can sit far outside FP32's range (the
+                    // log-polar camera's dO/dI carries 1/D^2); scale them by a power of two
+                    // so the largest is in [0.5, 1) and undo the scale in FP64.
+                    double wmax = 0.0;
+                    for (int f = 0; f < im.nfreq && f < NF; ++f) {
+                        const long long o = (long long)s.pix * im.nfreq + f;
+                        const double wf = fabs(dLdO[o] * scale_output(im, ps, 1.0, f) * kE2C);
+                        if (isfinite(wf)) wmax = fmax(wmax, wf);
+                    }
+                    s.wexp = 0;
+                    if (wmax > 0.0) frexp(wmax, &s.wexp);
+                    s.wexp = min(max(s.wexp, -1022), 1022);  // 2^wexp and 2^-wexp both normal
+                    const double wscale = pow2_double(-s.wexp);
 #pragma unroll
                     for (int f = 0; f < NF; ++f) {
                         s.tau[f] = 0.0f;
@@ -240,7 +265,7 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                             const long long o = (long long)s.pix * im.nfreq + f;
                             const double dOdI = scale_output(im, ps, 1.0, f) * kE2C;
                             s.Itot[f] = (float)(fwd[o] / dOdI);
-                            s.w[f] = (float)(dLdO[o] * dOdI);
+                            s.w[f] = (float)(dLdO[o] * dOdI * wscale);
                         }
                     }
 #pragma unroll
@@ -309,18 +334,20 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                             const float w0 = (1.0f - sc.d1) * (1.0f - sc.d2), w1 = (1.0f - sc.d1) * sc.d2;
                             const float w2 = sc.d1 * (1.0f - sc.d2), w3 = sc.d1 * sc.d2;
                             const long long c = sc.base, cn = sc.base + im.n2;
-                            atomicAdd(&g_rho[c], (double)(Gr * w0));
-                            atomicAdd(&g_rho[c + 1], (double)(Gr * w1));
-                            atomicAdd(&g_rho[cn], (double)(Gr * w2));
-                            atomicAdd(&g_rho[cn + 1], (double)(Gr * w3));
-                            atomicAdd(&g_u[c], (double)(Gu * w0));
-                            atomicAdd(&g_u[c + 1], (double)(Gu * w1));
-                            atomicAdd(&g_u[cn], (double)(Gu * w2));
-                            atomicAdd(&g_u[cn + 1], (double)(Gu * w3));
-                            atomicAdd(&g_th[c], (double)(Gt * w0));
-                            atomicAdd(&g_th[c + 1], (double)(Gt * w1));
-                            atomicAdd(&g_th[cn], (double)(Gt * w2));
-                            atomicAdd(&g_th[cn + 1], (double)(Gt * w3));
+                            const double un = pow2_double(s.wexp);
+                            const double gr = (double)Gr * un, gu = (double)Gu * un, gt = (double)Gt * un;
+                            atomicAdd(&g_rho[c], gr * w0);
+                            atomicAdd(&g_rho[c + 1], gr * w1);
+                            atomicAdd(&g_rho[cn], gr * w2);
+                            atomicAdd(&g_rho[cn + 1], gr * w3);
+                            atomicAdd(&g_u[c], gu * w0);
+                            atomicAdd(&g_u[c + 1], gu * w1);
+                            atomicAdd(&g_u[cn], gu * w2);
+                            atomicAdd(&g_u[cn + 1], gu * w3);
+                            atomicAdd(&g_th[c], gt * w0);
+                            atomicAdd(&g_th[c + 1], gt * w1);
+                            atomicAdd(&g_th[cn], gt * w2);
+                            atomicAdd(&g_th[cn + 1], gt * w3);
                         }
                     }
                 }
@@ -328,7 +355,7 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
             if (done) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if (isfinite(s.dIw[q])) acc[q] += (double)s.dIw[q];
+                    if (isfinite(s.dIw[q])) acc[q] += (double)s.dIw[q] * pow2_double(s.wexp);
                 n_steps += (unsigned long long)s.steps;
                 n_rays += 1;
                 active = false;

@@ -80,7 +80,8 @@ int ensure_buffer(raptor_gpu_ctx* ctx, void** ptr, size_t* cap, size_t bytes);
 int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, raptor::DevImage& im);
 int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs, Batch& b);
 // form: RAPTOR_PREC_FP64, RAPTOR_PREC_MIXED or RAPTOR_PREC_MIXED_DF
-RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn);
+// pool: the FP64 form's sample-pool kernel (ray_kernel_pool) instead of ray_kernel
+RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn, bool pool = true);
 RayLaunchFn pick_ray_kernel_df(int nf, const void** fn);
 LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn, int form);
 LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunchFn fn, const void* fnp);

@@ -397,13 +397,23 @@ static void launch_ray(const LaunchShape& ls, cudaStream_t st, const DevImage* i
     ray_kernel<NF, MIXED><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
 }
 
-RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn) {
+// The FP64 form's pooled kernel; a trace (per-step records of tau and I)
+// needs the in-place sample and takes ray_kernel.
+template <int NF>
+static void launch_ray_pool(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b,
+                            long long e, unsigned long long* ctr, double* out, TraceSpec tr) {
+    if (tr.out) ray_kernel<NF, false><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
+    else ray_kernel_pool<NF><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill);
+}
+
+RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn, bool pool) {
     if (form == RAPTOR_PREC_MIXED_DF) return pick_ray_kernel_df(nf, fn);
     const bool mixed = form == RAPTOR_PREC_MIXED;
     // one instantiation per frequency-count bucket so tau/I stay in registers
 #define PICK(NF)                                                        \
     if (nf <= NF) {                                                     \
         if (mixed) { *fn = (const void*)ray_kernel<NF, true>; return launch_ray<NF, true>; } \
+        if (pool) { *fn = (const void*)ray_kernel_pool<NF>; return launch_ray_pool<NF>; } \
         *fn = (const void*)ray_kernel<NF, false>;                      \
         return launch_ray<NF, false>;                                   \
     }
@@ -589,7 +599,7 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     if (rb > b.total_rays) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "ray range starts past the batch");
     const int form = precision;
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, form, &fnp);
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, form, &fnp, !ctx->opt.no_sample_pool);
     LaunchShape ls = choose_shape(ctx, b, form, fn, fnp);
     bool replayed = false;
     if (ctx->opt.use_graph && rb == 0 && re == b.total_rays) {
@@ -657,7 +667,7 @@ extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc
     if (rc) return rc;
     CK(cudaMemsetAsync(ctx->d_trace, 0, bytes, ctx->stream));
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp);
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp, false);
     LaunchShape ls = default_shape(ctx, fnp, precision);
     ls.grid = 1;
     ls.block = 32;

@@ -282,6 +282,107 @@ __device__ __forceinline__ void trace_record(const TraceSpec& tr, const RayState
 constexpr int kRayMaxBlock = 128;
 constexpr int kRayMinBlocks = RAPTOR_RAY_MIN_BLOCKS;
 
+// Per-launch statistics of the ray kernels, folded over the warp and added
+// to the counters buffer by one lane per warp.
+struct RayCounters {
+    unsigned long long steps = 0, rt_calls = 0, rt_samples = 0, rays = 0, cap = 0, nan = 0, max_steps = 0;
+    double kk_max = 0.0;
+
+    __device__ __forceinline__ void publish(unsigned long long* __restrict__ counters, int lane) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            steps += __shfl_xor_sync(kFull, steps, o);
+            rt_calls += __shfl_xor_sync(kFull, rt_calls, o);
+            rt_samples += __shfl_xor_sync(kFull, rt_samples, o);
+            rays += __shfl_xor_sync(kFull, rays, o);
+            cap += __shfl_xor_sync(kFull, cap, o);
+            nan += __shfl_xor_sync(kFull, nan, o);
+            max_steps = max(max_steps, __shfl_xor_sync(kFull, max_steps, o));
+            kk_max = fmax(kk_max, __shfl_xor_sync(kFull, kk_max, o));
+        }
+        if (lane == 0) {
+            atomicAdd(&counters[kCtrSteps], steps);
+            atomicAdd(&counters[kCtrRtCalls], rt_calls);
+            atomicAdd(&counters[kCtrRtSamples], rt_samples);
+            atomicAdd(&counters[kCtrRays], rays);
+            atomicAdd(&counters[kCtrStepCap], cap);
+            atomicAdd(&counters[kCtrNonFinite], nan);
+            atomicMax(&counters[kCtrMaxSteps], max_steps);
+            atomicMax(&counters[kCtrKkMax], (unsigned long long)__double_as_longlong(kk_max));
+        }
+    }
+};
+
+// A lane takes ray rid: its image, pixel, initial photon and zeroed transfer state.
+template <int NF, bool MIXED>
+__device__ __forceinline__ const DevImage* start_ray(const DevImage* __restrict__ imgs, int n_imgs, long long rid,
+                                                     RayState<NF, MIXED>& s) {
+    s.img = find_image(imgs, n_imgs, rid);
+    const DevImage* im = imgs + s.img;
+    s.pix = (int)(rid - im->ray_begin);
+    s.rid = rid;
+    const int px = s.pix % im->width, py = s.pix / im->width;
+    init_photon(*im, camera_of(*im), px, py, s.y, s.beta);
+    mks_point(s.y[1], s.y[2], im->geo, s.p);
+    s.steps = 0;
+    s.turns = 0;
+    s.stop = 0;
+    s.thdot_prev = 0.0;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        s.tau[f] = 0.0; s.I[f] = 0.0;
+        s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
+    }
+    return im;
+}
+
+// The ray has ended: write intensityfield[pix][f] * nu^3 (core.c:121-137) and
+// its statistics.
+template <int NF, bool MIXED>
+__device__ __forceinline__ void finish_ray(const DevImage& im, const RayState<NF, MIXED>& s,
+                                           double* __restrict__ out, RayCounters& c) {
+    double* o = out + im.out_offset + (long long)s.pix * im.nfreq;
+    const PixelScale ps = pixel_scale(im, s.pix % im.width);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        if (f >= im.nfreq) break;
+        double v;
+        if constexpr (MIXED) v = ((double)s.If[f] + (double)s.Ic[f]) * kE2C;
+        else v = s.I[f];
+        o[f] = scale_output(im, ps, v, f);
+    }
+    c.steps += (unsigned long long)s.steps;
+    c.rays += 1;
+    if ((double)s.steps >= kMaxSteps) ++c.cap;
+    if (!(s.p.rp == s.p.rp) || !isfinite(s.y[5])) ++c.nan;
+    c.max_steps = max(c.max_steps, (unsigned long long)s.steps);
+    const double kk = null_drift(s.p, im.geo, s.y);
+    if (kk == kk) c.kk_max = fmax(c.kk_max, kk);
+}
+
+// The step of integrate_geodesic's loop body (integrator.c:228-285) for a
+// ray that has not ended: theta-turn count, step size, RK step.  Returns the
+// event: 0 stepped outside the sampling region, 1 inside it (sample due),
+// 3 escaped outward (integrator.c:271-272), -1 the while-condition ended the
+// ray before the step.  dl is the step taken.
+template <int NF, bool MIXED>
+__device__ __forceinline__ int advance_ray(const DevImage& im, RayState<NF, MIXED>& s, double& dl) {
+    // while-condition of integrator.c:228-229 (r = exp(x1), no R0)
+    const double r = s.p.rp;
+    if (!(r < kCutoffOuter && r > im.cutoff_inner && (double)s.steps < kMaxSteps && !s.stop)) return -1;
+    // theta turning points limit the lensed-image order (integrator.c:243-247)
+    if (s.thdot_prev * s.y[6] < 0.0 && s.steps > 2) s.turns += 1;
+    s.thdot_prev = s.y[6];
+    if ((s.beta < 0.0 && s.turns > kMaxOrder) || (s.beta > 0.0 && s.turns > kMaxOrder + 1)) s.stop = 1;
+    dl = step_size(im, s.y);
+    if (im.integrator == 2) rk2_step(im.geo, s.y, s.p, dl);
+    else rk4_step(im.geo, s.y, s.p, dl);
+    s.steps += 1;
+    if (s.y[1] > im.stopx1 && s.y[5] < 0.0) return 3;
+    if (s.y[1] < im.stopx1 && s.y[1] > im.startx1 && s.y[2] > im.startx2 && s.y[2] < im.stopx2) return 1;
+    return 0;
+}
+
 template <int NF, bool MIXED>
 __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
     ray_kernel(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
@@ -291,9 +392,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
     RayState<NF, MIXED> s;
     bool active = false, live = true;
     const DevImage* im = imgs;
-    unsigned long long n_steps = 0, n_rt_calls = 0, n_rt_samples = 0, n_rays = 0, n_cap = 0, n_nan = 0;
-    unsigned long long max_steps = 0;
-    double kk_max = 0.0;
+    RayCounters c;
 
     while (true) {
         // refill idle lanes from the device-wide ray queue
@@ -306,22 +405,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
             if (!active && live) {
                 const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
                 if (rid < ray_end) {
-                    s.img = find_image(imgs, n_imgs, rid);
-                    im = imgs + s.img;
-                    s.pix = (int)(rid - im->ray_begin);
-                    s.rid = rid;
-                    const int px = s.pix % im->width, py = s.pix / im->width;
-                    init_photon(*im, camera_of(*im), px, py, s.y, s.beta);
-                    mks_point(s.y[1], s.y[2], im->geo, s.p);
-                    s.steps = 0;
-                    s.turns = 0;
-                    s.stop = 0;
-                    s.thdot_prev = 0.0;
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) {
-                        s.tau[f] = 0.0; s.I[f] = 0.0;
-                        s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
-                    }
+                    im = start_ray(imgs, n_imgs, rid, s);
                     active = true;
                     if (tr.out && rid == tr.ray) trace_record<NF, MIXED>(tr, s, 0.0, 0);
                 } else {
@@ -332,82 +416,209 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
         if (!__any_sync(kFull, active)) break;
         if (active) {
             for (int it = 0; it < refill_interval; ++it) {
-                // while-condition of integrator.c:228-229 (r = exp(x1), no R0)
-                const double r = s.p.rp;
-                bool done = !(r < kCutoffOuter && r > im->cutoff_inner && (double)s.steps < kMaxSteps &&
-                              !s.stop);
-                if (!done) {
-                    // theta turning points limit the lensed-image order (integrator.c:243-247)
-                    if (s.thdot_prev * s.y[6] < 0.0 && s.steps > 2) s.turns += 1;
-                    s.thdot_prev = s.y[6];
-                    if ((s.beta < 0.0 && s.turns > kMaxOrder) || (s.beta > 0.0 && s.turns > kMaxOrder + 1))
-                        s.stop = 1;
-                    const double dl = step_size(*im, s.y);
-                    if (im->integrator == 2) rk2_step(im->geo, s.y, s.p, dl);
-                    else rk4_step(im->geo, s.y, s.p, dl);
-                    s.steps += 1;
-                    int event = 0;
-                    if (s.y[1] > im->stopx1 && s.y[5] < 0.0) {
-                        done = true;  // escaped outward (integrator.c:271-272)
-                        event = 3;
-                    } else if (s.y[1] < im->stopx1 && s.y[1] > im->startx1 && s.y[2] > im->startx2 &&
-                               s.y[2] < im->stopx2) {
-                        ++n_rt_calls;
-                        bool sampled;
-                        if constexpr (MIXED) sampled = rt_sample_fp32<NF>(*im, s.y, s.p, fabs(dl), s.tf, s.tc, s.If, s.Ic);
-                        else sampled = rt_sample_fp64<NF>(*im, s.y, s.p, fabs(dl), s.tau, s.I);
-                        n_rt_samples += sampled ? 1 : 0;
-                        event = sampled ? 2 : 1;
-                    }
-                    if (tr.out && s.rid == tr.ray) trace_record<NF, MIXED>(tr, s, dl, event);
+                double dl = 0.0;
+                int event = advance_ray(*im, s, dl);
+                const bool done = event == -1 || event == 3;
+                if (event == 1) {
+                    ++c.rt_calls;
+                    bool sampled;
+                    if constexpr (MIXED) sampled = rt_sample_fp32<NF>(*im, s.y, s.p, fabs(dl), s.tf, s.tc, s.If, s.Ic);
+                    else sampled = rt_sample_fp64<NF>(*im, s.y, s.p, fabs(dl), s.tau, s.I);
+                    c.rt_samples += sampled ? 1 : 0;
+                    event = sampled ? 2 : 1;
                 }
+                if (event != -1 && tr.out && s.rid == tr.ray) trace_record<NF, MIXED>(tr, s, dl, event);
                 if (done) {
-                    // write intensityfield[pix][f] * nu^3 (core.c:121-137)
-                    double* o = out + im->out_offset + (long long)s.pix * im->nfreq;
-                    const PixelScale ps = pixel_scale(*im, s.pix % im->width);
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) {
-                        if (f >= im->nfreq) break;
-                        double v;
-                        if constexpr (MIXED) v = ((double)s.If[f] + (double)s.Ic[f]) * kE2C;
-                        else v = s.I[f];
-                        o[f] = scale_output(*im, ps, v, f);
-                    }
-                    n_steps += (unsigned long long)s.steps;
-                    n_rays += 1;
-                    if ((double)s.steps >= kMaxSteps) ++n_cap;
-                    if (!(s.p.rp == s.p.rp) || !isfinite(s.y[5])) ++n_nan;
-                    max_steps = max(max_steps, (unsigned long long)s.steps);
-                    const double kk = null_drift(s.p, im->geo, s.y);
-                    if (kk == kk) kk_max = fmax(kk_max, kk);
+                    finish_ray(*im, s, out, c);
                     active = false;
                     break;
                 }
             }
         }
     }
-    // fold per-lane statistics: warp shuffle, then one atomic per warp
+    c.publish(counters, lane);
+}
+
+// ------------------------------------------------- FP64 form, sample pool
+//
+// In the FP64 form a warp's lanes are seldom all inside the sampling region
+// at once (on a 1024x1024 image of the torus, 92 % of warp steps run the
+// sample with 60 % of their lanes taking part), so the in-place sample runs
+// at little more than half width.  ray_kernel_pool evaluates the
+// order-free part of the sample (rt_terms_fp64: fluid, emissivity,
+// absorptivity) at full width: each step, lanes inside the region append a
+// ticket - the sample's inputs - to a per-warp ring in shared memory; once 32
+// tickets wait, every lane evaluates one, and each owner then applies its
+// evaluated tickets in step order (rt_apply_fp64).  A ray that has ended waits
+// for its outstanding tickets before it writes its pixel; a partial batch is
+// evaluated when such a ray has waited kPoolDrainWait steps or no lane of the
+// warp is stepping.  Per ray the operations and their order are those of
+// ray_kernel, so the images are bit-identical.
+constexpr int kPoolCap = 64;  // ring entries per warp: up to 31 waiting + 32 appended in one step
+#ifndef RAPTOR_POOL_DRAIN_WAIT
+#define RAPTOR_POOL_DRAIN_WAIT 4
+#endif
+constexpr int kPoolDrainWait = RAPTOR_POOL_DRAIN_WAIT;
+
+template <int NF>
+struct PoolLayout {
+    // ticket fields, one row of kPoolCap doubles each: 0 |dl|, 1-2 x1 x2,
+    // 3-6 k^mu, 7-14 the point (r, s, c, c2x, iS, irp, ithp, isn); evaluated,
+    // rows 1..NF hold dtau and NF+1..2NF j / nu_p^2
+    static constexpr int kIn = 15;
+    static constexpr int kOut = 1 + 2 * NF;
+    static constexpr int kFields = kIn > kOut ? kIn : kOut;
+    // + the next-ticket links and image indices (two ints per entry)
+    static constexpr int kWarpDoubles = kFields * kPoolCap + kPoolCap;
+};
+
+template <int NF>
+__global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
+    ray_kernel_pool(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
+                    unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval) {
+    using L = PoolLayout<NF>;
+    constexpr int C = kPoolCap;
+    __shared__ double pool_mem[(kRayMaxBlock / 32) * L::kWarpDoubles];
+    const int lane = threadIdx.x & 31;
+    double* const fld = pool_mem + (threadIdx.x >> 5) * L::kWarpDoubles;
+    int* const nxt = reinterpret_cast<int*>(fld + L::kFields * C);
+    int* const timg = nxt + C;
+    RayState<NF, false> s;
+    int mode = 0;  // 0 idle, 1 stepping, 2 ended with tickets outstanding
+    bool live = true;
+    unsigned qh = 0, ql = 0;  // this lane's oldest and newest outstanding ticket (sequence numbers)
+    int qn = 0, wait = 0;
+    unsigned head = 0, tail = 0;  // warp-uniform: oldest unevaluated ticket, next free sequence number
+    int since_refill = refill_interval;
+    const DevImage* im = imgs;
+    RayCounters c;
+
+    while (true) {
+        // refill idle lanes every refill_interval steps, or at once when the warp has nothing to do
+        const unsigned need = __ballot_sync(kFull, mode == 0 && live);
+        if (need && (since_refill >= refill_interval || !__any_sync(kFull, mode != 0))) {
+            since_refill = 0;
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (mode == 0 && live) {
+                const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
+                if (rid < ray_end) {
+                    im = start_ray(imgs, n_imgs, rid, s);
+                    mode = 1;
+                } else {
+                    live = false;
+                }
+            }
+        }
+        if (!__any_sync(kFull, mode != 0)) break;
+        ++since_refill;
+
+        // one geodesic step per stepping lane; a step inside the region appends a ticket
+        bool want = false;
+        double dl = 0.0;
+        if (mode == 1) {
+            const int event = advance_ray(*im, s, dl);
+            if (event == 1) {
+                ++c.rt_calls;
+                want = true;
+            }
+            if (event == -1 || event == 3) {
+                mode = 2;
+                wait = 0;
+            }
+        }
+        const unsigned wm = __ballot_sync(kFull, want);
+        if (want) {
+            const unsigned seq = tail + __popc(wm & ((1u << lane) - 1u));
+            const int t = (int)(seq & (C - 1));
+            double* e = fld + t;
+            e[0] = fabs(dl);
+            e[1 * C] = s.y[1];
+            e[2 * C] = s.y[2];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        n_steps += __shfl_xor_sync(kFull, n_steps, o);
-        n_rt_calls += __shfl_xor_sync(kFull, n_rt_calls, o);
-        n_rt_samples += __shfl_xor_sync(kFull, n_rt_samples, o);
-        n_rays += __shfl_xor_sync(kFull, n_rays, o);
-        n_cap += __shfl_xor_sync(kFull, n_cap, o);
-        n_nan += __shfl_xor_sync(kFull, n_nan, o);
-        max_steps = max(max_steps, __shfl_xor_sync(kFull, max_steps, o));
-        kk_max = fmax(kk_max, __shfl_xor_sync(kFull, kk_max, o));
+            for (int i = 0; i < 4; ++i) e[(3 + i) * C] = s.y[4 + i];
+            e[7 * C] = s.p.r;
+            e[8 * C] = s.p.s;
+            e[9 * C] = s.p.c;
+            e[10 * C] = s.p.c2x;
+            e[11 * C] = s.p.iS;
+            e[12 * C] = s.p.irp;
+            e[13 * C] = s.p.ithp;
+            e[14 * C] = s.p.isn;
+            timg[t] = s.img;
+            if (qn > 0) nxt[ql & (C - 1)] = (int)seq;
+            else qh = seq;
+            ql = seq;
+            ++qn;
+        }
+        tail += (unsigned)__popc(wm);
+
+        if (mode == 2 && qn > 0) ++wait;
+        const unsigned cnt = tail - head;
+        const bool flush = __any_sync(kFull, mode == 2 && qn > 0 && wait > kPoolDrainWait) ||
+                           !__any_sync(kFull, mode == 1);
+        if (cnt >= 32u || (cnt > 0u && flush)) {
+            __syncwarp();
+            const unsigned n = cnt < 32u ? cnt : 32u;
+            if ((unsigned)lane < n) {
+                // evaluate ticket head + lane
+                double* e = fld + ((head + (unsigned)lane) & (C - 1));
+                double y[8];
+                MksPoint mp;
+                y[0] = 0.0;
+                y[1] = e[1 * C];
+                y[2] = e[2 * C];
+                y[3] = 0.0;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) y[4 + i] = e[(3 + i) * C];
+                mp.rp = 0.0;  // the metric does not read rp, s2x
+                mp.s2x = 0.0;
+                mp.r = e[7 * C];
+                mp.s = e[8 * C];
+                mp.c = e[9 * C];
+                mp.c2x = e[10 * C];
+                mp.iS = e[11 * C];
+                mp.irp = e[12 * C];
+                mp.ithp = e[13 * C];
+                mp.isn = e[14 * C];
+                double dtau[NF], jn[NF];
+                const bool ok = rt_terms_fp64<NF>(imgs[timg[(head + (unsigned)lane) & (C - 1)]], y, mp, e[0], dtau, jn);
+                c.rt_samples += ok ? 1 : 0;
+#pragma unroll
+                for (int f = 0; f < NF; ++f) {
+                    e[(1 + f) * C] = ok ? dtau[f] : 0.0;
+                    e[(1 + NF + f) * C] = ok ? jn[f] : 0.0;
+                }
+            }
+            __syncwarp();
+            head += n;
+            // owners apply their evaluated tickets, oldest first
+            while (true) {
+                const bool mine = qn > 0 && (int)(qh - head) < 0;
+                if (!__any_sync(kFull, mine)) break;
+                if (mine) {
+                    const int t = (int)(qh & (C - 1));
+                    const double* e = fld + t;
+                    double dtau[NF], jn[NF];
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        dtau[f] = e[(1 + f) * C];
+                        jn[f] = e[(1 + NF + f) * C];
+                    }
+                    rt_apply_fp64<NF>(*im, e[0], dtau, jn, s.tau, s.I);
+                    if (--qn > 0) qh = (unsigned)nxt[t];
+                }
+            }
+            __syncwarp();
+        }
+        if (mode == 2 && qn == 0) {
+            finish_ray(*im, s, out, c);
+            mode = 0;
+        }
     }
-    if (lane == 0) {
-        atomicAdd(&counters[kCtrSteps], n_steps);
-        atomicAdd(&counters[kCtrRtCalls], n_rt_calls);
-        atomicAdd(&counters[kCtrRtSamples], n_rt_samples);
-        atomicAdd(&counters[kCtrRays], n_rays);
-        atomicAdd(&counters[kCtrStepCap], n_cap);
-        atomicAdd(&counters[kCtrNonFinite], n_nan);
-        atomicMax(&counters[kCtrMaxSteps], max_steps);
-        atomicMax(&counters[kCtrKkMax], (unsigned long long)__double_as_longlong(kk_max));
-    }
+    c.publish(counters, lane);
 }
 
 // Spectrum: core.c:146-150 sums intensityfield over pixels per frequency.

@@ -161,9 +161,25 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
 }
 
 // ---------------------------------------------------------------- FP64 form
+// The sample splits into the part that depends only on the post-step point -
+// fluid, emissivity and absorptivity, per frequency the optical-depth
+// increment nu_p a_nu dl_f and j_nu / nu_p^2 - and the tau / I update that
+// depends on the ray's history.  rt_terms_fp64 and rt_apply_fp64 are that
+// split; run back to back (rt_sample_fp64) they are the sample of
+// radiative_transfer.c:71-98, operation for operation.
+
+// Returns false in the sigma cut (no change to the ray).  Frequencies that do
+// not emit get dtau = jn = 0, except where B_nu underflows to 0 (exp overflow
+// at very low Theta_e): there the reference gets a = 0 / 0 and tau NaN for the
+// rest of the ray, carried here as dtau = NaN.
 template <int NF>
-__device__ __forceinline__ bool rt_sample_fp64(const DevImage& im, const double y[8], const MksPoint& p,
-                                               double adl, double (&tau)[NF], double (&I)[NF]) {
+__device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y[8], const MksPoint& p,
+                                              double adl, double (&dtau)[NF], double (&jn)[NF]) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        dtau[f] = 0.0;
+        jn[f] = 0.0;
+    }
     MetricDD gd;
     MetricUU gu;
     mks_metric(p, im.geo, gd, gu);
@@ -198,27 +214,47 @@ __device__ __forceinline__ bool rt_sample_fp64(const DevImage& im, const double 
         double nup = -kU * im.freq[f];
         if (nup <= 0.0) nup = 1.0;
         const double dlf = adl * im.rg_over_nu[f];
+        const double Bnu = 2.0 * nup * nup * nup / (kC * kC) * 1.0 /
+                           (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
         if (emits && nup != 1.0) {
             const double X = nup / nus;
             const double cb = cbrt(X);
             const double sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);  // 2^(11/12)
             const double j = fl.ne * 1.4142135623730951 * CUDART_PI * nus / (3.0 * K2) * (sq * sq) *
                              exp(-cb) * kE2C;
-            const double Bnu = 2.0 * nup * nup * nup / (kC * kC) * 1.0 /
-                               (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
             const double an = j * kE2CH / Bnu / kE2C;
-            tau[f] += nup * an * dlf;
-            const double dI = (j / (nup * nup)) * exp(-tau[f]) * dlf;
-            if (tau[f] < 6.907755278982137 && !(tau[f] < 0.0)) I[f] += dI;  // log(1000)
-        } else {
-            // j = 0.  a = 0 / B_nu is 0 unless B_nu underflowed to 0 (exp
-            // overflow at very low Theta_e), where the reference gets NaN and
-            // tau stays NaN for the rest of the ray.
-            const double Bnu = 2.0 * nup * nup * nup / (kC * kC) * 1.0 /
-                               (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
-            if (!(Bnu != 0.0)) tau[f] = __longlong_as_double(0x7ff8000000000000ll);
+            dtau[f] = nup * an * dlf;
+            jn[f] = j / (nup * nup);
+        } else if (!(Bnu != 0.0)) {
+            dtau[f] = __longlong_as_double(0x7ff8000000000000ll);
         }
     }
+    return true;
+}
+
+// The ordered part: tau += dtau, then I += j/nu_p^2 e^-tau dl_f inside the
+// tau gate (radiative_transfer.c:89-95).  The two sums are rounded on their
+// own (as the reference, C without FMA contraction, does), so no kernel can
+// fuse them with the products that formed their terms.
+template <int NF>
+__device__ __forceinline__ void rt_apply_fp64(const DevImage& im, double adl, const double (&dtau)[NF],
+                                              const double (&jn)[NF], double (&tau)[NF], double (&I)[NF]) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        if (f >= im.nfreq) break;
+        if (dtau[f] == 0.0 && jn[f] == 0.0) continue;  // no emission: tau and I unchanged
+        tau[f] = __dadd_rn(tau[f], dtau[f]);
+        const double dI = jn[f] * exp(-tau[f]) * (adl * im.rg_over_nu[f]);
+        if (tau[f] < 6.907755278982137 && !(tau[f] < 0.0)) I[f] = __dadd_rn(I[f], dI);  // log(1000)
+    }
+}
+
+template <int NF>
+__device__ __forceinline__ bool rt_sample_fp64(const DevImage& im, const double y[8], const MksPoint& p,
+                                               double adl, double (&tau)[NF], double (&I)[NF]) {
+    double dtau[NF], jn[NF];
+    if (!rt_terms_fp64<NF>(im, y, p, adl, dtau, jn)) return false;
+    rt_apply_fp64<NF>(im, adl, dtau, jn, tau, I);
     return true;
 }
 

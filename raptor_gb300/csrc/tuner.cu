@@ -29,7 +29,11 @@ namespace {
 std::string signature(const raptor_gpu_ctx* ctx, const Batch& b, int form) {
     char k[384];
     const int size_class = (int)std::log2((double)std::max<long long>(b.total_rays, 1));
-    snprintf(k, sizeof k, "%s|%s|nf%d|2^%d", ctx->device_name, form == RAPTOR_PREC_MIXED_DF ? "mixed_df" : (form == RAPTOR_PREC_MIXED ? "mixed" : "fp64"), b.max_nf, size_class);
+    const char* name = form == RAPTOR_PREC_MIXED_DF ? "mixed_df"
+                       : form == RAPTOR_PREC_MIXED  ? "mixed"
+                       : ctx->opt.no_sample_pool    ? "fp64_inplace"
+                                                    : "fp64";
+    snprintf(k, sizeof k, "%s|%s|nf%d|2^%d", ctx->device_name, name, b.max_nf, size_class);
     std::string s(k);
     for (char& c : s)
         if (c == ' ') c = '_';

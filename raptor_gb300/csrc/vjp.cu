@@ -399,7 +399,7 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
 
     // forward render (its image is the I of the suffix identity)
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp);
+    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp, !ctx->opt.no_sample_pool);
     LaunchShape ls = choose_shape(ctx, b, precision, fn, fnp);
     rc = enqueue_render(ctx, b, precision, 0, b.total_rays, ls, fn, true);
     if (rc) return rc;

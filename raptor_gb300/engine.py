@@ -45,7 +45,7 @@ class EngineError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("block_size", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("refill_interval", ctypes.c_int), ("autotune", ctypes.c_int), ("use_graph", ctypes.c_int),
-                ("reserved", ctypes.c_int * 8)]
+                ("no_sample_pool", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
 class GridGeomC(ctypes.Structure):
@@ -138,9 +138,9 @@ class Engine:
     """One engine context on one CUDA device."""
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, refill_interval: int = 0,
-                 autotune: int = 0, use_graph: int = 0):
+                 autotune: int = 0, use_graph: int = 0, no_sample_pool: int = 0):
         self.lib = load()
-        opt = Options(device, block_size, blocks_per_sm, refill_interval, autotune, use_graph)
+        opt = Options(device, block_size, blocks_per_sm, refill_interval, autotune, use_graph, no_sample_pool)
         h = ctypes.c_void_p()
         rc = self.lib.raptor_gpu_init(ctypes.byref(opt), ctypes.byref(h))
         if rc != 0:

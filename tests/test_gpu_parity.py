@@ -209,6 +209,49 @@ def test_batch_equals_single_images(eng, torus64):
         assert np.array_equal(batch, np.concatenate([a, b]))
 
 
+def test_sample_pool_matches_in_place(eng, torus64, torus256):
+    """The FP64 form's pooled kernel (samples evaluated 32 at a time from a
+    per-warp pool, applied by their rays in step order) and the in-place
+    kernel run the same arithmetic per ray: same step and sample counts, and
+    the same bits where the compiler emits the same FMA contractions in both
+    kernels - the 1-, 2- and 4-frequency instantiations.  The 8-frequency
+    instantiations (images with 5-8 frequencies) are separate compilations
+    whose last bits may differ; they agree to 1e-12.  Cases: one frequency,
+    five, RK2, the log-polar camera, a mixed batch, and a 256x256 image whose
+    warps leave the emitting region at different steps."""
+    from raptor_gb300 import engine
+    ref = engine.Engine(no_sample_pool=1)
+    try:
+        g64, g256 = _grid(eng, torus64), _grid(eng, torus256)
+        r64, r256 = ref.upload_grid(torus64.geom, torus64.prims), ref.upload_grid(torus256.geom, torus256.prims)
+        cases = [
+            lambda g, h: engine.image_desc(64, 64, [230e9], grid=g, inclination=60.0),
+            lambda g, h: engine.image_desc(24, 20, [86e9, 140e9, 230e9, 345e9, 690e9], grid=g, inclination=35.0),
+            lambda g, h: engine.image_desc(32, 32, [230e9], grid=g, inclination=120.0, integrator=engine.RK2),
+            lambda g, h: engine.image_desc(32, 32, [230e9], grid=g, inclination=17.0, camera=engine.CAM_LOG),
+            lambda g, h: [engine.image_desc(17, 9, [230e9], grid=g, inclination=30.0),
+                          engine.image_desc(8, 12, [86e9, 345e9], grid=g, inclination=150.0, m_unit=5e18),
+                          engine.image_desc(40, 40, [230e9], grid=h, inclination=75.0)],
+            lambda g, h: engine.image_desc(256, 256, [230e9], grid=h, inclination=60.0),
+        ]
+        for k, mk in enumerate(cases):
+            a, sa = eng.render(mk(g64, g256), engine.PREC_FP64)
+            st_a = eng.stats()
+            b, sb = ref.render(mk(r64, r256), engine.PREC_FP64)
+            st_b = ref.stats()
+            descs = mk(g64, g256)
+            if max(d.n_freq for d in (descs if isinstance(descs, list) else [descs])) <= 4:
+                assert np.array_equal(a, b, equal_nan=True), f"case {k}: pooled and in-place images differ"
+                assert np.array_equal(sa, sb, equal_nan=True), f"case {k}: spectra differ"
+            else:
+                np.testing.assert_allclose(a, b, rtol=1e-12, atol=0, err_msg=f"case {k}")
+                np.testing.assert_allclose(sa, sb, rtol=1e-12, atol=0, err_msg=f"case {k}")
+            for key in ("steps", "rt_calls", "rt_samples", "rays", "max_ray_steps"):
+                assert st_a[key] == st_b[key], f"case {k}: {key} {st_a[key]} != {st_b[key]}"
+    finally:
+        ref.close()
+
+
 def test_range_render_is_a_slice(eng, torus64):
     from raptor_gb300 import engine
     gid = _grid(eng, torus64)

@@ -387,6 +387,34 @@ def run_differentiable(dev, n_cells=4, reps=2):
     }
 
 
+def run_inclination(eng, blib, dev, gid, incl, forms, steps):
+    """The headline image at another inclination (the workload's second
+    angle): each form rendered `steps` times after an L2 flush (device time,
+    mean), with flux / pixel / k.k errors against the FP64 form."""
+    from raptor_gb300 import engine
+    desc = engine.image_desc(W, H, [FREQ], grid=gid, inclination=incl, stepsize=EPS)
+    got = {}
+    for prec, name in forms:
+        ms = []
+        for _ in range(max(1, steps)):
+            blib.raptor_bench_flush_l2(dev, L2_FLUSH_BYTES)
+            img, spec = eng.render(desc, prec)
+            ms.append(eng.stats()["device_ms"])
+        st = eng.stats()
+        got[name] = dict(img=img, flux=float(spec[0]), ms=float(np.mean(ms)), kk=st["kk_max"], steps=st["steps"])
+    ref = got["fp64"]
+    nz = ref["img"] != 0
+    out = {"inclination_deg": incl}
+    for name, g in got.items():
+        row = {"ms_per_image": g["ms"], "kk_max": g["kk"], "steps": g["steps"]}
+        if name != "fp64":
+            pe = np.abs(g["img"][nz] - ref["img"][nz]) / np.abs(ref["img"][nz])
+            row.update(speedup_vs_fp64=ref["ms"] / g["ms"], flux_err_vs_fp64=abs(g["flux"] - ref["flux"]) / ref["flux"],
+                       pixel_err_median=float(np.median(pe)), pixel_err_max=float(np.max(pe)))
+        out[name] = row
+    return out
+
+
 def run_engine(args, rank, world, local):
     from raptor_gb300 import engine
     dev = local
@@ -495,8 +523,9 @@ def run_engine(args, rank, world, local):
     flop = workload.image_flops(st["rays"], st["steps"], st["rt_samples"], 1, rk4=True)
     achieved = flop / (k_fp64 * 1e-3) / 1e12
 
-    vjp = batch = None
+    vjp = batch = incl17 = None
     if not args.no_e2e:
+        incl17 = run_inclination(eng, blib, dev, gid, 17.0, forms, args.steps)
         vjp = run_vjp_config4()
         batch = run_batch_config3(dev)
 
@@ -547,6 +576,7 @@ def run_engine(args, rank, world, local):
                          "vs_fp64_dfma_peak": (flop / (k_df * 1e-3) / 1e12) / peak.value if peak.value > 0 else None,
                          "launch": [results["mixed_df"]["stats"][k] for k in
                                     ("block_size", "blocks_per_sm", "refill_interval")]},
+            "inclination_17": incl17,
             "vjp": vjp,
             "batch": batch,
         },

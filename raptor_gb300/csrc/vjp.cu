@@ -355,6 +355,293 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     }
 }
 
+// ------------------------------------------- sample pool, one frequency
+//
+// The dual sample at a post-step point (sample_common + sample_freq: fluid,
+// emission and absorption with their six tangents) does not depend on the
+// ray's history, so, as in the forward kernel's pool (ray_kernel_pool),
+// lanes inside the sampling region append a ticket - the point, wave vector
+// and |d lambda| with their inclination tangents - to the warp's ring in
+// shared memory, every lane evaluates one once 32 wait, and the owners then
+// consume their evaluated tickets in step order: tau, the suffix identity,
+// the scalar tangents and the per-cell scatter, exactly as vjp_kernel does
+// in place.  The evaluating lane recomputes the point's transcendentals from
+// (x1, x2) rather than carrying them (16 more doubles per ticket).  One
+// frequency only: a ticket's result is 14 doubles per frequency.
+namespace vpool {
+constexpr int C = kPoolCap;
+// ticket rows (C doubles each).  In: 0-1 |dl|, 2-3 x1, 4-5 x2, 6-13 k^mu (value,
+// tangent).  Out: 0-6 S (value, six tangents), 7-13 dtau, 14 d1, 15 d2,
+// 16 d ln Theta_e / d u_s; ints: next ticket, kind (-1 sigma cut, else
+// sample_freq's), first cell
+constexpr int kFields = 17;
+constexpr int kWarpDoubles = kFields * C + (3 * C) / 2;
+}  // namespace vpool
+
+__global__ void __launch_bounds__(kVjpBlock, 1)
+    vjp_kernel_pool(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
+                    const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
+                    double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
+                    double* __restrict__ g_th, int refill_interval) {
+    using namespace vpool;
+    __shared__ double pool_mem[(kVjpBlock / 32) * kWarpDoubles];
+    const DevImage& im = *imp;
+    const int lane = threadIdx.x & 31;
+    double* const fld = pool_mem + (threadIdx.x >> 5) * kWarpDoubles;
+    int* const nxt = reinterpret_cast<int*>(fld + kFields * C);
+    int* const tkind = nxt + C;
+    int* const tbase = tkind + C;
+    const long long nrays = (long long)im.width * im.height;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
+
+    D1 y[8];
+    MksPointT<D1> p;
+    double beta = 0.0, thdot_prev = 0.0;
+    int steps = 0, turns = 0, stop = 0;
+    // tau, the forward I, the part of I accumulated so far, dL/dI, d tau / d(scalars), dL/dI dI/d(scalars)
+    double tau = 0.0, Itot = 0.0, Ipart = 0.0, w = 0.0, dtg[4], dIw[4];
+    int mode = 0;  // 0 idle, 1 stepping, 2 ended with tickets outstanding
+    bool live = true;
+    unsigned qh = 0, ql = 0;
+    int qn = 0, wait = 0;
+    unsigned head = 0, tail = 0;
+    int since_refill = refill_interval;
+
+    while (true) {
+        const unsigned need = __ballot_sync(kFull, mode == 0 && live);
+        if (need && (since_refill >= refill_interval || !__any_sync(kFull, mode != 0))) {
+            since_refill = 0;
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (mode == 0 && live) {
+                const long long rid = (long long)(base + __popc(need & ((1u << lane) - 1u)));
+                if (rid < nrays) {
+                    const int pix = (int)rid;
+                    init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
+                    mks_point(y[1], y[2], im.geo, p);
+                    const PixelScale ps = pixel_scale(im, pix % im.width);
+                    const double dOdI = scale_output(im, ps, 1.0, 0);
+                    Itot = fwd[pix] / dOdI;
+                    w = dLdO[pix] * dOdI;
+                    tau = 0.0;
+                    Ipart = 0.0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        dtg[q] = 0.0;
+                        dIw[q] = 0.0;
+                    }
+                    steps = 0;
+                    turns = 0;
+                    stop = 0;
+                    thdot_prev = 0.0;
+                    mode = 1;
+                } else {
+                    live = false;
+                }
+            }
+        }
+        if (!__any_sync(kFull, mode != 0)) break;
+        ++since_refill;
+
+        bool want = false;
+        D1 adl(0.0);
+        if (mode == 1) {
+            const double r = p.rp.v;
+            bool done = !(r < kCutoffOuter && r > im.cutoff_inner && (double)steps < kMaxSteps && !stop);
+            if (!done) {
+                if (thdot_prev * y[6].v < 0.0 && steps > 2) turns += 1;
+                thdot_prev = y[6].v;
+                if ((beta < 0.0 && turns > kMaxOrder) || (beta > 0.0 && turns > kMaxOrder + 1)) stop = 1;
+                const D1 dl = step_size(im, y);
+                if (im.integrator == 2) rk2_step(im.geo, y, p, dl);
+                else rk4_step_rolled(im.geo, y, p, dl);
+                steps += 1;
+                if (y[1].v > im.stopx1 && y[5].v < 0.0) {
+                    done = true;
+                } else if (y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 &&
+                           y[2].v < im.stopx2) {
+                    ++n_calls;
+                    want = true;
+                    adl = fabs(dl);
+                }
+            }
+            if (done) {
+                mode = 2;
+                wait = 0;
+            }
+        }
+        const unsigned wm = __ballot_sync(kFull, want);
+        if (want) {
+            const unsigned seq = tail + __popc(wm & ((1u << lane) - 1u));
+            const int t = (int)(seq & (C - 1));
+            double* e = fld + t;
+            e[0] = adl.v;
+            e[1 * C] = adl.d[0];
+            e[2 * C] = y[1].v;
+            e[3 * C] = y[1].d[0];
+            e[4 * C] = y[2].v;
+            e[5 * C] = y[2].d[0];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                e[(6 + 2 * i) * C] = y[4 + i].v;
+                e[(7 + 2 * i) * C] = y[4 + i].d[0];
+            }
+            if (qn > 0) nxt[ql & (C - 1)] = (int)seq;
+            else qh = seq;
+            ql = seq;
+            ++qn;
+        }
+        tail += (unsigned)__popc(wm);
+
+        if (mode == 2 && qn > 0) ++wait;
+        const unsigned cnt = tail - head;
+        const bool flush = __any_sync(kFull, mode == 2 && qn > 0 && wait > kPoolDrainWait) ||
+                           !__any_sync(kFull, mode == 1);
+        if (cnt >= 32u || (cnt > 0u && flush)) {
+            __syncwarp();
+            const unsigned n = cnt < 32u ? cnt : 32u;
+            if ((unsigned)lane < n) {
+                const int t = (int)((head + (unsigned)lane) & (C - 1));
+                double* e = fld + t;
+                D1 a(e[0]), x1(e[2 * C]), x2(e[4 * C]), k1[4];
+                a.d[0] = e[1 * C];
+                x1.d[0] = e[3 * C];
+                x2.d[0] = e[5 * C];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    k1[i] = D1(e[(6 + 2 * i) * C]);
+                    k1[i].d[0] = e[(7 + 2 * i) * C];
+                }
+                MksPointT<D1> mp;
+                mks_point(x1, x2, im.geo, mp);
+                SampleCommon sc;
+                CellCoef cc;
+                int kd = -1;
+                if (sample_common(im, x1, x2, k1, mp, a, cc, sc)) {
+                    ++n_samples;
+                    D6 S, dt;
+                    kd = sample_freq(im, sc, 0, S, dt);
+                    if (kd == 1) {
+                        e[0] = S.v;
+                        e[7 * C] = dt.v;
+#pragma unroll
+                        for (int q = 0; q < 6; ++q) {
+                            e[(1 + q) * C] = S.d[q];
+                            e[(8 + q) * C] = dt.d[q];
+                        }
+                    }
+                    e[14 * C] = cc.d1;
+                    e[15 * C] = cc.d2;
+                    e[16 * C] = sc.dlnth_du;
+                    tbase[t] = cc.base;
+                }
+                tkind[t] = kd;
+            }
+            __syncwarp();
+            head += n;
+            // owners consume their evaluated tickets, oldest first
+            while (true) {
+                const bool mine = qn > 0 && (int)(qh - head) < 0;
+                if (!__any_sync(kFull, mine)) break;
+                if (mine) {
+                    const int t = (int)(qh & (C - 1));
+                    const double* e = fld + t;
+                    const int kd = tkind[t];
+                    if (kd >= 0) {
+                        double Gr = 0.0, Gt = 0.0;
+                        if (kd == 1) {
+                            ++n_emit;
+                            const double Sv = e[0], dtv = e[7 * C];
+                            tau += dtv;
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) dtg[q] += e[(8 + gdir(q)) * C];
+                            const double ex = exp(-tau);
+                            const bool gate = tau < 6.907755278982137 && !(tau < 0.0);
+                            const double suffix = Itot - Ipart;
+                            const double eS = gate ? ex : 0.0;
+                            if (suffix != 0.0 || gate) {
+                                Gr = w * (eS * e[(1 + kDirRho) * C] - suffix * e[(8 + kDirRho) * C]);
+                                Gt = w * (eS * e[(1 + kDirU) * C] - suffix * e[(8 + kDirU) * C]);
+                            }
+                            if (gate) {
+                                ++n_gate;
+                                const double we = w * ex;
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) dIw[q] += we * (e[(1 + gdir(q)) * C] - Sv * dtg[q]);
+                                Ipart += Sv * ex;
+                            }
+                        } else if (kd == 2) {
+                            tau = __longlong_as_double(0x7ff8000000000000ll);
+                        }
+                        const double Gu = Gt * e[16 * C];
+                        if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
+                            const double d1 = e[14 * C], d2 = e[15 * C];
+                            const double w0 = (1.0 - d1) * (1.0 - d2), w1 = (1.0 - d1) * d2;
+                            const double w2 = d1 * (1.0 - d2), w3 = d1 * d2;
+                            const long long c = tbase[t], cn = c + im.n2;
+                            atomicAdd(&g_rho[c], Gr * w0);
+                            atomicAdd(&g_rho[c + 1], Gr * w1);
+                            atomicAdd(&g_rho[cn], Gr * w2);
+                            atomicAdd(&g_rho[cn + 1], Gr * w3);
+                            atomicAdd(&g_u[c], Gu * w0);
+                            atomicAdd(&g_u[c + 1], Gu * w1);
+                            atomicAdd(&g_u[cn], Gu * w2);
+                            atomicAdd(&g_u[cn + 1], Gu * w3);
+                            atomicAdd(&g_th[c], Gt * w0);
+                            atomicAdd(&g_th[c + 1], Gt * w1);
+                            atomicAdd(&g_th[cn], Gt * w2);
+                            atomicAdd(&g_th[cn + 1], Gt * w3);
+                        }
+                    }
+                    if (--qn > 0) qh = (unsigned)nxt[t];
+                }
+            }
+            __syncwarp();
+        }
+        if (mode == 2 && qn == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (isfinite(dIw[q])) acc[q] += dIw[q];
+            n_steps += (unsigned long long)steps;
+            n_rays += 1;
+            mode = 0;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_steps += __shfl_xor_sync(kFull, n_steps, o);
+        n_rays += __shfl_xor_sync(kFull, n_rays, o);
+        n_calls += __shfl_xor_sync(kFull, n_calls, o);
+        n_samples += __shfl_xor_sync(kFull, n_samples, o);
+        n_emit += __shfl_xor_sync(kFull, n_emit, o);
+        n_gate += __shfl_xor_sync(kFull, n_gate, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&counters[kCtrSteps], n_steps);
+        atomicAdd(&counters[kCtrRays], n_rays);
+        atomicAdd(&counters[kCtrRtCalls], n_calls);
+        atomicAdd(&counters[kCtrRtSamples], n_samples);
+        atomicAdd(&counters[kCtrVjpEmit], n_emit);
+        atomicAdd(&counters[kCtrVjpGate], n_gate);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        double v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+        if (lane == 0) atomicAdd(&gscal[q], v);
+    }
+}
+
+void launch_vjp_pool(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
+                     const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
+                     int refill) {
+    vjp_kernel_pool<<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
+}
+
 template <int NF>
 void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                 const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
@@ -362,7 +649,9 @@ void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& c
     vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt);
 }
 
-VjpLaunchFn pick_vjp_fp64(int nf, const void** fn) {
+// pool: the one-frequency sample-pool kernel where it applies
+VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool) {
+    if (nf <= 1 && pool) { *fn = (const void*)vjp_kernel_pool; return launch_vjp_pool; }
     if (nf <= 1) { *fn = (const void*)vjp_kernel<1>; return launch_vjp<1>; }
     if (nf <= 2) { *fn = (const void*)vjp_kernel<2>; return launch_vjp<2>; }
     if (nf <= 4) { *fn = (const void*)vjp_kernel<4>; return launch_vjp<4>; }
@@ -423,7 +712,7 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     int occ = 1;
     const void* kp = nullptr;
     const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp)
-                                                              : pick_vjp_fp64(b.max_nf, &kp);
+                                                              : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool);
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
     const int grid = ctx->num_sms * std::max(occ, 1);
     double* gsc = ctx->d_grad;

@@ -122,36 +122,6 @@ __device__ __forceinline__ DF operator-(double c, DF a) { return (-a) + c; }
 __device__ __forceinline__ DF operator/(double c, DF a) { return df_const(c) / a; }
 __device__ __forceinline__ DF operator/(DF a, double c) { return a / df_const(c); }
 
-// Sum of products a_0 b_0 + a_1 b_1 + ... with one renormalisation at the
-// end: the leading parts of the products accumulate through two-sums, and
-// their rounding errors, the cross terms and the two-sum errors in one FP32
-// compensation (Ogita, Rump and Oishi's Dot2, 2005).  12 instructions per
-// term against 15 for a product and a renormalised sum.
-struct DFAcc {
-    float s, c;
-};
-__device__ __forceinline__ void df_acc(DFAcc& acc, DF a, DF b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    const DF t = two_sum(acc.s, p);
-    acc.s = t.hi;
-    acc.c = __fadd_rn(acc.c, __fadd_rn(t.lo, e));
-}
-__device__ __forceinline__ void df_acc_all(DFAcc&) {}
-template <class... Rest>
-__device__ __forceinline__ void df_acc_all(DFAcc& acc, DF a, DF b, Rest... rest) {
-    df_acc(acc, a, b);
-    df_acc_all(acc, rest...);
-}
-template <class... Rest>
-__device__ __forceinline__ DF df_dot(DF a, DF b, Rest... rest) {
-    DFAcc acc{0.0f, 0.0f};
-    df_acc_all(acc, a, b, rest...);
-    return quick_two_sum(acc.s, acc.c);
-}
-
 __device__ __forceinline__ DF fma(DF a, DF b, DF c) { return a * b + c; }
 __device__ __forceinline__ DF fma(DF a, DF b, double c) { return a * b + c; }
 

@@ -48,6 +48,24 @@ struct MksPointT {
 };
 using MksPoint = MksPointT<double>;
 
+// The point's four reciprocals 1/Sigma, 1/r', 1/theta', 1/sin(theta) from
+// one division: with q = r' theta' sin(theta) Sigma, each is 1/q times the
+// other three factors, built from the running products (9 multiplications
+// and 1 division instead of 4 divisions).  At the exact pole (sin = 0) all
+// four are non-finite, where one division would leave only 1/sin infinite;
+// the geodesic is singular there either way.
+template <class R>
+__device__ __forceinline__ void point_reciprocals(const R& Sg, const R& thp, MksPointT<R>& p) {
+    const R q1 = p.rp * thp, q2 = q1 * p.s, q3 = q2 * Sg;
+    const R iq3 = 1.0 / q3;
+    p.iS = iq3 * q2;
+    const R iq2 = iq3 * Sg;
+    p.isn = iq2 * q1;
+    const R iq1 = iq2 * p.s;
+    p.ithp = iq1 * p.rp;
+    p.irp = iq1 * thp;
+}
+
 template <class R, class G>
 __device__ __forceinline__ void mks_point(R x1, R x2, const G& g, MksPointT<R>& p) {
     p.rp = fast_exp(x1);
@@ -57,10 +75,7 @@ __device__ __forceinline__ void mks_point(R x1, R x2, const G& g, MksPointT<R>& 
     fast_sincospi(fma(g.th_coef, p.s2x, x2), &p.s, &p.c);
     const R Sg = fma(p.r, p.r, g.a2 * p.c * p.c);
     const R thp = CUDART_PI * fma(g.one_m_h, p.c2x, 1.0);
-    p.iS = 1.0 / Sg;
-    p.irp = 1.0 / p.rp;
-    p.ithp = 1.0 / thp;
-    p.isn = 1.0 / p.s;
+    point_reciprocals(Sg, thp, p);
 }
 
 // mks_point with the two sincospi evaluations (of 2 x2, then of theta / pi)
@@ -84,10 +99,7 @@ __device__ __forceinline__ void mks_point_rolled(R x1, R x2, const G& g, MksPoin
     p.c = cv;
     const R Sg = fma(p.r, p.r, g.a2 * p.c * p.c);
     const R thp = CUDART_PI * fma(g.one_m_h, p.c2x, 1.0);
-    p.iS = 1.0 / Sg;
-    p.irp = 1.0 / p.rp;
-    p.ithp = 1.0 / thp;
-    p.isn = 1.0 / p.s;
+    point_reciprocals(Sg, thp, p);
 }
 
 // d^2 x^i / d lambda^2 = -Gamma^i_jk U^j U^k  (integrator.c:126-146 with the

@@ -201,11 +201,14 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
                    (fabs(kU) * fl.B * im.inv_B_unit);
     if (fabs(pitch) > 1.0) pitch /= fabs(pitch);
     const double sth = sqrt(1.0 - pitch * pitch);
-    const double nuc = kECharge * fl.B / (2.0 * CUDART_PI * kEMass * kC);
+    const double nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
     const double nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
     const bool emits = (fabs(sth) >= 1.e-10) && (fl.thetae > 1e-4);
-    const double K2 = 2.0 * fl.thetae * fl.thetae;
-    const double T = fl.thetae * kEMass * kC * kC / kBoltz;
+    // j = n_e sqrt(2) pi nu_s / (3 K2) F(X) e2_c with K2 = 2 Theta^2: the
+    // frequency-independent factor once per sample
+    const double jpre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0) * nus / (fl.thetae * fl.thetae) * kE2C;
+    // h nu / (k T) = nu h / (m_e c^2 Theta_e)
+    const double hkt = (kPlanck / (kEMass * kC * kC)) / fl.thetae;
     // one copy of the frequency body (5 frequencies: 7 % faster than unrolled)
 #pragma unroll 1
     for (int f = 0; f < NF; ++f) {
@@ -213,19 +216,21 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
         // freq_in_plasma_frame with nu scaling folded: -(u . k_d) nu
         double nup = -kU * im.freq[f];
         if (nup <= 0.0) nup = 1.0;
-        const double dlf = adl * im.rg_over_nu[f];
-        const double Bnu = 2.0 * nup * nup * nup / (kC * kC) * 1.0 /
-                           (exp(kPlanck * nup / (kBoltz * T)) - 1.0);
+        // B_nu = 2 nu^3 / c^2 / (e^{h nu / k T} - 1); ex = e^{h nu / k T} - 1
+        const double ex = fast_exp(hkt * nup) - 1.0;
         if (emits && nup != 1.0) {
+            const double dlf = adl * im.rg_over_nu[f];
             const double X = nup / nus;
             const double cb = cbrt(X);
             const double sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);  // 2^(11/12)
-            const double j = fl.ne * 1.4142135623730951 * CUDART_PI * nus / (3.0 * K2) * (sq * sq) *
-                             exp(-cb) * kE2C;
-            const double an = j * kE2CH / Bnu / kE2C;
-            dtau[f] = nup * an * dlf;
-            jn[f] = j / (nup * nup);
-        } else if (!(Bnu != 0.0)) {
+            const double j = jpre * (sq * sq) * fast_exp(-cb);
+            const double inup2 = 1.0 / (nup * nup);
+            // a nu = j e2_ch / B_nu / e2_c nu = j (e2_ch c^2 / (2 e2_c)) ex / nu^2: inf where
+            // B_nu underflows (ex = inf), NaN where j = 0 there too, as j e2_ch / B_nu
+            dtau[f] = j * (kE2CH * kC * kC / (2.0 * kE2C)) * ex * inup2 * dlf;
+            jn[f] = j * inup2;
+        } else if (!(ex < CUDART_INF)) {
+            // j = 0 and B_nu underflowed to 0: the reference's a = 0 / 0
             dtau[f] = __longlong_as_double(0x7ff8000000000000ll);
         }
     }

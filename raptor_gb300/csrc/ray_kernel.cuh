@@ -144,43 +144,45 @@ __device__ __forceinline__ void rhs(const MksPointT<R>& p, const G& g, const R y
 }
 
 // One RK4 step (integrator.c:13-41): stage weights 1/2, 1/2, 1 and
-// y += (k1 + 2 k2 + 2 k3 + k4)/6 summed in the reference's order.
-// p holds the point at y on entry and at the new y on exit.
+// y += dt (f1 + 2 f2 + 2 f3 + f4) / 6.  dt multiplies the stage offsets and
+// the final sum instead of each stage's derivatives (the reference forms
+// k_i = dt f_i first): 8 multiplications fewer per stage, the same step to
+// rounding.  p holds the point at y on entry and at the new y on exit.
 // Stages 2-4 run as one rolled loop: the stage body (point transcendentals,
-// 40 Christoffels, contraction) is large, and one copy of it instead of
+// the connection, contraction) is large, and one copy of it instead of
 // three keeps the kernel's hot loop inside the instruction cache.
 template <class R, class G>
 __device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R dt) {
+    using W = typename StageWeight<R>::type;
     R acc[8], ys[8], f[8];
     rhs(p, g, y, f);
+    const R hdt = dt * 0.5;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const R d = dt * f[i];
-        acc[i] = d;
-        ys[i] = y[i] + d * 0.5;
+        acc[i] = f[i];
+        ys[i] = y[i] + hdt * f[i];
     }
 #pragma unroll 1
     for (int q = 1; q < 4; ++q) {
         MksPointT<R> qp;
         mks_point(ys[1], ys[2], g, qp);
         rhs(qp, g, ys, f);
-        using W = typename StageWeight<R>::type;
-        const W wacc = (q == 3) ? W(1.0) : W(2.0);   // k2, k3 count twice
-        const W wnext = (q == 1) ? W(0.5) : W(1.0);  // stage weights 1/2, 1/2, 1
+        const W wacc = (q == 3) ? W(1.0) : W(2.0);  // f2, f3 count twice
+        const R dnext = (q == 1) ? hdt : dt;          // stage offsets dt/2, dt/2, dt
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const R d = dt * f[i];
-            acc[i] = acc[i] + d * wacc;
-            ys[i] = y[i] + d * wnext;
+            acc[i] = acc[i] + f[i] * wacc;
+            ys[i] = y[i] + dnext * f[i];
         }
     }
+    const R dt6 = dt * (1.0 / 6.0);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) y[i] = y[i] + 1.0 / 6.0 * acc[i];
+    for (int i = 0; i < 8; ++i) y[i] = y[i] + dt6 * acc[i];
     mks_point(y[1], y[2], g, p);
 }
 
 // The same RK4 step with all four stages and the end point's evaluation in
-// one rolled loop, so the stage body (point transcendentals, Christoffels,
+// one rolled loop, so the stage body (point transcendentals, connection,
 // contraction) exists once.  Same operations in the same order as rk4_step.
 // For the double-float state, where each operation is about ten FP32
 // instructions, the single copy keeps the hot loop from stalling on
@@ -189,6 +191,7 @@ template <class R, class G>
 __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>& p, R dt) {
     using W = typename StageWeight<R>::type;
     R acc[8], ys[8], f[8];
+    const R hdt = dt * 0.5;
 #pragma unroll
     for (int i = 0; i < 8; ++i) ys[i] = y[i];
     MksPointT<R> qp = p;
@@ -197,18 +200,18 @@ __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>
         if (q > 0) mks_point(ys[1], ys[2], g, qp);
         if (q == 4) break;
         rhs(qp, g, ys, f);
-        const W wacc = (q == 1 || q == 2) ? W(2.0) : W(1.0);  // k2, k3 count twice
-        const W wnext = (q < 2) ? W(0.5) : W(1.0);           // stage weights 1/2, 1/2, 1
+        const W wacc = (q == 1 || q == 2) ? W(2.0) : W(1.0);  // f2, f3 count twice
+        const R dnext = (q < 2) ? hdt : dt;                   // stage offsets dt/2, dt/2, dt
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const R d = dt * f[i];
-            acc[i] = (q == 0) ? d : acc[i] + d * wacc;
-            ys[i] = y[i] + d * wnext;
+            acc[i] = (q == 0) ? f[i] : acc[i] + f[i] * wacc;
+            ys[i] = y[i] + dnext * f[i];
         }
         if (q == 3) {
+            const R dt6 = dt * (1.0 / 6.0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
-                y[i] = y[i] + 1.0 / 6.0 * acc[i];
+                y[i] = y[i] + dt6 * acc[i];
                 ys[i] = y[i];
             }
         }

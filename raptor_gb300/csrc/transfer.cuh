@@ -6,9 +6,10 @@
 // radiative_transfer.c:71-98.
 //
 // Two forms share the sampling structure:
-//  * rt_sample_fp64 - FP64 throughout, the reference's arithmetic (pow of
-//    1/2, 1/6, 1/3 written as sqrt / cbrt; a = j e2_ch / B_nu / e2_c kept
-//    literally so its edge cases match the reference's).
+//  * rt_sample_fp64 - FP64 throughout, the reference's formulas (pow of
+//    1/2, 1/6, 1/3 written as sqrt / cbrt) with fewer divisions: constant
+//    divisors folded, a nu formed without B_nu, its edge cases (B_nu
+//    underflow) those of the reference's a = j e2_ch / B_nu / e2_c.
 //  * rt_sample_fp32 - metric in FP64, then fluid, tetrad projection,
 //    emissivity and the tau / I accumulation in FP32 with Neumaier
 //    compensated sums.  Emissivity is carried without the e2_c factor and

@@ -223,7 +223,8 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
             const double dlf = adl * im.rg_over_nu[f];
             const double X = nup / nus;
             const double cb = cbrt(X);
-            const double sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);  // 2^(11/12)
+            // X^1/2 + 2^(11/12) X^1/6 = X^1/6 (X^1/3 + 2^(11/12)): one square root
+            const double sq = sqrt(cb) * (cb + 1.8877486253633869);
             const double j = jpre * (sq * sq) * fast_exp(-cb);
             const double inup2 = 1.0 / (nup * nup);
             // a nu = j e2_ch / B_nu / e2_c nu = j (e2_ch c^2 / (2 e2_c)) ex / nu^2: inf where
@@ -306,7 +307,7 @@ __device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const Me
         const float dlf = dlf_of(f);
         const float X = nup / nus;
         const float cb = cbrtf(X);
-        const float sq = sqrtf(X) + 1.8877486f * sqrtf(cb);
+        const float sq = sqrtf(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
         const float jh = jpre * (sq * sq) * expf(-cb);
         const float q = (jh / nup) / nup;
         const float dtau = q * expm1f(xpre * nup) * ktau * dlf;

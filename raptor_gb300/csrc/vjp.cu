@@ -140,7 +140,7 @@ __device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommo
         const D6 dlf = sc.adl * im.rg_over_nu[fi];
         const D6 X = nup / sc.nus;
         const D6 cb = cbrt(X);
-        const D6 sq = sqrt(X) + 1.8877486253633869 * sqrt(cb);
+        const D6 sq = sqrt(cb) * (cb + 1.8877486253633869);  // X^1/2 + 2^(11/12) X^1/6
         const D6 jn = sc.pre * (sq * sq) * exp(-cb) * kE2C;
         const D6 Bnu = 2.0 * nup * nup * nup / (kC * kC) / (exp(kPlanck * nup / sc.kT) - 1.0);
         const D6 an = jn * kE2CH / Bnu / kE2C;

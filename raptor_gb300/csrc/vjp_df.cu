@@ -162,7 +162,7 @@ __device__ __forceinline__ bool sample_freq_f(const DevImage& im, const SampleCo
     const F6 dlf = sc.adl * im.rg_over_nu_f[fi];
     const F6 X = nup / sc.nus;
     const F6 cb = cbrt(X);
-    const F6 sq = sqrt(X) + 1.8877486f * sqrt(cb);
+    const F6 sq = sqrt(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
     const F6 jh = sc.jpre * (sq * sq) * exp(-cb);
     const F6 q = (jh / nup) / nup;
     dtau = q * expm1(sc.xpre * nup) * (float)(kE2CH * kC * kC * 0.5) * dlf;

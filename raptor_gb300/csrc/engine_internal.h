@@ -62,6 +62,8 @@ struct raptor_gpu_ctx {
     size_t grad_cap = 0;
     double* d_dldi = nullptr;
     size_t dldi_cap = 0;
+    double* d_vjp_scratch = nullptr;  // the pooled FP64 adjoint's per-warp results (several frequencies)
+    size_t vjp_scratch_cap = 0;
     double* d_trace = nullptr;
     size_t trace_cap = 0;
     Batch batch;

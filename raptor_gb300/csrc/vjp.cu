@@ -44,23 +44,68 @@ using namespace raptor;
 
 namespace {
 
-__device__ __forceinline__ D6 lift(const D1& a) {
-    D6 r(a.v);
-    r.d[kDirIncl] = a.d[0];
+// The sample's dual directions: the inclination (through the geodesic), ln
+// Theta_e and ln B.  Everything else reaches a sample through these and n_e,
+// and n_e is a pure prefactor of j and a, so dS/d ln n_e = S and
+// d delta/d ln n_e = delta:
+//   rho_s:  n_e proportional to rho_s, and ln Theta_e by d ln Theta_e/d rho_s;
+//   u_s, R_high, R_low:  ln Theta_e only (the R-beta model, thetae_log_derivs);
+//   M_unit: n_e proportional to M_unit, B to sqrt(M_unit).
+// Three tangents instead of one per parameter: the dual sample costs about
+// half of a six-direction one.
+using D3 = Dual<3>;
+constexpr int kSIncl = 0, kSLnTh = 1, kSLnB = 2;
+
+__device__ __forceinline__ D3 lift(const D1& a) {
+    D3 r(a.v);
+    r.d[kSIncl] = a.d[0];
     return r;
 }
 
-// The frequency-independent part of one transfer sample, as value + six
+// The scalar factors that map a sample's (value, ln Theta_e) terms onto the
+// per-cell and scalar parameters.
+struct SampleScalars {
+    double irho;        // 1 / rho_s
+    double dlnth[4];    // d ln Theta_e / d(rho_s, u_s, R_high, R_low)
+};
+
+// d ln Theta_e / d(rho_s, u_s, R_high, R_low) of the R-beta electron
+// temperature (raptor_harm_model.c:262-276, fluid_from_prims):
+//   Theta_e = (u / rho) (gam(t) - 1) (m_p / m_e) / (1 + t),
+//   t = (R_high b^2 + R_low) / (1 + b^2),  b = (1/3) u / (Bsq / 2),
+//   gam(t) = ((1 + 2/3 (t + 1) / (t + 2)) + 4/3) / 2.
+// Zero where Theta_e was clamped (u / rho ... < 0).
+__device__ __forceinline__ void thetae_log_derivs(double rho, double uu, double bsq, double Rh, double Rl,
+                                                  double (&out)[4]) {
+    const double tiny = 1.e-20;
+    const double beta = uu * (4.0 / 3.0 - 1.0) / (0.5 * (bsq + tiny));
+    const double b2 = beta * beta;
+    const double i1b2 = 1.0 / (1.0 + b2);
+    const double t = Rh * b2 * i1b2 + Rl * i1b2;
+    const double gam = 0.5 * ((1.0 + 2.0 / 3.0 * (t + 1.0) / (t + 2.0)) + 4.0 / 3.0);
+    if ((uu / rho) * (gam - 1.0) < 0.0) {
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return;
+    }
+    const double dlnTU = (1.0 / 3.0) / ((t + 2.0) * (t + 2.0)) / (gam - 1.0) - 1.0 / (1.0 + t);  // d ln(Theta_e u^-1 rho) / dt
+    const double dt_dlnb = 2.0 * b2 * (Rh - Rl) * i1b2 * i1b2;                                  // dt / d ln beta
+    out[0] = -1.0 / rho;
+    out[1] = (1.0 + dlnTU * dt_dlnb) / uu;
+    out[2] = dlnTU * b2 * i1b2;
+    out[3] = dlnTU * i1b2;
+}
+
+// The frequency-independent part of one transfer sample, as value + three
 // tangents: the same arithmetic as rt_sample_fp64 (get_fluid_params
 // raptor_harm_model.c:190-290, pitch_angle radiative_transfer.c:32-47,
 // j_nu.c:130-153, 188-200) up to the frequency loop.
 struct SampleCommon {
-    D6 kU;        // k_mu u^mu
-    D6 nus;       // nu_s
-    D6 pre;       // n_e sqrt(2) pi nu_s / (3 K2), the first factors of j
-    D6 kT;        // k_B T
-    D6 adl;       // |d lambda|
-    double dlnth_du;  // d ln Theta_e / d u_s
+    D3 kU;        // k_mu u^mu
+    D3 nus;       // nu_s
+    D3 pre;       // n_e sqrt(2) pi nu_s / (3 K2), the first factors of j
+    D3 hkt;       // h / (k_B T): h nu / (k_B T) per Hz
+    D3 adl;       // |d lambda|
+    SampleScalars ss;
     bool emits;
 };
 
@@ -69,7 +114,7 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
     MetricDDT<D1> gd1;
     MetricUUT<D1> gu1;
     mks_metric(p, im.geo, gd1, gu1);
-    MetricT<D6> g;
+    MetricT<D3> g;
     g.d00 = lift(gd1.g00); g.d01 = lift(gd1.g01); g.d03 = lift(gd1.g03); g.d11 = lift(gd1.g11);
     g.d13 = lift(gd1.g13); g.d22 = lift(gd1.g22); g.d33 = lift(gd1.g33);
     g.u00 = lift(gu1.g00); g.u01 = lift(gu1.g01); g.u11 = lift(gu1.g11); g.u13 = lift(gu1.g13);
@@ -78,78 +123,145 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
     // Xtoij with the fractional offsets carrying their inclination tangent
     cc = cell_coef(im, x1.v, x2.v);
     const int i = cc.base / im.n2, j = cc.base % im.n2;
-    D6 d1 = D6(cc.d1), d2 = D6(cc.d2);
+    D3 d1 = D3(cc.d1), d2 = D3(cc.d2);
     {
         const double t1 = (x1.v - im.startx1) * im.idx1 - 0.5;
         const double t2 = (x2.v - im.startx2) * im.idx2 - 0.5;
-        if ((int)t1 == i) d1.d[kDirIncl] = x1.d[0] * im.idx1;  // not clamped
-        if ((int)t2 == j) d2.d[kDirIncl] = x2.d[0] * im.idx2;
+        if ((int)t1 == i) d1.d[kSIncl] = x1.d[0] * im.idx1;  // not clamped
+        if ((int)t2 == j) d2.d[kSIncl] = x2.d[0] * im.idx2;
     }
-    const D6 c0 = (1.0 - d1) * (1.0 - d2), c1 = (1.0 - d1) * d2, c2 = d1 * (1.0 - d2), c3 = d1 * d2;
+    const D3 c0 = (1.0 - d1) * (1.0 - d2), c1 = (1.0 - d1) * d2, c2 = d1 * (1.0 - d2), c3 = d1 * d2;
     double a[8], b[8], e[8], f[8];
     const double* cp = im.cells64 + (size_t)cc.base * 8;
     load_cell(cp, a);
     load_cell(cp + 8, b);
     load_cell(cp + (size_t)im.n2 * 8, e);
     load_cell(cp + (size_t)im.n2 * 8 + 8, f);
-    D6 v[8];
+    D3 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = c0 * a[q] + c1 * b[q] + c2 * e[q] + c3 * f[q];
-    v[0].d[kDirRho] += 1.0;  // rho_s and u_s as independent variables
-    v[1].d[kDirU] += 1.0;
 
-    D6 Ne_unit(im.Ne_unit), B_unit(im.B_unit), r_high(im.r_high), r_low(im.r_low);
-    Ne_unit.d[kDirLnM] = im.Ne_unit;     // Ne_unit proportional to M_unit
-    B_unit.d[kDirLnM] = 0.5 * im.B_unit;  // B_unit proportional to sqrt(M_unit)
-    r_high.d[kDirRh] = 1.0;
-    r_low.d[kDirRl] = 1.0;
-    Fluid<D6> fl;
-    if (!fluid_from_prims(v, g, Ne_unit, B_unit, r_high, r_low, fl)) return false;
-    // u_s moves nothing but Theta_e: keep d ln Theta_e/du_s and turn the
-    // direction into d/d ln Theta_e
-    out.dlnth_du = fl.thetae.v > 0.0 ? fl.thetae.d[kDirU] / fl.thetae.v : 0.0;
-    fl.thetae.d[kDirU] = fl.thetae.v;
+    const D3 B_unit(im.B_unit);
+    Fluid<D3> fl;
+    if (!fluid_from_prims(v, g, D3(im.Ne_unit), B_unit, D3(im.r_high), D3(im.r_low), fl)) return false;
+    out.ss.irho = 1.0 / v[0].v;
+    thetae_log_derivs(v[0].v, v[1].v, fl.bsq.v, im.r_high, im.r_low, out.ss.dlnth);
+    // pitch_angle divides by |k.u| B / B_unit, the field in code units, which
+    // M_unit does not move: formed before B takes its ln B direction
+    const D3 Bcode = fl.B / B_unit;
+    fl.thetae.d[kSLnTh] = fl.thetae.v;
+    fl.B.d[kSLnB] = fl.B.v - 1.e-20;  // B = sqrt(Bsq) B_unit + tiny: the part that scales
 
-    const D6 k[4] = {lift(k1[0]), lift(k1[1]), lift(k1[2]), lift(k1[3])};
-    D6 kd[4];
+    const D3 k[4] = {lift(k1[0]), lift(k1[1]), lift(k1[2]), lift(k1[3])};
+    D3 kd[4];
     lowerT(g, k, kd);
-    const D6* U = fl.ucon;
-    const D6* Bc = fl.bcon;
+    const D3* U = fl.ucon;
+    const D3* Bc = fl.bcon;
     out.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    D6 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * fl.B / B_unit);
-    if (fabs(pitch.v) > 1.0) pitch = D6(pitch.v > 0 ? 1.0 : -1.0);
-    const D6 s2 = 1.0 - pitch * pitch;
-    const D6 sth = s2.v > 0.0 ? sqrt(s2) : D6(0.0);
-    const D6 nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
+    D3 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * Bcode);
+    if (fabs(pitch.v) > 1.0) pitch = D3(pitch.v > 0 ? 1.0 : -1.0);
+    const D3 s2 = 1.0 - pitch * pitch;
+    const D3 sth = s2.v > 0.0 ? sqrt(s2) : D3(0.0);
+    const D3 nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
     out.nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
     out.emits = (fabs(sth.v) >= 1.e-10) && (fl.thetae.v > 1e-4);
-    const D6 K2 = 2.0 * fl.thetae * fl.thetae;
+    const D3 K2 = 2.0 * fl.thetae * fl.thetae;
     out.pre = fl.ne * (1.4142135623730951 * CUDART_PI) * out.nus / (3.0 * K2);
-    out.kT = kBoltz * (fl.thetae * (kEMass * kC * kC / kBoltz));
+    out.hkt = (kPlanck / (kEMass * kC * kC)) / fl.thetae;
     out.adl = lift(adl1);
     return true;
 }
 
-// The terms S and delta of the tau / I recurrence at frequency fi.
-// Returns 1 if the frequency emits, 2 where the primal's tau turns NaN
-// (0/0 in a with B_nu underflowed, transfer.cuh), else 0.
-__device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommon& sc, int fi, D6& S, D6& dtau) {
-    D6 nup = -sc.kU * im.freq[fi];
-    if (nup.v <= 0.0) nup = D6(1.0);
+// The terms S and delta of the tau / I recurrence at frequency fi, in the
+// FP64 sample's formulation (transfer.cuh, rt_terms_fp64): B_nu is never
+// formed, a nu = j (e2_ch c^2 / (2 e2_c)) (e^{h nu / k T} - 1) / nu^2.
+// Returns 1 if the frequency emits, 2 where the primal's tau turns NaN (B_nu
+// underflowed to 0), else 0.
+__device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommon& sc, int fi, D3& S, D3& dtau) {
+    D3 nup = -sc.kU * im.freq[fi];
+    if (nup.v <= 0.0) nup = D3(1.0);
     if (sc.emits && nup.v != 1.0) {
-        const D6 dlf = sc.adl * im.rg_over_nu[fi];
-        const D6 X = nup / sc.nus;
-        const D6 cb = cbrt(X);
-        const D6 sq = sqrt(cb) * (cb + 1.8877486253633869);  // X^1/2 + 2^(11/12) X^1/6
-        const D6 jn = sc.pre * (sq * sq) * exp(-cb) * kE2C;
-        const D6 Bnu = 2.0 * nup * nup * nup / (kC * kC) / (exp(kPlanck * nup / sc.kT) - 1.0);
-        const D6 an = jn * kE2CH / Bnu / kE2C;
-        dtau = nup * an * dlf;
-        S = jn / (nup * nup) * dlf;
+        const D3 dlf = sc.adl * im.rg_over_nu[fi];
+        const D3 X = nup / sc.nus;
+        const D3 cb = cbrt(X);
+        const D3 sq = sqrt(cb) * (cb + 1.8877486253633869);  // X^1/2 + 2^(11/12) X^1/6
+        const D3 jn = sc.pre * (sq * sq) * exp(-cb) * kE2C;
+        const D3 ex = exp(sc.hkt * nup) - 1.0;
+        const D3 inup2 = 1.0 / (nup * nup);
+        dtau = jn * (kE2CH * kC * kC / (2.0 * kE2C)) * ex * inup2 * dlf;
+        S = jn * inup2 * dlf;
         return 1;
     }
-    const double Bnu = 2.0 * nup.v * nup.v * nup.v / (kC * kC) * 1.0 / (exp(kPlanck * nup.v / sc.kT.v) - 1.0);
-    return !(Bnu != 0.0) ? 2 : 0;
+    const double ex = exp(sc.hkt.v * nup.v) - 1.0;
+    return !(ex < CUDART_INF) ? 2 : 0;
+}
+
+// A term's derivatives along the four scalar parameters (inclination,
+// ln M_unit, R_high, R_low) from its value and three tangents.
+__device__ __forceinline__ double scalar_tangent(const D3& x, const SampleScalars& ss, int q) {
+    if (q == 0) return x.d[kSIncl];
+    if (q == 1) return x.v + 0.5 * x.d[kSLnB];
+    return x.d[kSLnTh] * ss.dlnth[q];  // q = 2, 3: R_high, R_low
+}
+
+// One frequency's terms of a sample, consumed in step order: tau, the part
+// of I accumulated so far, d tau / d(scalars), dL/dI dI/d(scalars) (dIw), and
+// the sample's sums Gr, Gt of w (g e^-tau dS/dx - (I - I_<k) ddelta/dx) for
+// x = rho_s and ln Theta_e.  kind is sample_freq's.
+__device__ __forceinline__ void consume_term(int kind, const D3& S, const D3& dt, const SampleScalars& ss, double w,
+                                             double Itot, double& tau, double& Ipart, double (&dtg)[4],
+                                             double (&dIw)[4], double& Gr, double& Gt,
+                                             unsigned long long& n_emit, unsigned long long& n_gate) {
+    if (kind == 1) {
+        ++n_emit;
+        tau += dt.v;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dtg[q] += scalar_tangent(dt, ss, q);
+        const double e = exp(-tau);
+        const bool gate = tau < 6.907755278982137 && !(tau < 0.0);
+        const double suffix = Itot - Ipart;
+        const double eS = gate ? e : 0.0;
+        if (suffix != 0.0 || gate) {
+            // d/d rho_s = (d/d ln n_e) / rho_s + (d ln Theta_e / d rho_s) d/d ln Theta_e
+            const double S_rho = S.v * ss.irho + S.d[kSLnTh] * ss.dlnth[0];
+            const double dt_rho = dt.v * ss.irho + dt.d[kSLnTh] * ss.dlnth[0];
+            Gr += w * (eS * S_rho - suffix * dt_rho);
+            Gt += w * (eS * S.d[kSLnTh] - suffix * dt.d[kSLnTh]);
+        }
+        if (gate) {
+            ++n_gate;
+            const double we = w * e;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) dIw[q] += we * (scalar_tangent(S, ss, q) - S.v * dtg[q]);
+            Ipart += S.v * e;
+        }
+    } else if (kind == 2) {
+        tau = __longlong_as_double(0x7ff8000000000000ll);
+    }
+}
+
+// A sample's per-cell gradients: Gr, Gu = Gt d ln Theta_e / d u_s and Gt on
+// the four cells of its bilinear interpolation, with FP64 atomics.
+__device__ __forceinline__ void scatter_cells(double* __restrict__ g_rho, double* __restrict__ g_u,
+                                              double* __restrict__ g_th, long long base, int n2, double d1,
+                                              double d2, double Gr, double Gt, double dlnth_du) {
+    const double Gu = Gt * dlnth_du;
+    if (!((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho)) return;
+    const double w0 = (1.0 - d1) * (1.0 - d2), w1 = (1.0 - d1) * d2;
+    const double w2 = d1 * (1.0 - d2), w3 = d1 * d2;
+    const long long c = base, cn = base + n2;
+    atomicAdd(&g_rho[c], Gr * w0);
+    atomicAdd(&g_rho[c + 1], Gr * w1);
+    atomicAdd(&g_rho[cn], Gr * w2);
+    atomicAdd(&g_rho[cn + 1], Gr * w3);
+    atomicAdd(&g_u[c], Gu * w0);
+    atomicAdd(&g_u[c + 1], Gu * w1);
+    atomicAdd(&g_u[cn], Gu * w2);
+    atomicAdd(&g_u[cn + 1], Gu * w3);
+    atomicAdd(&g_th[c], Gt * w0);
+    atomicAdd(&g_th[c + 1], Gt * w1);
+    atomicAdd(&g_th[cn], Gt * w2);
+    atomicAdd(&g_th[cn + 1], Gt * w3);
 }
 
 // Inclination-dependent camera constants with their tangent per degree.
@@ -289,50 +401,12 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 #pragma unroll 1
                     for (int f = 0; f < NF; ++f) {
                         if (f >= im.nfreq) break;
-                        D6 S, dt;
+                        D3 S, dt;
                         const int kind = sample_freq(im, sc, f, S, dt);
-                        if (kind == 1) {
-                            ++n_emit;
-                            tau[f] += dt.v;
-#pragma unroll
-                            for (int q = 0; q < 4; ++q) dtg[f][q] += dt.d[gdir(q)];
-                            const double e = exp(-tau[f]);
-                            const bool gate = tau[f] < 6.907755278982137 && !(tau[f] < 0.0);
-                            const double suffix = Itot[f] - Ipart[f];
-                            const double eS = gate ? e : 0.0;
-                            if (suffix != 0.0 || gate) {
-                                Gr += w[f] * (eS * S.d[kDirRho] - suffix * dt.d[kDirRho]);
-                                Gt += w[f] * (eS * S.d[kDirU] - suffix * dt.d[kDirU]);
-                            }
-                            if (gate) {
-                                ++n_gate;
-                                const double we = w[f] * e;
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) dIw[q] += we * (S.d[gdir(q)] - S.v * dtg[f][q]);
-                                Ipart[f] += S.v * e;
-                            }
-                        } else if (kind == 2) {
-                            tau[f] = __longlong_as_double(0x7ff8000000000000ll);
-                        }
+                        consume_term(kind, S, dt, sc.ss, w[f], Itot[f], tau[f], Ipart[f], dtg[f], dIw, Gr, Gt,
+                                     n_emit, n_gate);
                     }
-                    const double Gu = Gt * sc.dlnth_du;
-                    if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
-                        const double w0 = (1.0 - cc.d1) * (1.0 - cc.d2), w1 = (1.0 - cc.d1) * cc.d2;
-                        const double w2 = cc.d1 * (1.0 - cc.d2), w3 = cc.d1 * cc.d2;
-                        const long long c = cc.base, cn = cc.base + im.n2;
-                        atomicAdd(&g_rho[c], Gr * w0);
-                        atomicAdd(&g_rho[c + 1], Gr * w1);
-                        atomicAdd(&g_rho[cn], Gr * w2);
-                        atomicAdd(&g_rho[cn + 1], Gr * w3);
-                        atomicAdd(&g_u[c], Gu * w0);
-                        atomicAdd(&g_u[c + 1], Gu * w1);
-                        atomicAdd(&g_u[cn], Gu * w2);
-                        atomicAdd(&g_u[cn + 1], Gu * w3);
-                        atomicAdd(&g_th[c], Gt * w0);
-                        atomicAdd(&g_th[c + 1], Gt * w1);
-                        atomicAdd(&g_th[cn], Gt * w2);
-                        atomicAdd(&g_th[cn + 1], Gt * w3);
-                    }
+                    scatter_cells(g_rho, g_u, g_th, cc.base, im.n2, cc.d1, cc.d2, Gr, Gt, sc.ss.dlnth[1]);
                 }
             }
         }
@@ -355,7 +429,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     }
 }
 
-// ------------------------------------------- sample pool, one frequency
+// ------------------------------------------------------------ sample pool
 //
 // The dual sample at a post-step point (sample_common + sample_freq: fluid,
 // emission and absorption with their six tangents) does not depend on the
@@ -366,31 +440,48 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 // consume their evaluated tickets in step order: tau, the suffix identity,
 // the scalar tangents and the per-cell scatter, exactly as vjp_kernel does
 // in place.  The evaluating lane recomputes the point's transcendentals from
-// (x1, x2) rather than carrying them (16 more doubles per ticket).  One
-// frequency only: a ticket's result is 14 doubles per frequency.
+// (x1, x2) rather than carrying them (16 more doubles per ticket).  A
+// ticket's result is 7 + 8 NF doubles: with one frequency it overwrites the
+// ticket in shared memory; with more it goes to the warp's slice of a
+// scratch buffer in device memory (L2-resident: 24 KB per warp at five
+// frequencies).
 namespace vpool {
 constexpr int C = kPoolCap;
-// ticket rows (C doubles each).  In: 0-1 |dl|, 2-3 x1, 4-5 x2, 6-13 k^mu (value,
-// tangent).  Out: 0-6 S (value, six tangents), 7-13 dtau, 14 d1, 15 d2,
-// 16 d ln Theta_e / d u_s; ints: next ticket, kind (-1 sigma cut, else
-// sample_freq's), first cell
-constexpr int kFields = 17;
-constexpr int kWarpDoubles = kFields * C + (3 * C) / 2;
+// ticket rows, C doubles each.  In: 0-1 |dl|, 2-3 x1, 4-5 x2, 6-13 k^mu
+// (value, tangent).  Out: 0 d1, 1 d2, 2 1/rho_s, 3-6 d ln Theta_e / d(rho_s,
+// u_s, R_high, R_low), then per frequency f at 7 + 8 f: S (value, three
+// tangents) and dtau.  Ints per entry: next ticket, first cell, per
+// frequency the kind (sample_freq's; -1 at frequency 0: sigma cut).
+constexpr int kIn = 14;
+template <int NF>
+struct Layout {
+    static constexpr int kOut = 7 + 8 * NF;
+    static constexpr bool kSharedOut = NF == 1;
+    static constexpr int kSharedRows = kSharedOut ? (kOut > kIn ? kOut : kIn) : kIn;
+    static constexpr int kWarpDoubles = kSharedRows * C + ((2 + NF) * C + 1) / 2;
+    static constexpr int kScratchRows = kSharedOut ? 0 : kOut;  // per warp, in the scratch buffer
+};
 }  // namespace vpool
 
+template <int NF>
 __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel_pool(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                     const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                     double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                    double* __restrict__ g_th, int refill_interval) {
+                    double* __restrict__ g_th, int refill_interval, double* __restrict__ scratch) {
     using namespace vpool;
-    __shared__ double pool_mem[(kVjpBlock / 32) * kWarpDoubles];
+    using L = Layout<NF>;
+    __shared__ double pool_mem[(kVjpBlock / 32) * L::kWarpDoubles];
     const DevImage& im = *imp;
     const int lane = threadIdx.x & 31;
-    double* const fld = pool_mem + (threadIdx.x >> 5) * kWarpDoubles;
-    int* const nxt = reinterpret_cast<int*>(fld + kFields * C);
-    int* const tkind = nxt + C;
-    int* const tbase = tkind + C;
+    double* const fld = pool_mem + (threadIdx.x >> 5) * L::kWarpDoubles;
+    int* const nxt = reinterpret_cast<int*>(fld + L::kSharedRows * C);
+    int* const tbase = nxt + C;
+    int* const tkind = tbase + C;  // [NF][C]
+    // evaluated results: the ticket rows themselves, or this warp's scratch slice
+    double* const res = L::kSharedOut ? fld
+                                      : scratch + (size_t)(blockIdx.x * (kVjpBlock / 32) + (threadIdx.x >> 5)) *
+                                                      L::kScratchRows * C;
     const long long nrays = (long long)im.width * im.height;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
@@ -399,8 +490,9 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     MksPointT<D1> p;
     double beta = 0.0, thdot_prev = 0.0;
     int steps = 0, turns = 0, stop = 0;
-    // tau, the forward I, the part of I accumulated so far, dL/dI, d tau / d(scalars), dL/dI dI/d(scalars)
-    double tau = 0.0, Itot = 0.0, Ipart = 0.0, w = 0.0, dtg[4], dIw[4];
+    // per frequency: tau, the forward I, the part of I accumulated so far, dL/dI and
+    // d tau / d(scalars); dIw = sum over frequencies of dL/dI dI/d(scalars)
+    double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dIw[4];
     int mode = 0;  // 0 idle, 1 stepping, 2 ended with tickets outstanding
     bool live = true;
     unsigned qh = 0, ql = 0;
@@ -423,16 +515,23 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                     init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
                     mks_point(y[1], y[2], im.geo, p);
                     const PixelScale ps = pixel_scale(im, pix % im.width);
-                    const double dOdI = scale_output(im, ps, 1.0, 0);
-                    Itot = fwd[pix] / dOdI;
-                    w = dLdO[pix] * dOdI;
-                    tau = 0.0;
-                    Ipart = 0.0;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        dtg[q] = 0.0;
-                        dIw[q] = 0.0;
+                    for (int f = 0; f < NF; ++f) {
+                        tau[f] = 0.0;
+                        Ipart[f] = 0.0;
+                        Itot[f] = 0.0;
+                        w[f] = 0.0;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) dtg[f][q] = 0.0;
+                        if (f < im.nfreq) {
+                            const long long o = (long long)pix * im.nfreq + f;
+                            const double dOdI = scale_output(im, ps, 1.0, f);
+                            Itot[f] = fwd[o] / dOdI;
+                            w[f] = dLdO[o] * dOdI;
+                        }
                     }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) dIw[q] = 0.0;
                     steps = 0;
                     turns = 0;
                     stop = 0;
@@ -519,26 +618,37 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 mks_point(x1, x2, im.geo, mp);
                 SampleCommon sc;
                 CellCoef cc;
-                int kd = -1;
+                double* const o = res + t;
                 if (sample_common(im, x1, x2, k1, mp, a, cc, sc)) {
                     ++n_samples;
-                    D6 S, dt;
-                    kd = sample_freq(im, sc, 0, S, dt);
-                    if (kd == 1) {
-                        e[0] = S.v;
-                        e[7 * C] = dt.v;
+#pragma unroll 1
+                    for (int f = 0; f < NF; ++f) {
+                        int kd = 0;
+                        if (f < im.nfreq) {
+                            D3 S, dt;
+                            kd = sample_freq(im, sc, f, S, dt);
+                            if (kd == 1) {
+                                double* of = o + (7 + 8 * f) * C;
+                                of[0] = S.v;
+                                of[4 * C] = dt.v;
 #pragma unroll
-                        for (int q = 0; q < 6; ++q) {
-                            e[(1 + q) * C] = S.d[q];
-                            e[(8 + q) * C] = dt.d[q];
+                                for (int q = 0; q < 3; ++q) {
+                                    of[(1 + q) * C] = S.d[q];
+                                    of[(5 + q) * C] = dt.d[q];
+                                }
+                            }
                         }
+                        tkind[f * C + t] = kd;
                     }
-                    e[14 * C] = cc.d1;
-                    e[15 * C] = cc.d2;
-                    e[16 * C] = sc.dlnth_du;
+                    o[0] = cc.d1;
+                    o[1 * C] = cc.d2;
+                    o[2 * C] = sc.ss.irho;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) o[(3 + q) * C] = sc.ss.dlnth[q];
                     tbase[t] = cc.base;
+                } else {
+                    tkind[t] = -1;
                 }
-                tkind[t] = kd;
             }
             __syncwarp();
             head += n;
@@ -548,53 +658,32 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 if (!__any_sync(kFull, mine)) break;
                 if (mine) {
                     const int t = (int)(qh & (C - 1));
-                    const double* e = fld + t;
-                    const int kd = tkind[t];
-                    if (kd >= 0) {
+                    const double* o = res + t;
+                    if (tkind[t] >= 0) {
+                        SampleScalars ss;
+                        ss.irho = o[2 * C];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) ss.dlnth[q] = o[(3 + q) * C];
                         double Gr = 0.0, Gt = 0.0;
-                        if (kd == 1) {
-                            ++n_emit;
-                            const double Sv = e[0], dtv = e[7 * C];
-                            tau += dtv;
+#pragma unroll 1
+                        for (int f = 0; f < NF; ++f) {
+                            if (f >= im.nfreq) break;
+                            const int kd = tkind[f * C + t];
+                            D3 S, dt;
+                            if (kd == 1) {
+                                const double* of = o + (7 + 8 * f) * C;
+                                S = D3(of[0]);
+                                dt = D3(of[4 * C]);
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) dtg[q] += e[(8 + gdir(q)) * C];
-                            const double ex = exp(-tau);
-                            const bool gate = tau < 6.907755278982137 && !(tau < 0.0);
-                            const double suffix = Itot - Ipart;
-                            const double eS = gate ? ex : 0.0;
-                            if (suffix != 0.0 || gate) {
-                                Gr = w * (eS * e[(1 + kDirRho) * C] - suffix * e[(8 + kDirRho) * C]);
-                                Gt = w * (eS * e[(1 + kDirU) * C] - suffix * e[(8 + kDirU) * C]);
+                                for (int q = 0; q < 3; ++q) {
+                                    S.d[q] = of[(1 + q) * C];
+                                    dt.d[q] = of[(5 + q) * C];
+                                }
                             }
-                            if (gate) {
-                                ++n_gate;
-                                const double we = w * ex;
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) dIw[q] += we * (e[(1 + gdir(q)) * C] - Sv * dtg[q]);
-                                Ipart += Sv * ex;
-                            }
-                        } else if (kd == 2) {
-                            tau = __longlong_as_double(0x7ff8000000000000ll);
+                            consume_term(kd, S, dt, ss, w[f], Itot[f], tau[f], Ipart[f], dtg[f], dIw, Gr, Gt,
+                                         n_emit, n_gate);
                         }
-                        const double Gu = Gt * e[16 * C];
-                        if ((Gr != 0.0 || Gt != 0.0) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
-                            const double d1 = e[14 * C], d2 = e[15 * C];
-                            const double w0 = (1.0 - d1) * (1.0 - d2), w1 = (1.0 - d1) * d2;
-                            const double w2 = d1 * (1.0 - d2), w3 = d1 * d2;
-                            const long long c = tbase[t], cn = c + im.n2;
-                            atomicAdd(&g_rho[c], Gr * w0);
-                            atomicAdd(&g_rho[c + 1], Gr * w1);
-                            atomicAdd(&g_rho[cn], Gr * w2);
-                            atomicAdd(&g_rho[cn + 1], Gr * w3);
-                            atomicAdd(&g_u[c], Gu * w0);
-                            atomicAdd(&g_u[c + 1], Gu * w1);
-                            atomicAdd(&g_u[cn], Gu * w2);
-                            atomicAdd(&g_u[cn + 1], Gu * w3);
-                            atomicAdd(&g_th[c], Gt * w0);
-                            atomicAdd(&g_th[c + 1], Gt * w1);
-                            atomicAdd(&g_th[cn], Gt * w2);
-                            atomicAdd(&g_th[cn + 1], Gt * w3);
-                        }
+                        scatter_cells(g_rho, g_u, g_th, tbase[t], im.n2, o[0], o[1 * C], Gr, Gt, ss.dlnth[1]);
                     }
                     if (--qn > 0) qh = (unsigned)nxt[t];
                 }
@@ -636,26 +725,44 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     }
 }
 
+template <int NF>
 void launch_vjp_pool(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                      const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                     int refill) {
-    vjp_kernel_pool<<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
+                     int refill, double* scratch) {
+    vjp_kernel_pool<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch);
 }
 
 template <int NF>
 void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                 const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                int) {
+                int, double*) {
     vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt);
 }
 
-// pool: the one-frequency sample-pool kernel where it applies
-VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool) {
-    if (nf <= 1 && pool) { *fn = (const void*)vjp_kernel_pool; return launch_vjp_pool; }
-    if (nf <= 1) { *fn = (const void*)vjp_kernel<1>; return launch_vjp<1>; }
-    if (nf <= 2) { *fn = (const void*)vjp_kernel<2>; return launch_vjp<2>; }
-    if (nf <= 4) { *fn = (const void*)vjp_kernel<4>; return launch_vjp<4>; }
-    if (nf <= 5) { *fn = (const void*)vjp_kernel<5>; return launch_vjp<5>; }
+// pool: the sample-pool kernel; *scratch_rows gets the scratch rows (of
+// kPoolCap doubles) it needs per warp
+VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows) {
+    *scratch_rows = 0;
+#define PICK(NF)                                                                         \
+    if (nf <= NF) {                                                                      \
+        if (pool) {                                                                      \
+            *fn = (const void*)vjp_kernel_pool<NF>;                                      \
+            *scratch_rows = vpool::Layout<NF>::kScratchRows;                             \
+            return launch_vjp_pool<NF>;                                                  \
+        }                                                                                \
+        *fn = (const void*)vjp_kernel<NF>;                                               \
+        return launch_vjp<NF>;                                                           \
+    }
+    PICK(1)
+    PICK(2)
+    PICK(4)
+    PICK(5)
+#undef PICK
+    if (pool) {
+        *fn = (const void*)vjp_kernel_pool<8>;
+        *scratch_rows = vpool::Layout<8>::kScratchRows;
+        return launch_vjp_pool<8>;
+    }
     *fn = (const void*)vjp_kernel<8>;
     return launch_vjp<8>;
 }
@@ -711,10 +818,18 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     // mixed forms, DF / FP32 duals for the mixed-DF form (vjp_df.cu)
     int occ = 1;
     const void* kp = nullptr;
-    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp)
-                                                              : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool);
+    int scratch_rows = 0;
+    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF
+                                ? pick_vjp_df(b.max_nf, &kp)
+                                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows);
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
     const int grid = ctx->num_sms * std::max(occ, 1);
+    // the pooled adjoint's per-warp result slices (several frequencies)
+    if (scratch_rows > 0) {
+        rc = ensure_buffer(ctx, (void**)&ctx->d_vjp_scratch, &ctx->vjp_scratch_cap,
+                           sizeof(double) * (size_t)grid * (kVjpBlock / 32) * scratch_rows * kPoolCap);
+        if (rc) return rc;
+    }
     double* gsc = ctx->d_grad;
     // the per-cell scatter runs when any of the three fields is asked for
     const bool fields = grad->d_rho || grad->d_u || grad->d_lnthetae;
@@ -723,7 +838,7 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     double* gth = fields ? ctx->d_grad + 4 + 2 * ncell : nullptr;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     vfn(grid, ctx->stream, ctx->d_imgs, cam, ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc, grho, gu, gth,
-        kVjpRefill);
+        kVjpRefill, ctx->d_vjp_scratch);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     double scal[4];

@@ -22,10 +22,11 @@ constexpr int kVjpRefill = 8;  // geodesic steps between lane refills of the mix
 // for image im (device pointer), camera constants with their inclination
 // tangent, the forward image fwd and dL/dI dl (device, image layout);
 // accumulates into counters, gscal[4] and the per-cell arrays (which may be
-// null); lanes take new rays every refill steps.
+// null); lanes take new rays every refill steps; scratch is the sample
+// pool's result buffer where the kernel has one.
 using VjpLaunchFn = void (*)(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                              const double* dl, unsigned long long* counters, double* gscal, double* g_rho,
-                             double* g_u, double* g_th, int refill);
+                             double* g_u, double* g_th, int refill, double* scratch);
 // the mixed-DF adjoint for nf frequencies (vjp_df.cu); *fn gets the kernel
 VjpLaunchFn pick_vjp_df(int nf, const void** fn);
 

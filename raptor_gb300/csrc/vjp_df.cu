@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
 template <int NF>
 void launch_vjp_df(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                    const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                   int refill) {
+                   int refill, double*) {
     vjp_kernel_df<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
 }
 

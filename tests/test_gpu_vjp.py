@@ -234,19 +234,21 @@ def test_vjp_log_camera_and_rk2(torus64, camera, integrator):
     assert not bad, "\n".join(bad)
 
 
-@pytest.mark.parametrize("camera,integrator", [(0, 4), (1, 2)])
-def test_vjp_sample_pool_matches_in_place(torus256, camera, integrator):
-    """The one-frequency FP64 adjoint with the per-warp sample pool
-    (vjp_kernel_pool) against the in-place kernel (no_sample_pool): the same
-    step, sample and term counts, scalar gradients within 1e-12 and per-cell
-    gradients within 1e-12 of the largest (the FP64 atomics of the per-cell
-    scatter add in a different order)."""
+@pytest.mark.parametrize("camera,integrator,freqs", [(0, 4, [230e9]), (1, 2, [230e9]),
+                                                     (0, 4, [86e9, 230e9, 345e9])])
+def test_vjp_sample_pool_matches_in_place(torus256, camera, integrator, freqs):
+    """The FP64 adjoint with the per-warp sample pool (vjp_kernel_pool; with
+    several frequencies its results go through the scratch buffer) against
+    the in-place kernel (no_sample_pool): the same step, sample and term
+    counts, scalar gradients within 1e-12 and per-cell gradients within 1e-12
+    of the largest (the FP64 atomics of the per-cell scatter add in a
+    different order)."""
     from raptor_gb300 import engine
     out = {}
     for nsp in (0, 1):
         eng = engine.Engine(no_sample_pool=nsp)
         gid = eng.upload_grid(torus256.geom, torus256.prims)
-        mk = lambda **o: engine.image_desc(64, 64, [230e9], **dict(dict(grid=gid, inclination=60.0, camera=camera, integrator=integrator), **o))  # noqa: E731
+        mk = lambda **o: engine.image_desc(64, 64, freqs, **dict(dict(grid=gid, inclination=60.0, camera=camera, integrator=integrator), **o))  # noqa: E731
         target, _ = eng.render(mk(inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0), engine.PREC_FP64)
         img, _ = eng.render(mk(), engine.PREC_FP64)
         _, g = eng.vjp(mk(), img - target, engine.PREC_FP64)

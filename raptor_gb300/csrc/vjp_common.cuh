@@ -1,6 +1,6 @@
 // Pieces shared by the two adjoint kernels (vjp.cu: FP64; vjp_df.cu:
-// mixed-DF): the dual types and tangent directions of a transfer sample,
-// and the launch interface of the mixed-DF adjoint.
+// mixed-DF): the inclination dual, the tangent directions of the mixed-DF
+// adjoint's six-direction sample, and the launch interface.
 #pragma once
 #include "dual.cuh"
 #include "ray_kernel.cuh"
@@ -8,9 +8,8 @@
 namespace raptor {
 
 using D1 = Dual<1>;
-using D6 = Dual<6>;
-// tangent directions of a sample: 0 inclination, 1 rho_s, 2 ln Theta_e (u_s),
-// 3 ln M_unit, 4 R_high, 5 R_low
+// tangent directions of the mixed-DF adjoint's sample: 0 inclination, 1 rho_s,
+// 2 ln Theta_e (u_s), 3 ln M_unit, 4 R_high, 5 R_low
 constexpr int kDirIncl = 0, kDirRho = 1, kDirU = 2, kDirLnM = 3, kDirRh = 4, kDirRl = 5;
 // the four scalar parameters' directions: 0 -> incl, 1 -> ln M, 2 -> R_high, 3 -> R_low
 __host__ __device__ __forceinline__ int gdir(int q) { return q == 0 ? kDirIncl : q + 2; }

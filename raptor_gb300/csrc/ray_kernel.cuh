@@ -458,6 +458,12 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
 // warp is stepping.  Per ray the operations and their order are those of
 // ray_kernel, so the images are bit-identical.
 constexpr int kPoolCap = 64;  // ring entries per warp: up to 31 waiting + 32 appended in one step
+// at least this many 128-thread blocks per SM: 2 gives 192 registers a
+// thread and 8 warps, 1 % faster at 1024x1024 than 3 (168 registers, 12
+// warps; 4 blocks spill)
+#ifndef RAPTOR_POOL_MIN_BLOCKS
+#define RAPTOR_POOL_MIN_BLOCKS 2
+#endif
 #ifndef RAPTOR_POOL_DRAIN_WAIT
 #define RAPTOR_POOL_DRAIN_WAIT 4
 #endif
@@ -476,7 +482,7 @@ struct PoolLayout {
 };
 
 template <int NF>
-__global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
+__global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
     ray_kernel_pool(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
                     unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval) {
     using L = PoolLayout<NF>;

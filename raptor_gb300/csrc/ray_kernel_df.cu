@@ -125,8 +125,10 @@ __device__ __forceinline__ void trace_record_df(const TraceSpec& tr, const RaySt
     r[15] = 0.0;
 }
 
+// 3 blocks of 128 per SM: 168 registers a thread and no spills (4 blocks
+// held 128 registers and spilled; 2 % slower at 1024x1024)
 #ifndef RAPTOR_RAY_DF_MIN_BLOCKS
-#define RAPTOR_RAY_DF_MIN_BLOCKS 4
+#define RAPTOR_RAY_DF_MIN_BLOCKS 3
 #endif
 
 template <int NF>

@@ -1,9 +1,10 @@
 // Launch-shape autotuner for the persistent ray kernel.
 //
-// The shape of the persistent launch - threads per block, resident blocks
-// per SM, and how many geodesic steps a lane runs between queue refills
-// ("steps per chunk") - trades FP64-pipe occupancy against lane idling at
-// ray ends.  With options.autotune set, the first render of a batch
+// The shape of the persistent launch - threads per block (at the resident
+// blocks per SM that the kernel's registers allow) and how many geodesic
+// steps a lane runs between queue refills ("steps per chunk") - trades
+// warp granularity against lane idling at ray ends.  With options.autotune
+// set, the first render of a batch
 // signature (device, precision, frequency bucket, size class) times each
 // candidate on a sample of that batch's rays - a contiguous range from its
 // middle, about six rays per lane - and keeps the fastest.  Results live in
@@ -77,22 +78,23 @@ LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunc
         ls.grid = ctx->num_sms * ls.bps;
         return ls;
     }
+    // Candidates run at full occupancy.  The timed sample has a few rays per
+    // lane, where a smaller grid wins by balancing the tail; on whole batches
+    // (~100 rays per lane) full occupancy is faster (64 images: 2 blocks of 128
+    // per SM 3545 ms, 1 block 3630 ms), so only the block size and the refill
+    // interval are tuned.
     std::vector<LaunchShape> cands;
     for (int block : {64, 128}) {
         int occ = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fnp, block, 0);
         occ = std::max(occ, 1);
-        for (int bps : {std::max(1, occ - 1), occ}) {
-            for (int refill : {1, 4, 8, 16}) {
-                LaunchShape ls;
-                ls.block = block;
-                ls.bps = bps;
-                ls.grid = ctx->num_sms * bps;
-                ls.refill = refill;
-                bool dup = false;
-                for (auto& c : cands) dup |= (c.block == ls.block && c.bps == ls.bps && c.refill == ls.refill);
-                if (!dup) cands.push_back(ls);
-            }
+        for (int refill : {1, 4, 8, 16}) {
+            LaunchShape ls;
+            ls.block = block;
+            ls.bps = occ;
+            ls.grid = ctx->num_sms * occ;
+            ls.refill = refill;
+            cands.push_back(ls);
         }
     }
     const long long lanes = (long long)ctx->num_sms * 3 * 128;

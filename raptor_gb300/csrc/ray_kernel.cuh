@@ -469,6 +469,58 @@ constexpr int kPoolCap = 64;  // ring entries per warp: up to 31 waiting + 32 ap
 #endif
 constexpr int kPoolDrainWait = RAPTOR_POOL_DRAIN_WAIT;
 
+// A warp's ring of sample tickets.  head (oldest unevaluated ticket) and
+// tail (next free sequence number) are the same in every lane; each lane
+// keeps its own outstanding tickets as a list - oldest qh, newest ql, count
+// qn - linked through nxt[] in shared memory.  Tickets are evaluated in ring
+// order, so a lane's evaluated tickets are always the oldest of its list and
+// it applies them oldest first.  Every member that votes (append, batch) is
+// called by all 32 lanes together.
+struct TicketRing {
+    unsigned head = 0, tail = 0;
+    unsigned qh = 0, ql = 0;
+    int qn = 0, wait = 0;
+
+    // Lanes with want take consecutive slots in lane order; returns this
+    // lane's slot, or -1.
+    __device__ __forceinline__ int append(bool want, int* nxt, int lane) {
+        const unsigned wm = __ballot_sync(kFull, want);
+        int t = -1;
+        if (want) {
+            const unsigned seq = tail + __popc(wm & ((1u << lane) - 1u));
+            t = (int)(seq & (kPoolCap - 1));
+            if (qn > 0) nxt[ql & (kPoolCap - 1)] = (int)seq;
+            else qh = seq;
+            ql = seq;
+            ++qn;
+        }
+        tail += (unsigned)__popc(wm);
+        return t;
+    }
+    // How many tickets to evaluate now: a warp's worth once 32 wait, or all
+    // that wait once a lane whose ray has ended (ended) has waited
+    // kPoolDrainWait steps for its tickets, or no lane is stepping; else 0.
+    __device__ __forceinline__ unsigned batch(bool ended, bool stepping) {
+        if (ended && qn > 0) ++wait;
+        const unsigned cnt = tail - head;
+        const bool flush = __any_sync(kFull, ended && qn > 0 && wait > kPoolDrainWait) || !__any_sync(kFull, stepping);
+        if (cnt >= 32u) return 32u;
+        return (cnt > 0u && flush) ? cnt : 0u;
+    }
+    // the slot a lane evaluates in the current batch
+    __device__ __forceinline__ int slot(int lane) const { return (int)((head + (unsigned)lane) & (kPoolCap - 1)); }
+    __device__ __forceinline__ void evaluated(unsigned n) { head += n; }
+    // this lane's oldest ticket if it has been evaluated, else -1
+    __device__ __forceinline__ int ready() const {
+        return (qn > 0 && (int)(qh - head) < 0) ? (int)(qh & (kPoolCap - 1)) : -1;
+    }
+    __device__ __forceinline__ void pop(const int* nxt, int t) {
+        if (--qn > 0) qh = (unsigned)nxt[t];
+    }
+    __device__ __forceinline__ bool empty() const { return qn == 0; }
+    __device__ __forceinline__ void ray_ended() { wait = 0; }
+};
+
 template <int NF>
 struct PoolLayout {
     // ticket fields, one row of kPoolCap doubles each: 0 |dl|, 1-2 x1 x2,
@@ -495,9 +547,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
     RayState<NF, false> s;
     int mode = 0;  // 0 idle, 1 stepping, 2 ended with tickets outstanding
     bool live = true;
-    unsigned qh = 0, ql = 0;  // this lane's oldest and newest outstanding ticket (sequence numbers)
-    int qn = 0, wait = 0;
-    unsigned head = 0, tail = 0;  // warp-uniform: oldest unevaluated ticket, next free sequence number
+    TicketRing ring;
     int since_refill = refill_interval;
     const DevImage* im = imgs;
     RayCounters c;
@@ -535,13 +585,11 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
             }
             if (event == -1 || event == 3) {
                 mode = 2;
-                wait = 0;
+                ring.ray_ended();
             }
         }
-        const unsigned wm = __ballot_sync(kFull, want);
-        if (want) {
-            const unsigned seq = tail + __popc(wm & ((1u << lane) - 1u));
-            const int t = (int)(seq & (C - 1));
+        const int t = ring.append(want, nxt, lane);
+        if (t >= 0) {
             double* e = fld + t;
             e[0] = fabs(dl);
             e[1 * C] = s.y[1];
@@ -557,23 +605,14 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
             e[13 * C] = s.p.ithp;
             e[14 * C] = s.p.isn;
             timg[t] = s.img;
-            if (qn > 0) nxt[ql & (C - 1)] = (int)seq;
-            else qh = seq;
-            ql = seq;
-            ++qn;
         }
-        tail += (unsigned)__popc(wm);
 
-        if (mode == 2 && qn > 0) ++wait;
-        const unsigned cnt = tail - head;
-        const bool flush = __any_sync(kFull, mode == 2 && qn > 0 && wait > kPoolDrainWait) ||
-                           !__any_sync(kFull, mode == 1);
-        if (cnt >= 32u || (cnt > 0u && flush)) {
+        const unsigned n = ring.batch(mode == 2, mode == 1);
+        if (n) {
             __syncwarp();
-            const unsigned n = cnt < 32u ? cnt : 32u;
             if ((unsigned)lane < n) {
-                // evaluate ticket head + lane
-                double* e = fld + ((head + (unsigned)lane) & (C - 1));
+                const int te = ring.slot(lane);
+                double* e = fld + te;
                 double y[8];
                 MksPoint mp;
                 y[0] = 0.0;
@@ -593,7 +632,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
                 mp.ithp = e[13 * C];
                 mp.isn = e[14 * C];
                 double dtau[NF], jn[NF];
-                const bool ok = rt_terms_fp64<NF>(imgs[timg[(head + (unsigned)lane) & (C - 1)]], y, mp, e[0], dtau, jn);
+                const bool ok = rt_terms_fp64<NF>(imgs[timg[te]], y, mp, e[0], dtau, jn);
                 c.rt_samples += ok ? 1 : 0;
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
@@ -602,14 +641,13 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
                 }
             }
             __syncwarp();
-            head += n;
+            ring.evaluated(n);
             // owners apply their evaluated tickets, oldest first
             while (true) {
-                const bool mine = qn > 0 && (int)(qh - head) < 0;
-                if (!__any_sync(kFull, mine)) break;
-                if (mine) {
-                    const int t = (int)(qh & (C - 1));
-                    const double* e = fld + t;
+                const int ta = ring.ready();
+                if (!__any_sync(kFull, ta >= 0)) break;
+                if (ta >= 0) {
+                    const double* e = fld + ta;
                     double dtau[NF], jn[NF];
 #pragma unroll
                     for (int f = 0; f < NF; ++f) {
@@ -617,12 +655,12 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
                         jn[f] = e[(1 + NF + f) * C];
                     }
                     rt_apply_fp64<NF>(*im, e[0], dtau, jn, s.tau, s.I);
-                    if (--qn > 0) qh = (unsigned)nxt[t];
+                    ring.pop(nxt, ta);
                 }
             }
             __syncwarp();
         }
-        if (mode == 2 && qn == 0) {
+        if (mode == 2 && ring.empty()) {
             finish_ray(*im, s, out, c);
             mode = 0;
         }

@@ -251,7 +251,7 @@ __device__ __forceinline__ void rt_apply_fp64(const DevImage& im, double adl, co
         if (f >= im.nfreq) break;
         if (dtau[f] == 0.0 && jn[f] == 0.0) continue;  // no emission: tau and I unchanged
         tau[f] = __dadd_rn(tau[f], dtau[f]);
-        const double dI = jn[f] * exp(-tau[f]) * (adl * im.rg_over_nu[f]);
+        const double dI = jn[f] * fast_exp(-tau[f]) * (adl * im.rg_over_nu[f]);
         if (tau[f] < 6.907755278982137 && !(tau[f] < 0.0)) I[f] = __dadd_rn(I[f], dI);  // log(1000)
     }
 }

@@ -495,9 +495,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     double tau[NF], Itot[NF], Ipart[NF], w[NF], dtg[NF][4], dIw[4];
     int mode = 0;  // 0 idle, 1 stepping, 2 ended with tickets outstanding
     bool live = true;
-    unsigned qh = 0, ql = 0;
-    int qn = 0, wait = 0;
-    unsigned head = 0, tail = 0;
+    TicketRing ring;
     int since_refill = refill_interval;
 
     while (true) {
@@ -569,13 +567,11 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             }
             if (done) {
                 mode = 2;
-                wait = 0;
+                ring.ray_ended();
             }
         }
-        const unsigned wm = __ballot_sync(kFull, want);
-        if (want) {
-            const unsigned seq = tail + __popc(wm & ((1u << lane) - 1u));
-            const int t = (int)(seq & (C - 1));
+        const int t = ring.append(want, nxt, lane);
+        if (t >= 0) {
             double* e = fld + t;
             e[0] = adl.v;
             e[1 * C] = adl.d[0];
@@ -588,23 +584,14 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 e[(6 + 2 * i) * C] = y[4 + i].v;
                 e[(7 + 2 * i) * C] = y[4 + i].d[0];
             }
-            if (qn > 0) nxt[ql & (C - 1)] = (int)seq;
-            else qh = seq;
-            ql = seq;
-            ++qn;
         }
-        tail += (unsigned)__popc(wm);
 
-        if (mode == 2 && qn > 0) ++wait;
-        const unsigned cnt = tail - head;
-        const bool flush = __any_sync(kFull, mode == 2 && qn > 0 && wait > kPoolDrainWait) ||
-                           !__any_sync(kFull, mode == 1);
-        if (cnt >= 32u || (cnt > 0u && flush)) {
+        const unsigned n = ring.batch(mode == 2, mode == 1);
+        if (n) {
             __syncwarp();
-            const unsigned n = cnt < 32u ? cnt : 32u;
             if ((unsigned)lane < n) {
-                const int t = (int)((head + (unsigned)lane) & (C - 1));
-                double* e = fld + t;
+                const int te = ring.slot(lane);
+                double* e = fld + te;
                 D1 a(e[0]), x1(e[2 * C]), x2(e[4 * C]), k1[4];
                 a.d[0] = e[1 * C];
                 x1.d[0] = e[3 * C];
@@ -618,7 +605,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 mks_point(x1, x2, im.geo, mp);
                 SampleCommon sc;
                 CellCoef cc;
-                double* const o = res + t;
+                double* const o = res + te;
                 if (sample_common(im, x1, x2, k1, mp, a, cc, sc)) {
                     ++n_samples;
 #pragma unroll 1
@@ -638,28 +625,27 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                                 }
                             }
                         }
-                        tkind[f * C + t] = kd;
+                        tkind[f * C + te] = kd;
                     }
                     o[0] = cc.d1;
                     o[1 * C] = cc.d2;
                     o[2 * C] = sc.ss.irho;
 #pragma unroll
                     for (int q = 0; q < 4; ++q) o[(3 + q) * C] = sc.ss.dlnth[q];
-                    tbase[t] = cc.base;
+                    tbase[te] = cc.base;
                 } else {
-                    tkind[t] = -1;
+                    tkind[te] = -1;
                 }
             }
             __syncwarp();
-            head += n;
+            ring.evaluated(n);
             // owners consume their evaluated tickets, oldest first
             while (true) {
-                const bool mine = qn > 0 && (int)(qh - head) < 0;
-                if (!__any_sync(kFull, mine)) break;
-                if (mine) {
-                    const int t = (int)(qh & (C - 1));
-                    const double* o = res + t;
-                    if (tkind[t] >= 0) {
+                const int ta = ring.ready();
+                if (!__any_sync(kFull, ta >= 0)) break;
+                if (ta >= 0) {
+                    const double* o = res + ta;
+                    if (tkind[ta] >= 0) {
                         SampleScalars ss;
                         ss.irho = o[2 * C];
 #pragma unroll
@@ -668,7 +654,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 #pragma unroll 1
                         for (int f = 0; f < NF; ++f) {
                             if (f >= im.nfreq) break;
-                            const int kd = tkind[f * C + t];
+                            const int kd = tkind[f * C + ta];
                             D3 S, dt;
                             if (kd == 1) {
                                 const double* of = o + (7 + 8 * f) * C;
@@ -683,14 +669,14 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                             consume_term(kd, S, dt, ss, w[f], Itot[f], tau[f], Ipart[f], dtg[f], dIw, Gr, Gt,
                                          n_emit, n_gate);
                         }
-                        scatter_cells(g_rho, g_u, g_th, tbase[t], im.n2, o[0], o[1 * C], Gr, Gt, ss.dlnth[1]);
+                        scatter_cells(g_rho, g_u, g_th, tbase[ta], im.n2, o[0], o[1 * C], Gr, Gt, ss.dlnth[1]);
                     }
-                    if (--qn > 0) qh = (unsigned)nxt[t];
+                    ring.pop(nxt, ta);
                 }
             }
             __syncwarp();
         }
-        if (mode == 2 && qn == 0) {
+        if (mode == 2 && ring.empty()) {
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 if (isfinite(dIw[q])) acc[q] += dIw[q];

@@ -21,11 +21,12 @@ def eng():
 
 
 def _grid(eng, dump):
-    """Upload each dump once per engine (the context holds 16 grid slots)."""
+    """Upload each dump once per engine (the context holds 16 grid slots).
+    The cache holds the dump itself, so its id cannot be reused by another."""
     cache = eng.__dict__.setdefault("_test_grids", {})
     if id(dump) not in cache:
-        cache[id(dump)] = eng.upload_grid(dump.geom, dump.prims)
-    return cache[id(dump)]
+        cache[id(dump)] = (dump, eng.upload_grid(dump.geom, dump.prims))
+    return cache[id(dump)][1]
 
 
 @pytest.fixture(scope="module")

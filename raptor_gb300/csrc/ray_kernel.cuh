@@ -456,7 +456,9 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
 // for its outstanding tickets before it writes its pixel; a partial batch is
 // evaluated when such a ray has waited kPoolDrainWait steps or no lane of the
 // warp is stepping.  Per ray the operations and their order are those of
-// ray_kernel, so the images are bit-identical.
+// ray_kernel: the images agree bit for bit wherever the compiler contracts
+// the two kernels' arithmetic alike (the 1-, 2- and 4-frequency
+// instantiations), and to rounding elsewhere.
 constexpr int kPoolCap = 64;  // ring entries per warp: up to 31 waiting + 32 appended in one step
 // at least this many 128-thread blocks per SM: 2 gives 192 registers a
 // thread and 8 warps, 1 % faster at 1024x1024 than 3 (168 registers, 12

@@ -61,9 +61,10 @@ typedef struct raptor_gpu_options {
                             (device, batch signature) and reuse the result */
     int use_graph;       /* 1: replay a render through a captured CUDA graph when the batch
                             signature repeats */
-    int no_sample_pool;  /* FP64 form: 1 = each lane evaluates its own ray's samples in place;
-                            0 (default) = a warp evaluates them 32 at a time from a shared-memory
-                            pool.  Both give bit-identical images. */
+    int no_sample_pool;  /* FP64 form and FP64 adjoint: 1 = each lane evaluates its own ray's
+                            samples in place; 0 (default) = a warp evaluates them 32 at a time
+                            from a shared-memory pool.  The same arithmetic per ray: the images
+                            agree bit for bit or to rounding. */
     int reserved[7];
 } raptor_gpu_options;
 

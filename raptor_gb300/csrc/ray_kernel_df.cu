@@ -81,7 +81,8 @@ __device__ __forceinline__ int df_trunc(DF t) {
 }
 
 // One transfer sample: Xtoij (grmhd.c:46-71) from the DF position, the
-// metric in FP32, the rest as the mixed form's FP32 sample.
+// metric in FP32 from the point's leading parts, the rest as the mixed
+// form's FP32 sample.
 template <int NF>
 __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], const MksPointT<DF>& p, float adl,
                                              float (&tau)[NF], float (&tauc)[NF], float (&I)[NF],
@@ -104,9 +105,6 @@ __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], 
                                    Ic);
 }
 
-// 4 blocks of 128 (16 warps) per SM: the DF arithmetic is FP32-latency bound,
-// and 16 warps at 128 registers (a few hundred bytes of spills) ran 1.4x
-// faster than 8 warps at 196 registers without spills (1024x1024 image).
 // Per-step record of the traced ray (the layout of trace_record in
 // ray_kernel.cuh), the DF state written as doubles.
 template <int NF>
@@ -125,12 +123,92 @@ __device__ __forceinline__ void trace_record_df(const TraceSpec& tr, const RaySt
     r[15] = 0.0;
 }
 
-// 3 blocks of 128 per SM: 168 registers a thread and no spills (4 blocks
-// held 128 registers and spilled; 2 % slower at 1024x1024)
+// A lane takes ray rid: camera set-up in FP64 (once per ray), then the DF state.
+template <int NF>
+__device__ __forceinline__ const DevImage* start_ray_df(const DevImage* __restrict__ imgs, int n_imgs, long long rid,
+                                                        RayStateDF<NF>& s) {
+    s.img = find_image(imgs, n_imgs, rid);
+    const DevImage* im = imgs + s.img;
+    s.pix = (int)(rid - im->ray_begin);
+    s.rid = rid;
+    double y0[8], beta;
+    init_photon(*im, camera_of(*im), s.pix % im->width, s.pix / im->width, y0, beta);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s.y[i] = df_const(y0[i]);
+    s.bsign = (beta < 0.0) ? -1 : ((beta > 0.0) ? 1 : 0);
+    mks_point(s.y[1], s.y[2], im->geo_df, s.p);
+    s.steps = 0;
+    s.turns = 0;
+    s.stop = 0;
+    s.thdot_prev = 0.0f;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
+    }
+    return im;
+}
+
+// One step of integrate_geodesic's loop (integrator.c:228-285), as
+// advance_ray in ray_kernel.cuh: -1 the while-condition ended the ray, 0
+// stepped outside the sampling region, 1 inside it, 3 escaped outward.
+template <int NF>
+__device__ __forceinline__ int advance_ray_df(const DevImage& im, RayStateDF<NF>& s, DF& dl) {
+    const DF r = s.p.rp;
+    if (!(r < df_const(kCutoffOuter) && r > im.cutoff_inner_df && s.steps < (int)kMaxSteps && !s.stop)) return -1;
+    // theta turning points (integrator.c:243-247)
+    const float th = s.y[6].hi;
+    if (((s.thdot_prev < 0.0f && th > 0.0f) || (s.thdot_prev > 0.0f && th < 0.0f)) && s.steps > 2) s.turns += 1;
+    s.thdot_prev = th;
+    if ((s.bsign < 0 && s.turns > kMaxOrder) || (s.bsign > 0 && s.turns > kMaxOrder + 1)) s.stop = 1;
+    dl = step_size_df(im, s.y);
+    if (im.integrator == 2) rk2_step(im.geo_df, s.y, s.p, dl);
+    else rk4_step_rolled(im.geo_df, s.y, s.p, dl);
+    s.steps += 1;
+    if (s.y[1] > im.stopx1_df && s.y[5].hi < 0.0f) return 3;
+    if (s.y[1] < im.stopx1_df && s.y[1] > im.startx1_df && s.y[2] > im.startx2_df && s.y[2] < im.stopx2_df) return 1;
+    return 0;
+}
+
+// The ray has ended: write I nu^3 (core.c:121-137) and the ray's statistics,
+// with the k.k drift in FP64 at the final state.
+template <int NF>
+__device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayStateDF<NF>& s, double* __restrict__ out,
+                                              RayCounters& c) {
+    double* o = out + im.out_offset + (long long)s.pix * im.nfreq;
+    const PixelScale ps = pixel_scale(im, s.pix % im.width);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        if (f >= im.nfreq) break;
+        o[f] = scale_output(im, ps, ((double)s.If[f] + (double)s.Ic[f]) * kE2C, f);
+    }
+    c.steps += (unsigned long long)s.steps;
+    c.rays += 1;
+    if ((double)s.steps >= kMaxSteps) ++c.cap;
+    if (!(s.p.rp.hi == s.p.rp.hi) || !isfinite(s.y[5].hi)) ++c.nan;
+    c.max_steps = max(c.max_steps, (unsigned long long)s.steps);
+    double yd[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) yd[i] = df_to_double(s.y[i]);
+    MksPoint pd;
+    mks_point(yd[1], yd[2], im.geo, pd);
+    const double kk = null_drift(pd, im.geo, yd);
+    if (kk == kk) c.kk_max = fmax(c.kk_max, kk);
+}
+
+// 3 blocks of 128 per SM: 168 registers a thread and no spills.  The DF
+// arithmetic wants warps to hide FP32 latency, but 4 blocks (128 registers,
+// a few hundred bytes of spills) were 2 % slower at 1024x1024, and 2 blocks
+// (8 warps at 196 registers) ran 1.4x slower.
 #ifndef RAPTOR_RAY_DF_MIN_BLOCKS
 #define RAPTOR_RAY_DF_MIN_BLOCKS 3
 #endif
 
+// Each lane samples its own ray in place.  A sample pool as in the FP64
+// form (ray_kernel_pool) gave the same images but ran 9 % slower here
+// (1024x1024: 122 against 112 ms): the FP32 sample is a quarter of this
+// kernel's time, and the ring's code (and a sample split into its
+// order-free and ordered halves) adds to an instruction stream that already
+// stalls on fetch.
 template <int NF>
 __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
     ray_kernel_df(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
@@ -140,10 +218,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
     RayStateDF<NF> s;
     bool active = false, live = true;
     const DevImage* im = imgs;
-    unsigned long long n_steps = 0, n_rt_calls = 0, n_rt_samples = 0, n_rays = 0, n_cap = 0, n_nan = 0;
-    unsigned long long max_steps = 0;
-    double kk_max = 0.0;
-    const DF cut_outer = df_const(kCutoffOuter);
+    RayCounters c;
 
     while (true) {
         const unsigned need = __ballot_sync(kFull, !active && live);
@@ -155,25 +230,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
             if (!active && live) {
                 const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
                 if (rid < ray_end) {
-                    s.img = find_image(imgs, n_imgs, rid);
-                    im = imgs + s.img;
-                    s.pix = (int)(rid - im->ray_begin);
-                    s.rid = rid;
-                    // camera set-up in FP64 (once per ray), then the DF state
-                    double y0[8], beta;
-                    init_photon(*im, camera_of(*im), s.pix % im->width, s.pix / im->width, y0, beta);
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) s.y[i] = df_const(y0[i]);
-                    s.bsign = (beta < 0.0) ? -1 : ((beta > 0.0) ? 1 : 0);
-                    mks_point(s.y[1], s.y[2], im->geo_df, s.p);
-                    s.steps = 0;
-                    s.turns = 0;
-                    s.stop = 0;
-                    s.thdot_prev = 0.0f;
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) {
-                        s.tf[f] = 0.f; s.tc[f] = 0.f; s.If[f] = 0.f; s.Ic[f] = 0.f;
-                    }
+                    im = start_ray_df(imgs, n_imgs, rid, s);
                     active = true;
                     if (tr.out && rid == tr.ray) trace_record_df<NF>(tr, s, 0.0, 0);
                 } else {
@@ -184,81 +241,25 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
         if (!__any_sync(kFull, active)) break;
         if (active) {
             for (int it = 0; it < refill_interval; ++it) {
-                // while-condition of integrator.c:228-229
-                const DF r = s.p.rp;
-                bool done = !(r < cut_outer && r > im->cutoff_inner_df && s.steps < (int)kMaxSteps && !s.stop);
-                if (!done) {
-                    // theta turning points (integrator.c:243-247)
-                    const float th = s.y[6].hi;
-                    if (((s.thdot_prev < 0.0f && th > 0.0f) || (s.thdot_prev > 0.0f && th < 0.0f)) && s.steps > 2)
-                        s.turns += 1;
-                    s.thdot_prev = th;
-                    if ((s.bsign < 0 && s.turns > kMaxOrder) || (s.bsign > 0 && s.turns > kMaxOrder + 1)) s.stop = 1;
-                    const DF dl = step_size_df(*im, s.y);
-                    if (im->integrator == 2) rk2_step(im->geo_df, s.y, s.p, dl);
-                    else rk4_step_rolled(im->geo_df, s.y, s.p, dl);
-                    s.steps += 1;
-                    int event = 0;
-                    if (s.y[1] > im->stopx1_df && s.y[5].hi < 0.0f) {
-                        done = true;  // escaped outward (integrator.c:271-272)
-                        event = 3;
-                    } else if (s.y[1] < im->stopx1_df && s.y[1] > im->startx1_df && s.y[2] > im->startx2_df &&
-                               s.y[2] < im->stopx2_df) {
-                        ++n_rt_calls;
-                        const bool sampled = rt_sample_df<NF>(*im, s.y, s.p, -dl.hi, s.tf, s.tc, s.If, s.Ic);
-                        n_rt_samples += sampled ? 1 : 0;
-                        event = sampled ? 2 : 1;
-                    }
-                    if (tr.out && s.rid == tr.ray) trace_record_df<NF>(tr, s, df_to_double(dl), event);
+                DF dl = df_const(0.0);
+                int event = advance_ray_df(*im, s, dl);
+                const bool done = event == -1 || event == 3;
+                if (event == 1) {
+                    ++c.rt_calls;
+                    const bool sampled = rt_sample_df<NF>(*im, s.y, s.p, -dl.hi, s.tf, s.tc, s.If, s.Ic);
+                    c.rt_samples += sampled ? 1 : 0;
+                    event = sampled ? 2 : 1;
                 }
+                if (event != -1 && tr.out && s.rid == tr.ray) trace_record_df<NF>(tr, s, df_to_double(dl), event);
                 if (done) {
-                    double* o = out + im->out_offset + (long long)s.pix * im->nfreq;
-                    const PixelScale ps = pixel_scale(*im, s.pix % im->width);
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) {
-                        if (f >= im->nfreq) break;
-                        o[f] = scale_output(*im, ps, ((double)s.If[f] + (double)s.Ic[f]) * kE2C, f);
-                    }
-                    n_steps += (unsigned long long)s.steps;
-                    n_rays += 1;
-                    if ((double)s.steps >= kMaxSteps) ++n_cap;
-                    if (!(s.p.rp.hi == s.p.rp.hi) || !isfinite(s.y[5].hi)) ++n_nan;
-                    max_steps = max(max_steps, (unsigned long long)s.steps);
-                    // k.k drift in FP64 at the final state (once per ray)
-                    double yd[8];
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) yd[i] = df_to_double(s.y[i]);
-                    MksPoint pd;
-                    mks_point(yd[1], yd[2], im->geo, pd);
-                    const double kk = null_drift(pd, im->geo, yd);
-                    if (kk == kk) kk_max = fmax(kk_max, kk);
+                    finish_ray_df(*im, s, out, c);
                     active = false;
                     break;
                 }
             }
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        n_steps += __shfl_xor_sync(kFull, n_steps, o);
-        n_rt_calls += __shfl_xor_sync(kFull, n_rt_calls, o);
-        n_rt_samples += __shfl_xor_sync(kFull, n_rt_samples, o);
-        n_rays += __shfl_xor_sync(kFull, n_rays, o);
-        n_cap += __shfl_xor_sync(kFull, n_cap, o);
-        n_nan += __shfl_xor_sync(kFull, n_nan, o);
-        max_steps = max(max_steps, __shfl_xor_sync(kFull, max_steps, o));
-        kk_max = fmax(kk_max, __shfl_xor_sync(kFull, kk_max, o));
-    }
-    if (lane == 0) {
-        atomicAdd(&counters[kCtrSteps], n_steps);
-        atomicAdd(&counters[kCtrRtCalls], n_rt_calls);
-        atomicAdd(&counters[kCtrRtSamples], n_rt_samples);
-        atomicAdd(&counters[kCtrRays], n_rays);
-        atomicAdd(&counters[kCtrStepCap], n_cap);
-        atomicAdd(&counters[kCtrNonFinite], n_nan);
-        atomicMax(&counters[kCtrMaxSteps], max_steps);
-        atomicMax(&counters[kCtrKkMax], (unsigned long long)__double_as_longlong(kk_max));
-    }
+    c.publish(counters, lane);
 }
 
 template <int NF>

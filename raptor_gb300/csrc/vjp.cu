@@ -44,55 +44,15 @@ using namespace raptor;
 
 namespace {
 
-// The sample's dual directions: the inclination (through the geodesic), ln
-// Theta_e and ln B.  Everything else reaches a sample through these and n_e,
-// and n_e is a pure prefactor of j and a, so dS/d ln n_e = S and
-// d delta/d ln n_e = delta:
-//   rho_s:  n_e proportional to rho_s, and ln Theta_e by d ln Theta_e/d rho_s;
-//   u_s, R_high, R_low:  ln Theta_e only (the R-beta model, thetae_log_derivs);
-//   M_unit: n_e proportional to M_unit, B to sqrt(M_unit).
-// Three tangents instead of one per parameter: the dual sample costs about
-// half of a six-direction one.
+// The FP64 adjoint's sample: value and the three directions of
+// vjp_common.cuh (inclination, ln Theta_e, ln B) in FP64.
 using D3 = Dual<3>;
-constexpr int kSIncl = 0, kSLnTh = 1, kSLnB = 2;
+using SampleScalars = SampleScalarsT<double>;
 
 __device__ __forceinline__ D3 lift(const D1& a) {
     D3 r(a.v);
     r.d[kSIncl] = a.d[0];
     return r;
-}
-
-// The scalar factors that map a sample's (value, ln Theta_e) terms onto the
-// per-cell and scalar parameters.
-struct SampleScalars {
-    double irho;        // 1 / rho_s
-    double dlnth[4];    // d ln Theta_e / d(rho_s, u_s, R_high, R_low)
-};
-
-// d ln Theta_e / d(rho_s, u_s, R_high, R_low) of the R-beta electron
-// temperature (raptor_harm_model.c:262-276, fluid_from_prims):
-//   Theta_e = (u / rho) (gam(t) - 1) (m_p / m_e) / (1 + t),
-//   t = (R_high b^2 + R_low) / (1 + b^2),  b = (1/3) u / (Bsq / 2),
-//   gam(t) = ((1 + 2/3 (t + 1) / (t + 2)) + 4/3) / 2.
-// Zero where Theta_e was clamped (u / rho ... < 0).
-__device__ __forceinline__ void thetae_log_derivs(double rho, double uu, double bsq, double Rh, double Rl,
-                                                  double (&out)[4]) {
-    const double tiny = 1.e-20;
-    const double beta = uu * (4.0 / 3.0 - 1.0) / (0.5 * (bsq + tiny));
-    const double b2 = beta * beta;
-    const double i1b2 = 1.0 / (1.0 + b2);
-    const double t = Rh * b2 * i1b2 + Rl * i1b2;
-    const double gam = 0.5 * ((1.0 + 2.0 / 3.0 * (t + 1.0) / (t + 2.0)) + 4.0 / 3.0);
-    if ((uu / rho) * (gam - 1.0) < 0.0) {
-        out[0] = out[1] = out[2] = out[3] = 0.0;
-        return;
-    }
-    const double dlnTU = (1.0 / 3.0) / ((t + 2.0) * (t + 2.0)) / (gam - 1.0) - 1.0 / (1.0 + t);  // d ln(Theta_e u^-1 rho) / dt
-    const double dt_dlnb = 2.0 * b2 * (Rh - Rl) * i1b2 * i1b2;                                  // dt / d ln beta
-    out[0] = -1.0 / rho;
-    out[1] = (1.0 + dlnTU * dt_dlnb) / uu;
-    out[2] = dlnTU * b2 * i1b2;
-    out[3] = dlnTU * i1b2;
 }
 
 // The frequency-independent part of one transfer sample, as value + three
@@ -196,14 +156,6 @@ __device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommo
     return !(ex < CUDART_INF) ? 2 : 0;
 }
 
-// A term's derivatives along the four scalar parameters (inclination,
-// ln M_unit, R_high, R_low) from its value and three tangents.
-__device__ __forceinline__ double scalar_tangent(const D3& x, const SampleScalars& ss, int q) {
-    if (q == 0) return x.d[kSIncl];
-    if (q == 1) return x.v + 0.5 * x.d[kSLnB];
-    return x.d[kSLnTh] * ss.dlnth[q];  // q = 2, 3: R_high, R_low
-}
-
 // One frequency's terms of a sample, consumed in step order: tau, the part
 // of I accumulated so far, d tau / d(scalars), dL/dI dI/d(scalars) (dIw), and
 // the sample's sums Gr, Gt of w (g e^-tau dS/dx - (I - I_<k) ddelta/dx) for
@@ -222,10 +174,7 @@ __device__ __forceinline__ void consume_term(int kind, const D3& S, const D3& dt
         const double suffix = Itot - Ipart;
         const double eS = gate ? e : 0.0;
         if (suffix != 0.0 || gate) {
-            // d/d rho_s = (d/d ln n_e) / rho_s + (d ln Theta_e / d rho_s) d/d ln Theta_e
-            const double S_rho = S.v * ss.irho + S.d[kSLnTh] * ss.dlnth[0];
-            const double dt_rho = dt.v * ss.irho + dt.d[kSLnTh] * ss.dlnth[0];
-            Gr += w * (eS * S_rho - suffix * dt_rho);
+            Gr += w * (eS * rho_tangent(S, ss) - suffix * rho_tangent(dt, ss));
             Gt += w * (eS * S.d[kSLnTh] - suffix * dt.d[kSLnTh]);
         }
         if (gate) {

@@ -1,6 +1,7 @@
 // Pieces shared by the two adjoint kernels (vjp.cu: FP64; vjp_df.cu:
-// mixed-DF): the inclination dual, the tangent directions of the mixed-DF
-// adjoint's six-direction sample, and the launch interface.
+// mixed-DF): the inclination dual, the sample's three dual directions and
+// the scalar factors that map them onto the parameters, and the launch
+// interface.
 #pragma once
 #include "dual.cuh"
 #include "ray_kernel.cuh"
@@ -8,11 +9,67 @@
 namespace raptor {
 
 using D1 = Dual<1>;
-// tangent directions of the mixed-DF adjoint's sample: 0 inclination, 1 rho_s,
-// 2 ln Theta_e (u_s), 3 ln M_unit, 4 R_high, 5 R_low
-constexpr int kDirIncl = 0, kDirRho = 1, kDirU = 2, kDirLnM = 3, kDirRh = 4, kDirRl = 5;
-// the four scalar parameters' directions: 0 -> incl, 1 -> ln M, 2 -> R_high, 3 -> R_low
-__host__ __device__ __forceinline__ int gdir(int q) { return q == 0 ? kDirIncl : q + 2; }
+
+// The sample's dual directions: the inclination (through the geodesic), ln
+// Theta_e and ln B.  Everything else reaches a sample through these and n_e,
+// and n_e is a pure prefactor of j and a, so dS/d ln n_e = S and
+// d delta/d ln n_e = delta:
+//   rho_s:  n_e proportional to rho_s, and ln Theta_e by d ln Theta_e/d rho_s;
+//   u_s, R_high, R_low:  ln Theta_e only (the R-beta model, thetae_log_derivs);
+//   M_unit: n_e proportional to M_unit, B to sqrt(M_unit).
+// Three tangents instead of one per parameter.
+constexpr int kSIncl = 0, kSLnTh = 1, kSLnB = 2;
+
+// The scalar factors that map a sample's (value, ln Theta_e) terms onto the
+// per-cell and scalar parameters.
+template <class T>
+struct SampleScalarsT {
+    T irho;      // 1 / rho_s
+    T dlnth[4];  // d ln Theta_e / d(rho_s, u_s, R_high, R_low)
+};
+
+// d ln Theta_e / d(rho_s, u_s, R_high, R_low) of the R-beta electron
+// temperature (raptor_harm_model.c:262-276, fluid_from_prims):
+//   Theta_e = (u / rho) (gam(t) - 1) (m_p / m_e) / (1 + t),
+//   t = (R_high b^2 + R_low) / (1 + b^2),  b = (1/3) u / (Bsq / 2),
+//   gam(t) = ((1 + 2/3 (t + 1) / (t + 2)) + 4/3) / 2.
+// Zero where Theta_e was clamped (u / rho ... < 0).
+template <class T>
+__device__ __forceinline__ void thetae_log_derivs(T rho, T uu, T bsq, T Rh, T Rl, T (&out)[4]) {
+    const T tiny = (T)1.e-20;
+    const T beta = uu * (T(4) / T(3) - T(1)) / (T(0.5) * (bsq + tiny));
+    const T b2 = beta * beta;
+    const T i1b2 = T(1) / (T(1) + b2);
+    const T t = Rh * b2 * i1b2 + Rl * i1b2;
+    const T gam = T(0.5) * ((T(1) + T(2) / T(3) * (t + T(1)) / (t + T(2))) + T(4) / T(3));
+    if ((uu / rho) * (gam - T(1)) < T(0)) {
+        out[0] = out[1] = out[2] = out[3] = T(0);
+        return;
+    }
+    // d ln((gam - 1) / (1 + t)) / dt and dt / d ln beta
+    const T dlnTU = (T(1) / T(3)) / ((t + T(2)) * (t + T(2))) / (gam - T(1)) - T(1) / (T(1) + t);
+    const T dt_dlnb = T(2) * b2 * (Rh - Rl) * i1b2 * i1b2;
+    out[0] = -T(1) / rho;
+    out[1] = (T(1) + dlnTU * dt_dlnb) / uu;
+    out[2] = dlnTU * b2 * i1b2;
+    out[3] = dlnTU * i1b2;
+}
+
+// A term's derivative along scalar parameter q (0 inclination, 1 ln M_unit,
+// 2 R_high, 3 R_low) from its value and three tangents.
+template <class Dl, class T>
+__device__ __forceinline__ T scalar_tangent(const Dl& x, const SampleScalarsT<T>& ss, int q) {
+    if (q == 0) return x.d[kSIncl];
+    if (q == 1) return x.v + T(0.5) * x.d[kSLnB];
+    return x.d[kSLnTh] * ss.dlnth[q];  // q = 2, 3: R_high, R_low
+}
+
+// A term's derivative along rho_s: (d/d ln n_e) / rho_s + (d ln Theta_e /
+// d rho_s) d/d ln Theta_e.
+template <class Dl, class T>
+__device__ __forceinline__ T rho_tangent(const Dl& x, const SampleScalarsT<T>& ss) {
+    return x.v * ss.irho + x.d[kSLnTh] * ss.dlnth[0];
+}
 
 constexpr int kVjpBlock = 128;
 constexpr int kVjpRefill = 8;  // geodesic steps between lane refills of the mixed-DF adjoint

@@ -8,9 +8,10 @@
 //    float>; the tangent needs ~1e-5, not the path's 1e-14) through the same
 //    templated code as every other form (step size, rolled RK4, point
 //    transcendentals, Christoffels), so the path is ray_kernel_df's;
-//  * the sample as Dual<6, float>, the FP32 transfer of the mixed forms
+//  * the sample as Dual<3, float>, the FP32 transfer of the mixed forms
 //    (rt_sample_fp32_core: emissivity without e2_c, absorptivity through
-//    expm1) with its six tangents, accumulated per ray in FP32.
+//    expm1) along the three directions of vjp_common.cuh (inclination, ln
+//    Theta_e, ln B), accumulated per ray in FP32.
 // FP64 is used once per ray (camera set-up, the forward image's I, the
 // scalar gradients) and for the per-cell atomics.
 #include <cuda_runtime.h>
@@ -24,7 +25,8 @@ namespace {
 
 using DD1 = Dual<1, DF, float>;  // DF value, FP32 inclination tangent
 using F1 = Dual<1, float>;
-using F6 = Dual<6, float>;
+using F3 = Dual<3, float>;
+using SampleScalarsF = SampleScalarsT<float>;
 
 // mks_point for the dual DF state: the rolled form (kerr_mks.cuh)
 __device__ __forceinline__ void mks_point(DD1 x1, DD1 x2, const GeoDF& g, MksPointT<DD1>& p) {
@@ -36,16 +38,16 @@ __device__ __forceinline__ F1 to_f1(const DD1& x) {
     r.d[0] = x.d[0];
     return r;
 }
-__device__ __forceinline__ F6 liftf(const F1& a) {
-    F6 r(a.v);
-    r.d[kDirIncl] = a.d[0];
+__device__ __forceinline__ F3 liftf(const F1& a) {
+    F3 r(a.v);
+    r.d[kSIncl] = a.d[0];
     return r;
 }
 
 // The sample's metric (metric.c:94-137, 207-231) in FP32 with its
 // inclination tangent, from the point's leading parts (as metric_f32 in
 // ray_kernel_df.cu).
-__device__ __forceinline__ MetricT<F6> metric_f6(const MksPointT<DD1>& pd, const GeoDF& gd) {
+__device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<DD1>& pd, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
     const F1 r = to_f1(pd.r), s = to_f1(pd.s), c = to_f1(pd.c), irho2 = to_f1(pd.iS);
     const F1 c2x = to_f1(pd.c2x), irp = to_f1(pd.irp), ithp = to_f1(pd.ithp), isn = to_f1(pd.isn);
@@ -56,7 +58,7 @@ __device__ __forceinline__ MetricT<F6> metric_f6(const MksPointT<DD1>& pd, const
     const F1 z = 2.0f * (r * irho2);
     const F1 ir = (R0 == 0.0f) ? irp : F1(1.0f) / r;
     const F1 opz = 1.0f + z;
-    MetricT<F6> g;
+    MetricT<F3> g;
     g.d00 = liftf(-1.0f + z);
     g.d01 = liftf(z * rfac);
     g.d03 = liftf((-a) * (z * s2));
@@ -83,10 +85,10 @@ __device__ __forceinline__ int df_trunc_i(DF t) {
     return i;
 }
 
-// The frequency-independent part of one FP32 sample with six tangents.
+// The frequency-independent part of one FP32 sample with three tangents.
 struct SampleCommonF {
-    F6 kU, nus, jpre, xpre, adl;
-    float dlnth_du;  // d ln Theta_e / d u_s
+    F3 kU, nus, jpre, xpre, adl;
+    SampleScalarsF ss;
     bool emits;
     int base;        // first of the four cells
     float d1, d2;    // bilinear offsets
@@ -94,57 +96,54 @@ struct SampleCommonF {
 
 __device__ bool sample_common_f(const DevImage& im, const DD1 y[8], const MksPointT<DD1>& pd, const DD1& adl,
                                 SampleCommonF& out) {
-    const MetricT<F6> g = metric_f6(pd, im.geo_df);
+    const MetricT<F3> g = metric_f3(pd, im.geo_df);
     // Xtoij (grmhd.c:46-71) from the DF position; the offsets carry the
     // inclination tangent unless clamped
     const DF t1 = (y[1].v - im.startx1_df) * im.idx1_df - 0.5;
     const DF t2 = (y[2].v - im.startx2_df) * im.idx2_df - 0.5;
     int i = df_trunc_i(t1), j = df_trunc_i(t2);
-    F6 d1(0.0f), d2(0.0f);
+    F3 d1(0.0f), d2(0.0f);
     if (i < 0) i = 0;
-    else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F6(1.0f); }
-    else { d1 = F6(add_f(t1, (float)-i).hi); d1.d[kDirIncl] = y[1].d[0] * im.idx1_df.hi; }
+    else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F3(1.0f); }
+    else { d1 = F3(add_f(t1, (float)-i).hi); d1.d[kSIncl] = y[1].d[0] * im.idx1_df.hi; }
     if (j < 0) j = 0;
-    else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F6(1.0f); }
-    else { d2 = F6(add_f(t2, (float)-j).hi); d2.d[kDirIncl] = y[2].d[0] * im.idx2_df.hi; }
+    else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F3(1.0f); }
+    else { d2 = F3(add_f(t2, (float)-j).hi); d2.d[kSIncl] = y[2].d[0] * im.idx2_df.hi; }
     out.base = i * im.n2 + j;
     out.d1 = d1.v;
     out.d2 = d2.v;
-    const F6 c0 = (1.0f - d1) * (1.0f - d2), c1 = (1.0f - d1) * d2, c2 = d1 * (1.0f - d2), c3 = d1 * d2;
+    const F3 c0 = (1.0f - d1) * (1.0f - d2), c1 = (1.0f - d1) * d2, c2 = d1 * (1.0f - d2), c3 = d1 * d2;
     float a[8], b[8], e[8], f[8];
     const float* cp = im.cells32 + (size_t)out.base * 8;
     load_cell(cp, a);
     load_cell(cp + 8, b);
     load_cell(cp + (size_t)im.n2 * 8, e);
     load_cell(cp + (size_t)im.n2 * 8 + 8, f);
-    F6 v[8];
+    F3 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = c0 * a[q] + c1 * b[q] + c2 * e[q] + c3 * f[q];
-    v[0].d[kDirRho] += 1.0f;  // rho_s and u_s as independent variables
-    v[1].d[kDirU] += 1.0f;
 
-    F6 Ne_unit(im.ne_unit_f), B_unit(im.b_unit_f), r_high(im.r_high_f), r_low(im.r_low_f);
-    Ne_unit.d[kDirLnM] = im.ne_unit_f;
-    B_unit.d[kDirLnM] = 0.5f * im.b_unit_f;
-    r_high.d[kDirRh] = 1.0f;
-    r_low.d[kDirRl] = 1.0f;
-    Fluid<F6> fl;
-    if (!fluid_from_prims(v, g, Ne_unit, B_unit, r_high, r_low, fl)) return false;
-    out.dlnth_du = fl.thetae.v > 0.0f ? fl.thetae.d[kDirU] / fl.thetae.v : 0.0f;
-    fl.thetae.d[kDirU] = fl.thetae.v;
+    const F3 B_unit(im.b_unit_f);
+    Fluid<F3> fl;
+    if (!fluid_from_prims(v, g, F3(im.ne_unit_f), B_unit, F3(im.r_high_f), F3(im.r_low_f), fl)) return false;
+    out.ss.irho = 1.0f / v[0].v;
+    thetae_log_derivs(v[0].v, v[1].v, fl.bsq.v, im.r_high_f, im.r_low_f, out.ss.dlnth);
+    // |b| in code units for the pitch angle, which M_unit does not move:
+    // formed before B takes its ln B direction
+    const F3 Bcode = fl.B / B_unit;
+    fl.thetae.d[kSLnTh] = fl.thetae.v;
+    fl.B.d[kSLnB] = fl.B.v - 1.e-20f;  // B = sqrt(Bsq) B_unit + tiny: the part that scales
 
-    const F6 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
-    F6 kd[4];
+    const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
+    F3 kd[4];
     lowerT(g, k, kd);
-    const F6* U = fl.ucon;
-    const F6* Bc = fl.bcon;
+    const F3* U = fl.ucon;
+    const F3* Bc = fl.bcon;
     out.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    // |b| in code units: B / B_unit with B_unit's own M_unit tangent (B is
-    // proportional to B_unit, so the pitch angle does not depend on M_unit)
-    F6 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * (fl.B / B_unit));
-    if (fabsf(pitch.v) > 1.0f) pitch = F6(pitch.v > 0.0f ? 1.0f : -1.0f);
-    const F6 sth = sqrt(1.0f - pitch * pitch);
-    const F6 nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
+    F3 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * Bcode);
+    if (fabsf(pitch.v) > 1.0f) pitch = F3(pitch.v > 0.0f ? 1.0f : -1.0f);
+    const F3 sth = sqrt(1.0f - pitch * pitch);
+    const F3 nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
     out.nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
     out.emits = (fabsf(sth.v) >= 1.e-10f) && (fl.thetae.v > 1e-4f);
     out.jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
@@ -155,16 +154,16 @@ __device__ bool sample_common_f(const DevImage& im, const DD1 y[8], const MksPoi
 
 // S and delta at frequency fi (rt_sample_fp32_core's arithmetic, emissivity
 // without e2_c); false if the frequency does not emit.
-__device__ __forceinline__ bool sample_freq_f(const DevImage& im, const SampleCommonF& sc, int fi, F6& S, F6& dtau) {
-    F6 nup = -sc.kU * im.freq_f[fi];
-    if (nup.v <= 0.0f) nup = F6(1.0f);
+__device__ __forceinline__ bool sample_freq_f(const DevImage& im, const SampleCommonF& sc, int fi, F3& S, F3& dtau) {
+    F3 nup = -sc.kU * im.freq_f[fi];
+    if (nup.v <= 0.0f) nup = F3(1.0f);
     if (!(sc.emits && nup.v != 1.0f)) return false;
-    const F6 dlf = sc.adl * im.rg_over_nu_f[fi];
-    const F6 X = nup / sc.nus;
-    const F6 cb = cbrt(X);
-    const F6 sq = sqrt(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
-    const F6 jh = sc.jpre * (sq * sq) * exp(-cb);
-    const F6 q = (jh / nup) / nup;
+    const F3 dlf = sc.adl * im.rg_over_nu_f[fi];
+    const F3 X = nup / sc.nus;
+    const F3 cb = cbrt(X);
+    const F3 sq = sqrt(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
+    const F3 jh = sc.jpre * (sq * sq) * exp(-cb);
+    const F3 q = (jh / nup) / nup;
     dtau = q * expm1(sc.xpre * nup) * (float)(kE2CH * kC * kC * 0.5) * dlf;
     S = q * dlf;
     return true;
@@ -309,27 +308,28 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
 #pragma unroll 1
                         for (int f = 0; f < NF; ++f) {
                             if (f >= im.nfreq) break;
-                            F6 S, dt;
+                            F3 S, dt;
                             if (!sample_freq_f(im, sc, f, S, dt)) continue;
                             ++n_emit;
                             s.tau[f] += dt.v;
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) s.dtg[f][q] += dt.d[gdir(q)];
+                            for (int q = 0; q < 4; ++q) s.dtg[f][q] += scalar_tangent(dt, sc.ss, q);
                             const float e = expf(-s.tau[f]);
                             const bool gate = s.tau[f] < 6.9077553f && !(s.tau[f] < 0.0f);
                             const float suffix = s.Itot[f] - s.Ipart[f];
                             const float eS = gate ? e : 0.0f;
-                            Gr += s.w[f] * (eS * S.d[kDirRho] - suffix * dt.d[kDirRho]);
-                            Gt += s.w[f] * (eS * S.d[kDirU] - suffix * dt.d[kDirU]);
+                            Gr += s.w[f] * (eS * rho_tangent(S, sc.ss) - suffix * rho_tangent(dt, sc.ss));
+                            Gt += s.w[f] * (eS * S.d[kSLnTh] - suffix * dt.d[kSLnTh]);
                             if (gate) {
                                 ++n_gate;
                                 const float we = s.w[f] * e;
 #pragma unroll
-                                for (int q = 0; q < 4; ++q) s.dIw[q] += we * (S.d[gdir(q)] - S.v * s.dtg[f][q]);
+                                for (int q = 0; q < 4; ++q)
+                                    s.dIw[q] += we * (scalar_tangent(S, sc.ss, q) - S.v * s.dtg[f][q]);
                                 s.Ipart[f] += S.v * e;
                             }
                         }
-                        const float Gu = Gt * sc.dlnth_du;
+                        const float Gu = Gt * sc.ss.dlnth[1];
                         if ((Gr != 0.0f || Gt != 0.0f) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
                             const float w0 = (1.0f - sc.d1) * (1.0f - sc.d2), w1 = (1.0f - sc.d1) * sc.d2;
                             const float w2 = sc.d1 * (1.0f - sc.d2), w3 = sc.d1 * sc.d2;

@@ -161,21 +161,25 @@ __device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g
     const R X0 = q00 - as2 * q03;
     const R X1 = q01 - as2 * q13;
     const R H = q00 + rp * (q01 + rp * q11);  // q00 + r' q01 + r'^2 q11
-    const R Wp = a2 * r * s2th * iS2;         // G0_02 = -Wp theta'
+    const R iS2thp = iS2 * thp;
+    const R a2rs = a2 * r * s2th;
+    const R Wp = a2rs * iS2;                  // G0_02 = -Wp theta'
+    const R WpT = a2rs * iS2thp;              // Wp theta'
+    const R riSthp2 = riS * thp2;
     const R Cs2 = C * s2;
     const R Dlirp = Dl * irp;
+    const R Rr2 = two_r * r2a2;               // 2 r (r^2 + a^2)
     const R G1_12 = -a2 * sc * iS * thp;
-    A[0] = -(B * (two_r * X0 + Tr * X1 + 2.0 * (Sg + r) * rp2 * q11) - Wp * thp * (q02 + rp * q12 - as2 * q23) -
-             2.0 * r2 * iS * thp2 * q22 - two_r * Cs2 * q33);
+    A[0] = -(B * (two_r * X0 + Tr * X1 + 2.0 * (Sg + r) * rp2 * q11) - WpT * (q02 + rp * q12 - as2 * q23) -
+             two_r * riSthp2 * q22 - two_r * Cs2 * q33);
     A[1] = -(B * (Dlirp * X0 + (Dl - Sg) * X1 - (2.0 * Sg - Dl) * rp * q11) + q11 + riS * as2 * q13 +
-             G1_12 * q12 - riS * Dlirp * thp2 * q22 - Dlirp * Cs2 * q33);
+             G1_12 * q12 - riSthp2 * Dlirp * q22 - Dlirp * Cs2 * q33);
     const R Z = sc * iS3 * ithp;
-    A[2] = -(Z * (2.0 * a * r * r2a2 * q03 + a * (Aq + Sg * (Sg - Dl)) * rp * q13 -
-                  (Dl * Sg * Sg + 2.0 * r * r2a2 * r2a2) * q33) -
+    A[2] = -(Z * (a * Rr2 * q03 + a * (Aq + Sg * (Sg - Dl)) * rp * q13 - (Dl * Sg * Sg + Rr2 * r2a2) * q33) -
              iS * Wp * ithp * H + riS * rp * q12 + (thpp * ithp + G1_12) * q22);
-    const R K = a * cot * iS2 * thp;  // G3_02 = -2 r K, G3_12 = -(Sigma+2r) r' K
+    const R K = a * cot * iS2thp;  // G3_02 = -2 r K, G3_12 = -(Sigma+2r) r' K
     A[3] = -(a * B * (H - as2 * q03) - K * (two_r * q02 + Tr * q12) + C * (rp * q13 - as2 * q33) -
-             a * riS * thp2 * q22 + (cot + Wp) * thp * q23);
+             a * riSthp2 * q22 + (cot * thp + WpT) * q23);
 }
 
 // Covariant metric (metric.c:94-137); the 7 independent entries.

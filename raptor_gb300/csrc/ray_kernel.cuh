@@ -623,8 +623,10 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
                 y[3] = 0.0;
 #pragma unroll
                 for (int i = 0; i < 4; ++i) y[4 + i] = e[(3 + i) * C];
-                mp.rp = 0.0;  // the metric does not read rp, s2x
+                mp.rp = 0.0;  // the metric does not read rp, s2x, Sg, thp
                 mp.s2x = 0.0;
+                mp.Sg = 0.0;
+                mp.thp = 0.0;
                 mp.r = e[7 * C];
                 mp.s = e[8 * C];
                 mp.c = e[9 * C];

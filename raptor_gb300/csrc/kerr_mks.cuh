@@ -204,8 +204,8 @@ __device__ __forceinline__ void mks_metric(const MksPointT<R>& p, const G& g, Me
     const R s2 = p.s * p.s;
     const R irho2 = p.iS;
     const R rfac = r - g.R0;
-    const R hfac = CUDART_PI * fma(g.one_m_h, p.c2x, 1.0);
-    const R rho2 = fma(r, r, g.a2 * p.c * p.c);
+    const R hfac = p.thp;
+    const R rho2 = p.Sg;
     const R z = 2.0 * r * irho2;
     d.g00 = -1.0 + z;
     d.g01 = z * rfac;

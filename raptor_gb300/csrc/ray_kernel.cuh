@@ -526,9 +526,9 @@ struct TicketRing {
 template <int NF>
 struct PoolLayout {
     // ticket fields, one row of kPoolCap doubles each: 0 |dl|, 1-2 x1 x2,
-    // 3-6 k^mu, 7-14 the point (r, s, c, c2x, iS, irp, ithp, isn); evaluated,
-    // rows 1..NF hold dtau and NF+1..2NF j / nu_p^2
-    static constexpr int kIn = 15;
+    // 3-6 k^mu, 7-15 the point (r, s, c, Sigma, theta', iS, irp, ithp, isn);
+    // evaluated, rows 1..NF hold dtau and NF+1..2NF j / nu_p^2
+    static constexpr int kIn = 16;
     static constexpr int kOut = 1 + 2 * NF;
     static constexpr int kFields = kIn > kOut ? kIn : kOut;
     // + the next-ticket links and image indices (two ints per entry)
@@ -601,11 +601,12 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
             e[7 * C] = s.p.r;
             e[8 * C] = s.p.s;
             e[9 * C] = s.p.c;
-            e[10 * C] = s.p.c2x;
-            e[11 * C] = s.p.iS;
-            e[12 * C] = s.p.irp;
-            e[13 * C] = s.p.ithp;
-            e[14 * C] = s.p.isn;
+            e[10 * C] = s.p.Sg;
+            e[11 * C] = s.p.thp;
+            e[12 * C] = s.p.iS;
+            e[13 * C] = s.p.irp;
+            e[14 * C] = s.p.ithp;
+            e[15 * C] = s.p.isn;
             timg[t] = s.img;
         }
 
@@ -623,18 +624,18 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
                 y[3] = 0.0;
 #pragma unroll
                 for (int i = 0; i < 4; ++i) y[4 + i] = e[(3 + i) * C];
-                mp.rp = 0.0;  // the metric does not read rp, s2x, Sg, thp
+                mp.rp = 0.0;  // the metric does not read rp, s2x, c2x
                 mp.s2x = 0.0;
-                mp.Sg = 0.0;
-                mp.thp = 0.0;
+                mp.c2x = 0.0;
                 mp.r = e[7 * C];
                 mp.s = e[8 * C];
                 mp.c = e[9 * C];
-                mp.c2x = e[10 * C];
-                mp.iS = e[11 * C];
-                mp.irp = e[12 * C];
-                mp.ithp = e[13 * C];
-                mp.isn = e[14 * C];
+                mp.Sg = e[10 * C];
+                mp.thp = e[11 * C];
+                mp.iS = e[12 * C];
+                mp.irp = e[13 * C];
+                mp.ithp = e[14 * C];
+                mp.isn = e[15 * C];
                 double dtau[NF], jn[NF];
                 const bool ok = rt_terms_fp64<NF>(imgs[timg[te]], y, mp, e[0], dtau, jn);
                 c.rt_samples += ok ? 1 : 0;

@@ -46,11 +46,11 @@ __device__ __forceinline__ void mks_point(DF x1, DF x2, const GeoDF& g, MksPoint
 // projection.
 __device__ __forceinline__ MetricT<float> metric_f32(const MksPointT<DF>& p, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
-    const float r = p.r.hi, s = p.s.hi, c = p.c.hi, irho2 = p.iS.hi;
+    const float r = p.r.hi, s = p.s.hi, irho2 = p.iS.hi;
     const float s2 = s * s;
     const float rfac = r - R0;
-    const float hfac = 3.14159265f * fmaf(gd.one_m_h.hi, p.c2x.hi, 1.0f);
-    const float rho2 = fmaf(r, r, a2 * c * c);
+    const float hfac = p.thp.hi;
+    const float rho2 = p.Sg.hi;
     const float z = 2.0f * r * irho2;
     const float ir = (R0 == 0.0f) ? p.irp.hi : 1.0f / r;
     MetricT<float> g;

@@ -153,12 +153,16 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     const T b2 = beta * beta;
     const T i1b2 = T(1) / (T(1) + b2);
     const T trat = r_high * b2 * i1b2 + r_low * i1b2;
-    const T two_temp_gam = T(0.5) * ((T(1) + T(2) / T(3) * (trat + T(1)) / (trat + T(2))) + T(4) / T(3));
-    const T Thetae_unit = (two_temp_gam - T(1)) * (T)(kPMass / kEMass) / (T(1) + trat);
-    T th = (uu / rho) * Thetae_unit;
+    // (trat + 1)/(trat + 2) and 1/(1 + trat) from one division
+    const T tp1 = trat + T(1), tp2 = trat + T(2);
+    const T itt = T(1) / (tp1 * tp2);
+    const T two_temp_gam = T(0.5) * ((T(1) + T(2) / T(3) * (tp1 * tp1 * itt)) + T(4) / T(3));
+    const T Thetae_unit = (two_temp_gam - T(1)) * (T)(kPMass / kEMass) * (tp2 * itt);
+    const T irho = T(1) / rho;
+    T th = (uu * irho) * Thetae_unit;
     if (th < T(0)) th = tiny;
     fl.thetae = th;
-    return !(Bsq / rho > T(1));
+    return !(Bsq * irho > T(1));  // the sigma cut, b^2 / rho > 1
 }
 
 // ---------------------------------------------------------------- FP64 form
@@ -207,9 +211,10 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     const bool emits = (fabs(sth) >= 1.e-10) && (fl.thetae > 1e-4);
     // j = n_e sqrt(2) pi nu_s / (3 K2) F(X) e2_c with K2 = 2 Theta^2: the
     // frequency-independent factor once per sample
-    const double jpre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0) * nus / (fl.thetae * fl.thetae) * kE2C;
+    const double ith = 1.0 / fl.thetae;
+    const double jpre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0) * nus * (ith * ith) * kE2C;
     // h nu / (k T) = nu h / (m_e c^2 Theta_e)
-    const double hkt = (kPlanck / (kEMass * kC * kC)) / fl.thetae;
+    const double hkt = (kPlanck / (kEMass * kC * kC)) * ith;
     // one copy of the frequency body (5 frequencies: 7 % faster than unrolled)
 #pragma unroll 1
     for (int f = 0; f < NF; ++f) {

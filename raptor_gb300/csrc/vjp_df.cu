@@ -49,12 +49,12 @@ __device__ __forceinline__ F3 liftf(const F1& a) {
 // ray_kernel_df.cu).
 __device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<DD1>& pd, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
-    const F1 r = to_f1(pd.r), s = to_f1(pd.s), c = to_f1(pd.c), irho2 = to_f1(pd.iS);
-    const F1 c2x = to_f1(pd.c2x), irp = to_f1(pd.irp), ithp = to_f1(pd.ithp), isn = to_f1(pd.isn);
+    const F1 r = to_f1(pd.r), s = to_f1(pd.s), irho2 = to_f1(pd.iS);
+    const F1 irp = to_f1(pd.irp), ithp = to_f1(pd.ithp), isn = to_f1(pd.isn);
     const F1 s2 = s * s;
     const F1 rfac = r - R0;
-    const F1 hfac = 3.14159265f * (gd.one_m_h.hi * c2x + 1.0f);
-    const F1 rho2 = r * r + a2 * (c * c);
+    const F1 hfac = to_f1(pd.thp);
+    const F1 rho2 = to_f1(pd.Sg);
     const F1 z = 2.0f * (r * irho2);
     const F1 ir = (R0 == 0.0f) ? irp : F1(1.0f) / r;
     const F1 opz = 1.0f + z;

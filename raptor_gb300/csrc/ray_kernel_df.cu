@@ -30,10 +30,9 @@ struct RayStateDF {
 __device__ __forceinline__ DF step_size_df(const DevImage& im, const DF y[8]) {
     const float t = 1.e-40f;
     const DF m2 = fmin(y[2], 1.0 - y[2]);
-    const DF i1 = add_f(fabs(y[5]), t) * im.inv_stepsize_df;
-    const DF i2 = add_f(fabs(y[6]), t) * im.inv_stepsize_df / m2;
-    const DF i3 = add_f(fabs(y[7]), t) * im.inv_stepsize_df;
-    return -fmax(1.0 / (i1 + i2 + i3), df_const(1e-12));
+    const DF i13 = add_f(fabs(y[5]), t) + add_f(fabs(y[7]), t);
+    const DF i2 = add_f(fabs(y[6]), t);
+    return -fmax(m2 / ((m2 * i13 + i2) * im.inv_stepsize_df), df_const(1e-12));
 }
 
 // mks_point for DF states: the rolled form (kerr_mks.cuh)

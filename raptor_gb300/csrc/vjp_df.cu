@@ -173,10 +173,9 @@ __device__ __forceinline__ bool sample_freq_f(const DevImage& im, const SampleCo
 __device__ __forceinline__ DD1 step_size_dd1(const DevImage& im, const DD1 y[8]) {
     const DF t = df_const(1.e-40);
     const DD1 m2 = fmin(y[2], 1.0 - y[2]);
-    const DD1 i1 = (fabs(y[5]) + t) * im.inv_stepsize_df;
-    const DD1 i2 = (fabs(y[6]) + t) * im.inv_stepsize_df / m2;
-    const DD1 i3 = (fabs(y[7]) + t) * im.inv_stepsize_df;
-    return -fmax(1.0 / (i1 + i2 + i3), 1e-12);
+    const DD1 i13 = (fabs(y[5]) + t) + (fabs(y[7]) + t);
+    const DD1 i2 = fabs(y[6]) + t;
+    return -fmax(m2 / ((m2 * i13 + i2) * im.inv_stepsize_df), 1e-12);
 }
 
 template <int NF>

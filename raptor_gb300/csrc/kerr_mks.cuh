@@ -207,13 +207,16 @@ __device__ __forceinline__ void mks_metric(const MksPointT<R>& p, const G& g, Me
     const R hfac = p.thp;
     const R rho2 = p.Sg;
     const R z = 2.0 * r * irho2;
+    const R mas2 = -a * s2;
+    const R opz = 1.0 + z;
+    const R opzr = opz * rfac;
     d.g00 = -1.0 + z;
     d.g01 = z * rfac;
-    d.g03 = -a * z * s2;
-    d.g11 = (1.0 + z) * rfac * rfac;
-    d.g13 = -a * s2 * (1.0 + z) * rfac;
+    d.g03 = mas2 * z;
+    d.g11 = opzr * rfac;
+    d.g13 = mas2 * opzr;
     d.g22 = rho2 * hfac * hfac;
-    d.g33 = s2 * (rho2 + g.a2 * s2 * (1.0 + z));
+    d.g33 = s2 * (rho2 + g.a2 * s2 * opz);
     const R ir = (g.R0 == 0.0) ? p.irp : 1.0 / r;  // r == rp exactly when R0 == 0
     u.g00 = -1.0 - z;
     u.g01 = 2.0 * irho2;

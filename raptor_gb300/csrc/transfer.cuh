@@ -125,9 +125,8 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     const T V1 = v[2], V2 = v[3], V3 = v[4];
     const T Bp1 = v[5], Bp2 = v[6], Bp3 = v[7];
     fl.ne = rho * Ne_unit;
-    // g_ij V^i V^j, i,j = 1..3, in the reference's loop order with its zeros dropped
-    const T VdotV = g.d11 * V1 * V1 + g.d13 * V1 * V3 + g.d22 * V2 * V2 + g.d13 * V3 * V1 +
-                    g.d33 * V3 * V3;
+    // g_ij V^i V^j, i,j = 1..3, with g_12 = g_23 = 0
+    const T VdotV = (g.d11 * V1 + T(2) * g.d13 * V3) * V1 + g.d22 * V2 * V2 + g.d33 * V3 * V3;
     const T Vfac = sqrt(T(-1) / g.u00 * (T(1) + fabs(VdotV)));
     T* U = fl.ucon;
     U[0] = -Vfac * g.u00;

@@ -128,7 +128,9 @@ __device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g
     const R iS = p.iS, iS2 = iS * iS, iS3 = iS2 * iS;
     const R B = (2.0 * r2 - Sg) * iS3;
     const R riS = r * iS;
-    const R C = riS - a2 * B * s2;
+    const R as2 = a * s2;
+    const R aB = a * B;
+    const R C = riS - aB * as2;
     const R irp = p.irp, ithp = p.ithp;
 
     const R u0 = U[0], u1 = U[1], u2 = U[2], u3 = U[3];
@@ -159,28 +161,29 @@ __device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g
     // The double-float type gains as much (1024x1024 mixed-DF render 137 ->
     // 119 ms against compensated dot products over the 40 symbols), with its
     // geodesic still within 1e-10 of the FP64 one.
-    const R as2 = a * s2;
     const R Tr = (Sg + two_r) * rp;
     const R X0 = q00 - as2 * q03;
     const R X1 = q01 - as2 * q13;
     const R H = q00 + rp * (q01 + rp * q11);  // q00 + r' q01 + r'^2 q11
-    const R iS2thp = iS2 * thp;
-    const R a2rs = a2 * r * s2th;
-    const R Wp = a2rs * iS2;                  // G0_02 = -Wp theta'
-    const R WpT = a2rs * iS2thp;              // Wp theta'
+    const R iSthp = iS * thp;
+    const R iS2thp = iS * iSthp;
+    const R a2sc = a2 * sc;
+    const R WpT = two_r * a2sc * iS2thp;      // -G0_02 = a^2 r sin 2theta iS^2 theta'
     const R riSthp2 = riS * thp2;
-    const R Cs2 = C * s2;
+    const R M = riSthp2 * q22 + C * s2 * q33;  // shared by A0 and A1
     const R Dlirp = Dl * irp;
-    const R G1_12 = -a2 * sc * iS * thp;
+    const R G1_12 = -a2sc * iSthp;
     A[0] = -(B * (two_r * X0 + Tr * X1 + 2.0 * (Sg + r) * rp2 * q11) - WpT * (q02 + rp * q12 - as2 * q23) -
-             two_r * riSthp2 * q22 - two_r * Cs2 * q33);
+             two_r * M);
     A[1] = -(B * (Dlirp * X0 + (Dl - Sg) * X1 - (2.0 * Sg - Dl) * rp * q11) + q11 + riS * as2 * q13 +
-             G1_12 * q12 - riSthp2 * Dlirp * q22 - Dlirp * Cs2 * q33);
+             G1_12 * q12 - Dlirp * M);
+    // Z = sin cos iS^3 / theta'; the G2_00 terms -iS Wp / theta' H are 2 a^2 r Z H
     const R Z = sc * iS3 * ithp;
-    A[2] = -(Z * (a * Rr2 * q03 + a * (Aq + Sg * (Sg - Dl)) * rp * q13 - (Dl * Sg * Sg + Rr2 * r2a2) * q33) -
-             iS * Wp * ithp * H + riS * rp * q12 + (thpp * ithp + G1_12) * q22);
+    A[2] = -(Z * (a * (Rr2 * q03 + (Aq + Sg * (Sg - Dl)) * rp * q13) - (Dl * Sg * Sg + Rr2 * r2a2) * q33 -
+                  a2 * two_r * H) +
+             riS * rp * q12 + (thpp * ithp + G1_12) * q22);
     const R K = a * cot * iS2thp;  // G3_02 = -2 r K, G3_12 = -(Sigma+2r) r' K
-    A[3] = -(a * B * (H - as2 * q03) - K * (two_r * q02 + Tr * q12) + C * (rp * q13 - as2 * q33) -
+    A[3] = -(aB * (H - as2 * q03) - K * (two_r * q02 + Tr * q12) + C * (rp * q13 - as2 * q33) -
              a * riSthp2 * q22 + (cot * thp + WpT) * q23);
 }
 

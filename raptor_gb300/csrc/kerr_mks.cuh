@@ -119,12 +119,11 @@ __device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g
     const R sc = s * c;
     const R s2th = 2.0 * sc;
     const R cot = c * p.isn;
-    const R Sg = p.Sg;
-    const R Dl = r2 - 2.0 * r + a2;
+    const R Sg = p.Sg, Sg2 = Sg * Sg;
     const R r2a2 = r2 + a2;
     const R two_r = 2.0 * r;
+    const R Dl = r2a2 - two_r;
     const R Rr2 = two_r * r2a2;  // 2 r (r^2 + a^2)
-    const R Aq = Sg * Dl + Rr2;
     const R iS = p.iS, iS2 = iS * iS, iS3 = iS2 * iS;
     const R B = (2.0 * r2 - Sg) * iS3;
     const R riS = r * iS;
@@ -177,10 +176,11 @@ __device__ __forceinline__ void geodesic_accel(const MksPointT<R>& p, const G& g
              two_r * M);
     A[1] = -(B * (Dlirp * X0 + (Dl - Sg) * X1 - (2.0 * Sg - Dl) * rp * q11) + q11 + riS * as2 * q13 +
              G1_12 * q12 - Dlirp * M);
-    // Z = sin cos iS^3 / theta'; the G2_00 terms -iS Wp / theta' H are 2 a^2 r Z H
+    // Z = sin cos iS^3 / theta'; the G2_00 terms -iS Wp / theta' H are 2 a^2 r Z H,
+    // and G2_13's Aq + Sigma (Sigma - Delta) with Aq = Sigma Delta + 2 r (r^2 + a^2)
+    // is Sigma^2 + 2 r (r^2 + a^2)
     const R Z = sc * iS3 * ithp;
-    A[2] = -(Z * (a * (Rr2 * q03 + (Aq + Sg * (Sg - Dl)) * rp * q13) - (Dl * Sg * Sg + Rr2 * r2a2) * q33 -
-                  a2 * two_r * H) +
+    A[2] = -(Z * (a * (Rr2 * q03 + (Sg2 + Rr2) * rp * q13) - (Dl * Sg2 + Rr2 * r2a2) * q33 - a2 * two_r * H) +
              riS * rp * q12 + (thpp * ithp + G1_12) * q22);
     const R K = a * cot * iS2thp;  // G3_02 = -2 r K, G3_12 = -(Sigma+2r) r' K
     A[3] = -(aB * (H - as2 * q03) - K * (two_r * q02 + Tr * q12) + C * (rp * q13 - as2 * q33) -

@@ -392,18 +392,21 @@ extern "C" long long raptor_gpu_spectrum_size(const raptor_image_desc* imgs, int
 }
 
 // ----------------------------------------------------------------- render
+// Renders take ray_kernel<NF, MIXED, false>; a trace (any frequency count)
+// takes the 8-frequency trace kernel, which also integrates t and phi.
 template <int NF, bool MIXED>
 static void launch_ray(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b, long long e,
                        unsigned long long* ctr, double* out, TraceSpec tr) {
-    ray_kernel<NF, MIXED><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
+    if (tr.out) ray_kernel<kMaxFreqs, MIXED, true><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
+    else ray_kernel<NF, MIXED, false><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
 }
 
 // The FP64 form's pooled kernel; a trace (per-step records of tau and I)
-// needs the in-place sample and takes ray_kernel.
+// needs the in-place sample and takes the trace kernel.
 template <int NF>
 static void launch_ray_pool(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b,
                             long long e, unsigned long long* ctr, double* out, TraceSpec tr) {
-    if (tr.out) ray_kernel<NF, false><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
+    if (tr.out) ray_kernel<kMaxFreqs, false, true><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
     else ray_kernel_pool<NF><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill);
 }
 
@@ -413,9 +416,9 @@ RayLaunchFn pick_ray_kernel(int nf, int form, const void** fn, bool pool) {
     // one instantiation per frequency-count bucket so tau/I stay in registers
 #define PICK(NF)                                                        \
     if (nf <= NF) {                                                     \
-        if (mixed) { *fn = (const void*)ray_kernel<NF, true>; return launch_ray<NF, true>; } \
+        if (mixed) { *fn = (const void*)ray_kernel<NF, true, false>; return launch_ray<NF, true>; } \
         if (pool) { *fn = (const void*)ray_kernel_pool<NF>; return launch_ray_pool<NF>; } \
-        *fn = (const void*)ray_kernel<NF, false>;                      \
+        *fn = (const void*)ray_kernel<NF, false, false>;               \
         return launch_ray<NF, false>;                                   \
     }
     PICK(1)

@@ -143,6 +143,15 @@ __device__ __forceinline__ void rhs(const MksPointT<R>& p, const G& g, const R y
     geodesic_accel(p, g, ys + 4, f + 4);
 }
 
+// Whether an RK step updates state component i.  The metric does not depend
+// on t or phi, so x^0 and x^3 feed nothing the image, its derivatives or the
+// stopping tests read; kernels that do not record traces (TPhi = false)
+// leave them at their initial values.
+template <bool TPhi>
+__device__ __forceinline__ constexpr bool rk_updates(int i) {
+    return TPhi || (i != 0 && i != 3);
+}
+
 // One RK4 step (integrator.c:13-41): stage weights 1/2, 1/2, 1 and
 // y += dt (f1 + 2 f2 + 2 f3 + f4) / 6.  dt multiplies the stage offsets and
 // the final sum instead of each stage's derivatives (the reference forms
@@ -151,7 +160,7 @@ __device__ __forceinline__ void rhs(const MksPointT<R>& p, const G& g, const R y
 // Stages 2-4 run as one rolled loop: the stage body (point transcendentals,
 // the connection, contraction) is large, and one copy of it instead of
 // three keeps the kernel's hot loop inside the instruction cache.
-template <class R, class G>
+template <class R, class G, bool TPhi = true>
 __device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R dt) {
     using W = typename StageWeight<R>::type;
     R acc[8], ys[8], f[8];
@@ -160,7 +169,7 @@ __device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R 
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         acc[i] = f[i];
-        ys[i] = y[i] + hdt * f[i];
+        ys[i] = rk_updates<TPhi>(i) ? y[i] + hdt * f[i] : y[i];
     }
 #pragma unroll 1
     for (int q = 1; q < 4; ++q) {
@@ -171,13 +180,15 @@ __device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R 
         const R dnext = (q == 1) ? hdt : dt;          // stage offsets dt/2, dt/2, dt
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
+            if (!rk_updates<TPhi>(i)) continue;
             acc[i] = acc[i] + f[i] * wacc;
             ys[i] = y[i] + dnext * f[i];
         }
     }
     const R dt6 = dt * (1.0 / 6.0);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) y[i] = y[i] + dt6 * acc[i];
+    for (int i = 0; i < 8; ++i)
+        if (rk_updates<TPhi>(i)) y[i] = y[i] + dt6 * acc[i];
     mks_point(y[1], y[2], g, p);
 }
 
@@ -187,7 +198,7 @@ __device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R 
 // For the double-float state, where each operation is about ten FP32
 // instructions, the single copy keeps the hot loop from stalling on
 // instruction fetch.
-template <class R, class G>
+template <class R, class G, bool TPhi = true>
 __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>& p, R dt) {
     using W = typename StageWeight<R>::type;
     R acc[8], ys[8], f[8];
@@ -204,6 +215,7 @@ __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>
         const R dnext = (q < 2) ? hdt : dt;                   // stage offsets dt/2, dt/2, dt
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
+            if (!rk_updates<TPhi>(i)) continue;
             acc[i] = (q == 0) ? f[i] : acc[i] + f[i] * wacc;
             ys[i] = y[i] + dnext * f[i];
         }
@@ -211,6 +223,7 @@ __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>
             const R dt6 = dt * (1.0 / 6.0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
+                if (!rk_updates<TPhi>(i)) continue;
                 y[i] = y[i] + dt6 * acc[i];
                 ys[i] = y[i];
             }
@@ -220,17 +233,18 @@ __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>
 }
 
 // RK2 midpoint step (integrator.c:44-70).
-template <class R, class G>
+template <class R, class G, bool TPhi = true>
 __device__ __forceinline__ void rk2_step(const G& g, R y[8], MksPointT<R>& p, R dt) {
     R ys[8], f[8];
     rhs(p, g, y, f);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) ys[i] = y[i] + dt * f[i] * 0.5;
+    for (int i = 0; i < 8; ++i) ys[i] = rk_updates<TPhi>(i) ? y[i] + dt * f[i] * 0.5 : y[i];
     MksPointT<R> q;
     mks_point(ys[1], ys[2], g, q);
     rhs(q, g, ys, f);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) y[i] = y[i] + dt * f[i];
+    for (int i = 0; i < 8; ++i)
+        if (rk_updates<TPhi>(i)) y[i] = y[i] + dt * f[i];
     mks_point(y[1], y[2], g, p);
 }
 
@@ -368,7 +382,7 @@ __device__ __forceinline__ void finish_ray(const DevImage& im, const RayState<NF
 // event: 0 stepped outside the sampling region, 1 inside it (sample due),
 // 3 escaped outward (integrator.c:271-272), -1 the while-condition ended the
 // ray before the step.  dl is the step taken.
-template <int NF, bool MIXED>
+template <int NF, bool MIXED, bool TPhi = true>
 __device__ __forceinline__ int advance_ray(const DevImage& im, RayState<NF, MIXED>& s, double& dl) {
     // while-condition of integrator.c:228-229 (r = exp(x1), no R0)
     const double r = s.p.rp;
@@ -378,15 +392,16 @@ __device__ __forceinline__ int advance_ray(const DevImage& im, RayState<NF, MIXE
     s.thdot_prev = s.y[6];
     if ((s.beta < 0.0 && s.turns > kMaxOrder) || (s.beta > 0.0 && s.turns > kMaxOrder + 1)) s.stop = 1;
     dl = step_size(im, s.y);
-    if (im.integrator == 2) rk2_step(im.geo, s.y, s.p, dl);
-    else rk4_step(im.geo, s.y, s.p, dl);
+    if (im.integrator == 2) rk2_step<double, Geo, TPhi>(im.geo, s.y, s.p, dl);
+    else rk4_step<double, Geo, TPhi>(im.geo, s.y, s.p, dl);
     s.steps += 1;
     if (s.y[1] > im.stopx1 && s.y[5] < 0.0) return 3;
     if (s.y[1] < im.stopx1 && s.y[1] > im.startx1 && s.y[2] > im.startx2 && s.y[2] < im.stopx2) return 1;
     return 0;
 }
 
-template <int NF, bool MIXED>
+// TRACE: the per-step trace kernel (t and phi integrated, records written)
+template <int NF, bool MIXED, bool TRACE>
 __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
     ray_kernel(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
                unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval,
@@ -410,7 +425,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
                 if (rid < ray_end) {
                     im = start_ray(imgs, n_imgs, rid, s);
                     active = true;
-                    if (tr.out && rid == tr.ray) trace_record<NF, MIXED>(tr, s, 0.0, 0);
+                    if (TRACE && rid == tr.ray) trace_record<NF, MIXED>(tr, s, 0.0, 0);
                 } else {
                     live = false;
                 }
@@ -420,7 +435,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
         if (active) {
             for (int it = 0; it < refill_interval; ++it) {
                 double dl = 0.0;
-                int event = advance_ray(*im, s, dl);
+                int event = advance_ray<NF, MIXED, TRACE>(*im, s, dl);
                 const bool done = event == -1 || event == 3;
                 if (event == 1) {
                     ++c.rt_calls;
@@ -430,7 +445,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
                     c.rt_samples += sampled ? 1 : 0;
                     event = sampled ? 2 : 1;
                 }
-                if (event != -1 && tr.out && s.rid == tr.ray) trace_record<NF, MIXED>(tr, s, dl, event);
+                if (TRACE && event != -1 && s.rid == tr.ray) trace_record<NF, MIXED>(tr, s, dl, event);
                 if (done) {
                     finish_ray(*im, s, out, c);
                     active = false;
@@ -580,7 +595,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
         bool want = false;
         double dl = 0.0;
         if (mode == 1) {
-            const int event = advance_ray(*im, s, dl);
+            const int event = advance_ray<NF, false, false>(*im, s, dl);
             if (event == 1) {
                 ++c.rt_calls;
                 want = true;

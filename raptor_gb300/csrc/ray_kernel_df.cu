@@ -150,7 +150,7 @@ __device__ __forceinline__ const DevImage* start_ray_df(const DevImage* __restri
 // One step of integrate_geodesic's loop (integrator.c:228-285), as
 // advance_ray in ray_kernel.cuh: -1 the while-condition ended the ray, 0
 // stepped outside the sampling region, 1 inside it, 3 escaped outward.
-template <int NF>
+template <int NF, bool TPhi>
 __device__ __forceinline__ int advance_ray_df(const DevImage& im, RayStateDF<NF>& s, DF& dl) {
     const DF r = s.p.rp;
     if (!(r < df_const(kCutoffOuter) && r > im.cutoff_inner_df && s.steps < (int)kMaxSteps && !s.stop)) return -1;
@@ -160,8 +160,8 @@ __device__ __forceinline__ int advance_ray_df(const DevImage& im, RayStateDF<NF>
     s.thdot_prev = th;
     if ((s.bsign < 0 && s.turns > kMaxOrder) || (s.bsign > 0 && s.turns > kMaxOrder + 1)) s.stop = 1;
     dl = step_size_df(im, s.y);
-    if (im.integrator == 2) rk2_step(im.geo_df, s.y, s.p, dl);
-    else rk4_step_rolled(im.geo_df, s.y, s.p, dl);
+    if (im.integrator == 2) rk2_step<DF, GeoDF, TPhi>(im.geo_df, s.y, s.p, dl);
+    else rk4_step_rolled<DF, GeoDF, TPhi>(im.geo_df, s.y, s.p, dl);
     s.steps += 1;
     if (s.y[1] > im.stopx1_df && s.y[5].hi < 0.0f) return 3;
     if (s.y[1] < im.stopx1_df && s.y[1] > im.startx1_df && s.y[2] > im.startx2_df && s.y[2] < im.stopx2_df) return 1;
@@ -208,7 +208,8 @@ __device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayState
 // kernel's time, and the ring's code (and a sample split into its
 // order-free and ordered halves) adds to an instruction stream that already
 // stalls on fetch.
-template <int NF>
+// TRACE: the per-step trace kernel (t and phi integrated, records written)
+template <int NF, bool TRACE>
 __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
     ray_kernel_df(const DevImage* __restrict__ imgs, int n_imgs, long long ray_begin, long long ray_end,
                   unsigned long long* __restrict__ counters, double* __restrict__ out, int refill_interval,
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
                 if (rid < ray_end) {
                     im = start_ray_df(imgs, n_imgs, rid, s);
                     active = true;
-                    if (tr.out && rid == tr.ray) trace_record_df<NF>(tr, s, 0.0, 0);
+                    if (TRACE && rid == tr.ray) trace_record_df<NF>(tr, s, 0.0, 0);
                 } else {
                     live = false;
                 }
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
         if (active) {
             for (int it = 0; it < refill_interval; ++it) {
                 DF dl = df_const(0.0);
-                int event = advance_ray_df(*im, s, dl);
+                int event = advance_ray_df<NF, TRACE>(*im, s, dl);
                 const bool done = event == -1 || event == 3;
                 if (event == 1) {
                     ++c.rt_calls;
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
                     c.rt_samples += sampled ? 1 : 0;
                     event = sampled ? 2 : 1;
                 }
-                if (event != -1 && tr.out && s.rid == tr.ray) trace_record_df<NF>(tr, s, df_to_double(dl), event);
+                if (TRACE && event != -1 && s.rid == tr.ray) trace_record_df<NF>(tr, s, df_to_double(dl), event);
                 if (done) {
                     finish_ray_df(*im, s, out, c);
                     active = false;
@@ -261,10 +262,12 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
     c.publish(counters, lane);
 }
 
+// renders; a trace (any frequency count) takes the 8-frequency trace kernel
 template <int NF>
 void launch_ray_df(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs, int n, long long b, long long e,
                    unsigned long long* ctr, double* out, TraceSpec tr) {
-    ray_kernel_df<NF><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
+    if (tr.out) ray_kernel_df<kMaxFreqs, true><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
+    else ray_kernel_df<NF, false><<<ls.grid, ls.block, 0, st>>>(imgs, n, b, e, ctr, out, ls.refill, tr);
 }
 
 }  // namespace
@@ -273,9 +276,9 @@ void launch_ray_df(const LaunchShape& ls, cudaStream_t st, const DevImage* imgs,
 using namespace raptor;
 
 RayLaunchFn pick_ray_kernel_df(int nf, const void** fn) {
-    if (nf <= 1) { *fn = (const void*)ray_kernel_df<1>; return launch_ray_df<1>; }
-    if (nf <= 2) { *fn = (const void*)ray_kernel_df<2>; return launch_ray_df<2>; }
-    if (nf <= 4) { *fn = (const void*)ray_kernel_df<4>; return launch_ray_df<4>; }
-    *fn = (const void*)ray_kernel_df<8>;
+    if (nf <= 1) { *fn = (const void*)ray_kernel_df<1, false>; return launch_ray_df<1>; }
+    if (nf <= 2) { *fn = (const void*)ray_kernel_df<2, false>; return launch_ray_df<2>; }
+    if (nf <= 4) { *fn = (const void*)ray_kernel_df<4, false>; return launch_ray_df<4>; }
+    *fn = (const void*)ray_kernel_df<8, false>;
     return launch_ray_df<8>;
 }

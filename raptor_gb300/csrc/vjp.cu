@@ -332,8 +332,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             thdot_prev = y[6].v;
             if ((beta < 0.0 && turns > kMaxOrder) || (beta > 0.0 && turns > kMaxOrder + 1)) stop = 1;
             const D1 dl = step_size(im, y);
-            if (im.integrator == 2) rk2_step(im.geo, y, p, dl);
-            else rk4_step_rolled(im.geo, y, p, dl);
+            if (im.integrator == 2) rk2_step<D1, Geo, false>(im.geo, y, p, dl);
+            else rk4_step_rolled<D1, Geo, false>(im.geo, y, p, dl);
             steps += 1;
             if (y[1].v > im.stopx1 && y[5].v < 0.0) break;
             if (y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2) {
@@ -502,8 +502,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 thdot_prev = y[6].v;
                 if ((beta < 0.0 && turns > kMaxOrder) || (beta > 0.0 && turns > kMaxOrder + 1)) stop = 1;
                 const D1 dl = step_size(im, y);
-                if (im.integrator == 2) rk2_step(im.geo, y, p, dl);
-                else rk4_step_rolled(im.geo, y, p, dl);
+                if (im.integrator == 2) rk2_step<D1, Geo, false>(im.geo, y, p, dl);
+                else rk4_step_rolled<D1, Geo, false>(im.geo, y, p, dl);
                 steps += 1;
                 if (y[1].v > im.stopx1 && y[5].v < 0.0) {
                     done = true;

@@ -290,8 +290,8 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                 s.thdot_prev = th;
                 if ((s.bsign < 0 && s.turns > kMaxOrder) || (s.bsign > 0 && s.turns > kMaxOrder + 1)) s.stop = 1;
                 const DD1 dl = step_size_dd1(im, s.y);
-                if (im.integrator == 2) rk2_step(im.geo_df, s.y, s.p, dl);
-                else rk4_step_rolled(im.geo_df, s.y, s.p, dl);
+                if (im.integrator == 2) rk2_step<DD1, GeoDF, false>(im.geo_df, s.y, s.p, dl);
+                else rk4_step_rolled<DD1, GeoDF, false>(im.geo_df, s.y, s.p, dl);
                 s.steps += 1;
                 if (s.y[1].v > im.stopx1_df && s.y[5].v.hi < 0.0f) {
                     done = true;

@@ -50,6 +50,7 @@ struct DevImage {
     double freq[kMaxFreqs];
     double nu3[kMaxFreqs];        // freq^3 (core.c:136)
     double rg_over_nu[kMaxFreqs]; // R_g / freq (radiative_transfer.c:88)
+    double inv_freq2[kMaxFreqs];  // 1 / freq^2
     // log-polar camera (integrator.c:191-198, core.c:123-133)
     int camera;                   // 0 linear, 1 log-polar
     double ln20;                  // log(20.)

@@ -176,6 +176,7 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
         im.freq[f] = d.freq[f];
         im.nu3[f] = pow(d.freq[f], 3.);
         im.rg_over_nu[f] = Rg / d.freq[f];
+        im.inv_freq2[f] = 1.0 / (d.freq[f] * d.freq[f]);
         im.freq_f[f] = (float)im.freq[f];
         im.rg_over_nu_f[f] = (float)im.rg_over_nu[f];
     }

@@ -164,6 +164,62 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     return !(Bsq * irho > T(1));  // the sigma cut, b^2 / rho > 1
 }
 
+// get_fluid_params for the FP64 sample: fluid_from_prims's quantities from
+// one reciprocal square root and two divisions where the template takes a
+// square root and six divisions (the mixed forms and the adjoint keep the
+// template).  With w = 1 + |V.V| and P = -g^00 w: u^0 = sqrt(P), the 1/u^0 of
+// b^i is rsqrt(P) and Vfac = sqrt(w / -g^00) = w rsqrt(P).  In the R-beta
+// model beta = h / D with h = 2u/3 and D = b^2 + tiny, so trat = N / Q with
+// N = r_high h^2 + r_low D^2 and Q = h^2 + D^2; with A = N + Q and C = A + Q
+// the two quotients the model needs, (trat + 1)/(trat + 2) = A / C and
+// 1/(1 + trat) = Q / A, come from one reciprocal of A C.  D^2 >= 1e-40, so
+// no product underflows.
+__device__ __forceinline__ bool fluid_fp64(const double v[8], const MetricT<double>& g, double Ne_unit,
+                                           double B_unit, double r_high, double r_low, Fluid<double>& fl) {
+    const double tiny = 1.e-20;
+    const double rho = v[0], uu = v[1];
+    const double V1 = v[2], V2 = v[3], V3 = v[4];
+    const double Bp1 = v[5], Bp2 = v[6], Bp3 = v[7];
+    fl.ne = rho * Ne_unit;
+    const double VdotV = (g.d11 * V1 + 2.0 * g.d13 * V3) * V1 + g.d22 * V2 * V2 + g.d33 * V3 * V3;
+    const double w = 1.0 + fabs(VdotV);
+    const double P = -g.u00 * w;
+    const double iU0 = rsqrt(P);
+    const double Vfac = w * iU0;
+    double* U = fl.ucon;
+    U[0] = P * iU0;
+    U[1] = V1 - Vfac * g.u01;
+    U[2] = V2;  // g^{02} = 0
+    U[3] = V3;  // g^{03} = 0
+    double Ucov[4];
+    lowerT(g, U, Ucov);
+    const double UdotBp = Ucov[1] * Bp1 + Ucov[2] * Bp2 + Ucov[3] * Bp3;
+    double* Bc = fl.bcon;
+    Bc[0] = UdotBp;
+    Bc[1] = (Bp1 + U[1] * UdotBp) * iU0;
+    Bc[2] = (Bp2 + U[2] * UdotBp) * iU0;
+    Bc[3] = (Bp3 + U[3] * UdotBp) * iU0;
+    double Bcov[4];
+    lowerT(g, Bc, Bcov);
+    const double Bsq = Bc[0] * Bcov[0] + Bc[1] * Bcov[1] + Bc[2] * Bcov[2] + Bc[3] * Bcov[3];
+    fl.bsq = Bsq;
+    fl.B = sqrt(Bsq) * B_unit + tiny;
+    // R-beta electron temperature, raptor_harm_model.c:262-276
+    const double h = uu * (2.0 / 3.0), D = Bsq + tiny;
+    const double h2 = h * h, D2 = D * D;
+    const double Q = h2 + D2;
+    const double A = r_high * h2 + r_low * D2 + Q;
+    const double C = A + Q;
+    const double iAC = 1.0 / (A * C);
+    const double two_temp_gam = 0.5 * ((1.0 + 2.0 / 3.0 * (A * A * iAC)) + 4.0 / 3.0);
+    const double Thetae_unit = (two_temp_gam - 1.0) * (kPMass / kEMass) * (Q * C * iAC);
+    const double irho = 1.0 / rho;
+    double th = (uu * irho) * Thetae_unit;
+    if (th < 0.0) th = tiny;
+    fl.thetae = th;
+    return !(Bsq * irho > 1.0);  // the sigma cut, b^2 / rho > 1
+}
+
 // ---------------------------------------------------------------- FP64 form
 // The sample splits into the part that depends only on the post-step point -
 // fluid, emissivity and absorptivity, per frequency the optical-depth
@@ -192,7 +248,7 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     double v[8];
     interp_prims(im.cells64, im.n2, cc, v);
     Fluid<double> fl;
-    if (!fluid_from_prims(v, g, im.Ne_unit, im.B_unit, im.r_high, im.r_low, fl)) return false;
+    if (!fluid_fp64(v, g, im.Ne_unit, im.B_unit, im.r_high, im.r_low, fl)) return false;
 
     const double k[4] = {y[4], y[5], y[6], y[7]};
     double kd[4];
@@ -200,20 +256,26 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     const double* U = fl.ucon;
     const double* Bc = fl.bcon;
     const double kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    // pitch_angle (radiative_transfer.c:32-47): cosine, clamped to [-1, 1]
-    double pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) /
-                   (fabs(kU) * fl.B * im.inv_B_unit);
+    // pitch_angle (radiative_transfer.c:32-47): cosine, clamped to [-1, 1].
+    // 1/(k.u |B|) gives the cosine's 1/(|k.u| |B|) (|B| > 0) and 1/(k.u).
+    const double Bn = fl.B * im.inv_B_unit;
+    const double ikB = 1.0 / (kU * Bn);
+    double pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) * fabs(ikB);
     if (fabs(pitch) > 1.0) pitch /= fabs(pitch);
     const double sth = sqrt(1.0 - pitch * pitch);
     const double nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
     const double nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
     const bool emits = (fabs(sth) >= 1.e-10) && (fl.thetae > 1e-4);
     // j = n_e sqrt(2) pi nu_s / (3 K2) F(X) e2_c with K2 = 2 Theta^2: the
-    // frequency-independent factor once per sample
-    const double ith = 1.0 / fl.thetae;
-    const double jpre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0) * nus * (ith * ith) * kE2C;
+    // frequency-independent factor n_e sqrt(2) pi (2/9) nu_c sin(theta) e2_c / 6
+    // once per sample (nu_s / Theta^2 taken as (2/9) nu_c sin(theta))
+    const double jpre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0 * (2.0 / 9.0) * kE2C) * (nuc * sth);
     // h nu / (k T) = nu h / (m_e c^2 Theta_e)
-    const double hkt = (kPlanck / (kEMass * kC * kC)) * ith;
+    const double hkt = (kPlanck / (kEMass * kC * kC)) / fl.thetae;
+    // 1/nu_s, and 1/nu_p^2 = (1/(k.u))^2 / nu^2, once per sample
+    const double inus = 1.0 / nus;
+    const double ikU = ikB * Bn;
+    const double ikU2 = ikU * ikU;
     // one copy of the frequency body (5 frequencies: 7 % faster than unrolled)
 #pragma unroll 1
     for (int f = 0; f < NF; ++f) {
@@ -225,12 +287,12 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
         const double ex = fast_exp(hkt * nup) - 1.0;
         if (emits && nup != 1.0) {
             const double dlf = adl * im.rg_over_nu[f];
-            const double X = nup / nus;
+            const double X = nup * inus;
             const double cb = cbrt(X);
             // X^1/2 + 2^(11/12) X^1/6 = X^1/6 (X^1/3 + 2^(11/12)): one square root
             const double sq = sqrt(cb) * (cb + 1.8877486253633869);
             const double j = jpre * (sq * sq) * fast_exp(-cb);
-            const double inup2 = 1.0 / (nup * nup);
+            const double inup2 = ikU2 * im.inv_freq2[f];
             // a nu = j e2_ch / B_nu / e2_c nu = j (e2_ch c^2 / (2 e2_c)) ex / nu^2: inf where
             // B_nu underflows (ex = inf), NaN where j = 0 there too, as j e2_ch / B_nu
             dtau[f] = j * (kE2CH * kC * kC / (2.0 * kE2C)) * ex * inup2 * dlf;

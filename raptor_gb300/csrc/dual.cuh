@@ -28,6 +28,7 @@ using ::fma;
 using ::fmax;
 using ::fmin;
 using ::log;
+using ::rsqrt;
 using ::sincos;
 using ::sincospi;
 using ::sqrt;
@@ -211,6 +212,11 @@ __host__ __device__ inline Dual<N, T, TD> chain(const Dual<N, T, TD>& a, T f, T 
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> sqrt(const Dual<N, T, TD>& a) {
     const T s = sqrt(a.v);
     return chain(a, s, s > scalar_cast<T>(0.0) ? scalar_cast<T>(0.5) / s : scalar_cast<T>(0.0));
+}
+// 1/sqrt(x) of an FP64 dual, its tangent -r^3/2 without a division
+template <int N> __device__ inline Dual<N, double, double> rsqrt(const Dual<N, double, double>& a) {
+    const double r = rsqrt(a.v);
+    return chain(a, r, -0.5 * r * r * r);
 }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> exp(const Dual<N, T, TD>& a) { const T e = exp(a.v); return chain(a, e, e); }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> log(const Dual<N, T, TD>& a) { return chain(a, log(a.v), scalar_cast<T>(1.0) / a.v); }

@@ -113,6 +113,7 @@ template <class T>
 struct Fluid {
     T ne, thetae, B, bsq;
     T ucon[4], bcon[4];
+    T irho;  // 1 / rho
 };
 
 // get_fluid_params (raptor_harm_model.c:190-290) from interpolated
@@ -158,64 +159,68 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     const T two_temp_gam = T(0.5) * ((T(1) + T(2) / T(3) * (tp1 * tp1 * itt)) + T(4) / T(3));
     const T Thetae_unit = (two_temp_gam - T(1)) * (T)(kPMass / kEMass) * (tp2 * itt);
     const T irho = T(1) / rho;
+    fl.irho = irho;
     T th = (uu * irho) * Thetae_unit;
     if (th < T(0)) th = tiny;
     fl.thetae = th;
     return !(Bsq * irho > T(1));  // the sigma cut, b^2 / rho > 1
 }
 
-// get_fluid_params for the FP64 sample: fluid_from_prims's quantities from
-// one reciprocal square root and two divisions where the template takes a
-// square root and six divisions (the mixed forms and the adjoint keep the
-// template).  With w = 1 + |V.V| and P = -g^00 w: u^0 = sqrt(P), the 1/u^0 of
-// b^i is rsqrt(P) and Vfac = sqrt(w / -g^00) = w rsqrt(P).  In the R-beta
-// model beta = h / D with h = 2u/3 and D = b^2 + tiny, so trat = N / Q with
+// get_fluid_params for the FP64 sample and the FP64 adjoint's dual sample
+// (T = double or an FP64 dual): fluid_from_prims's quantities from one
+// reciprocal square root and two divisions where the template takes a
+// square root and six divisions (the mixed forms keep the template).  With
+// w = 1 + |V.V| and P = -g^00 w: u^0 = sqrt(P), the 1/u^0 of b^i is rsqrt(P)
+// and Vfac = sqrt(w / -g^00) = w rsqrt(P).  In the R-beta model beta = h / D
+// with h = 2u/3 and D = b^2 + tiny, so trat = N / Q with
 // N = r_high h^2 + r_low D^2 and Q = h^2 + D^2; with A = N + Q and C = A + Q
 // the two quotients the model needs, (trat + 1)/(trat + 2) = A / C and
 // 1/(1 + trat) = Q / A, come from one reciprocal of A C.  D^2 >= 1e-40, so
 // no product underflows.
-__device__ __forceinline__ bool fluid_fp64(const double v[8], const MetricT<double>& g, double Ne_unit,
-                                           double B_unit, double r_high, double r_low, Fluid<double>& fl) {
+template <class T>
+__device__ __forceinline__ bool fluid_fast(const T v[8], const MetricT<T>& g, const T& Ne_unit, const T& B_unit,
+                                           const T& r_high, const T& r_low, Fluid<T>& fl) {
     const double tiny = 1.e-20;
-    const double rho = v[0], uu = v[1];
-    const double V1 = v[2], V2 = v[3], V3 = v[4];
-    const double Bp1 = v[5], Bp2 = v[6], Bp3 = v[7];
+    const T rho = v[0], uu = v[1];
+    const T V1 = v[2], V2 = v[3], V3 = v[4];
+    const T Bp1 = v[5], Bp2 = v[6], Bp3 = v[7];
     fl.ne = rho * Ne_unit;
-    const double VdotV = (g.d11 * V1 + 2.0 * g.d13 * V3) * V1 + g.d22 * V2 * V2 + g.d33 * V3 * V3;
-    const double w = 1.0 + fabs(VdotV);
-    const double P = -g.u00 * w;
-    const double iU0 = rsqrt(P);
-    const double Vfac = w * iU0;
-    double* U = fl.ucon;
+    const T VdotV = (g.d11 * V1 + 2.0 * g.d13 * V3) * V1 + g.d22 * V2 * V2 + g.d33 * V3 * V3;
+    const T w = 1.0 + fabs(VdotV);
+    const T P = -g.u00 * w;
+    const T iU0 = rsqrt(P);
+    const T Vfac = w * iU0;
+    T* U = fl.ucon;
     U[0] = P * iU0;
     U[1] = V1 - Vfac * g.u01;
     U[2] = V2;  // g^{02} = 0
     U[3] = V3;  // g^{03} = 0
-    double Ucov[4];
+    T Ucov[4];
     lowerT(g, U, Ucov);
-    const double UdotBp = Ucov[1] * Bp1 + Ucov[2] * Bp2 + Ucov[3] * Bp3;
-    double* Bc = fl.bcon;
+    const T UdotBp = Ucov[1] * Bp1 + Ucov[2] * Bp2 + Ucov[3] * Bp3;
+    T* Bc = fl.bcon;
     Bc[0] = UdotBp;
     Bc[1] = (Bp1 + U[1] * UdotBp) * iU0;
     Bc[2] = (Bp2 + U[2] * UdotBp) * iU0;
     Bc[3] = (Bp3 + U[3] * UdotBp) * iU0;
-    double Bcov[4];
+    T Bcov[4];
     lowerT(g, Bc, Bcov);
-    const double Bsq = Bc[0] * Bcov[0] + Bc[1] * Bcov[1] + Bc[2] * Bcov[2] + Bc[3] * Bcov[3];
+    const T Bsq = Bc[0] * Bcov[0] + Bc[1] * Bcov[1] + Bc[2] * Bcov[2] + Bc[3] * Bcov[3];
     fl.bsq = Bsq;
     fl.B = sqrt(Bsq) * B_unit + tiny;
     // R-beta electron temperature, raptor_harm_model.c:262-276
-    const double h = uu * (2.0 / 3.0), D = Bsq + tiny;
-    const double h2 = h * h, D2 = D * D;
-    const double Q = h2 + D2;
-    const double A = r_high * h2 + r_low * D2 + Q;
-    const double C = A + Q;
-    const double iAC = 1.0 / (A * C);
-    const double two_temp_gam = 0.5 * ((1.0 + 2.0 / 3.0 * (A * A * iAC)) + 4.0 / 3.0);
-    const double Thetae_unit = (two_temp_gam - 1.0) * (kPMass / kEMass) * (Q * C * iAC);
-    const double irho = 1.0 / rho;
-    double th = (uu * irho) * Thetae_unit;
-    if (th < 0.0) th = tiny;
+    const T h = uu * (2.0 / 3.0), D = Bsq + tiny;
+    const T h2 = h * h, D2 = D * D;
+    const T Q = h2 + D2;
+    const T A = r_high * h2 + r_low * D2 + Q;
+    const T C = A + Q;
+    const T iAC = 1.0 / (A * C);
+    const T two_temp_gam = 0.5 * ((1.0 + 2.0 / 3.0 * (A * A * iAC)) + 4.0 / 3.0);
+    const T Thetae_unit = (two_temp_gam - 1.0) * (kPMass / kEMass) * (Q * C * iAC);
+    const T irho = 1.0 / rho;
+    fl.irho = irho;
+    T th = (uu * irho) * Thetae_unit;
+    if (th < 0.0) th = T(tiny);
     fl.thetae = th;
     return !(Bsq * irho > 1.0);  // the sigma cut, b^2 / rho > 1
 }
@@ -248,7 +253,7 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     double v[8];
     interp_prims(im.cells64, im.n2, cc, v);
     Fluid<double> fl;
-    if (!fluid_fp64(v, g, im.Ne_unit, im.B_unit, im.r_high, im.r_low, fl)) return false;
+    if (!fluid_fast<double>(v, g, im.Ne_unit, im.B_unit, im.r_high, im.r_low, fl)) return false;
 
     const double k[4] = {y[4], y[5], y[6], y[7]};
     double kd[4];

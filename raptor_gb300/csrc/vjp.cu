@@ -61,10 +61,13 @@ __device__ __forceinline__ D3 lift(const D1& a) {
 // j_nu.c:130-153, 188-200) up to the frequency loop.
 struct SampleCommon {
     D3 kU;        // k_mu u^mu
-    D3 nus;       // nu_s
-    D3 pre;       // n_e sqrt(2) pi nu_s / (3 K2), the first factors of j
+    D3 inus;      // 1 / nu_s
+    D3 ikU2;      // 1 / (k.u)^2: 1/nu_p^2 = ikU2 / nu^2
+    D3 pre;       // n_e sqrt(2) pi nu_s e2_c / (3 K2), the first factors of j
     D3 hkt;       // h / (k_B T): h nu / (k_B T) per Hz
     D3 adl;       // |d lambda|
+    double nus;   // nu_s
+    double ikU;   // 1 / (k.u)
     SampleScalars ss;
     bool emits;
 };
@@ -101,14 +104,13 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = c0 * a[q] + c1 * b[q] + c2 * e[q] + c3 * f[q];
 
-    const D3 B_unit(im.B_unit);
     Fluid<D3> fl;
-    if (!fluid_from_prims(v, g, D3(im.Ne_unit), B_unit, D3(im.r_high), D3(im.r_low), fl)) return false;
-    out.ss.irho = 1.0 / v[0].v;
-    thetae_log_derivs(v[0].v, v[1].v, fl.bsq.v, im.r_high, im.r_low, out.ss.dlnth);
+    if (!fluid_fast(v, g, D3(im.Ne_unit), D3(im.B_unit), D3(im.r_high), D3(im.r_low), fl)) return false;
+    out.ss.irho = fl.irho.v;
+    thetae_log_derivs_fp64(fl.irho.v, v[1].v, fl.bsq.v, im.r_high, im.r_low, out.ss.dlnth);
     // pitch_angle divides by |k.u| B / B_unit, the field in code units, which
     // M_unit does not move: formed before B takes its ln B direction
-    const D3 Bcode = fl.B / B_unit;
+    const D3 Bcode = fl.B * im.inv_B_unit;
     fl.thetae.d[kSLnTh] = fl.thetae.v;
     fl.B.d[kSLnB] = fl.B.v - 1.e-20;  // B = sqrt(Bsq) B_unit + tiny: the part that scales
 
@@ -118,16 +120,25 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
     const D3* U = fl.ucon;
     const D3* Bc = fl.bcon;
     out.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    D3 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * Bcode);
+    // 1/(k.u |B|) gives the cosine's 1/(|k.u| |B|) and 1/(k.u), as in the
+    // FP64 sample (rt_terms_fp64)
+    const D3 ikB = 1.0 / (out.kU * Bcode);
+    D3 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) * fabs(ikB);
     if (fabs(pitch.v) > 1.0) pitch = D3(pitch.v > 0 ? 1.0 : -1.0);
     const D3 s2 = 1.0 - pitch * pitch;
     const D3 sth = s2.v > 0.0 ? sqrt(s2) : D3(0.0);
     const D3 nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
-    out.nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
+    const D3 nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;
     out.emits = (fabs(sth.v) >= 1.e-10) && (fl.thetae.v > 1e-4);
-    const D3 K2 = 2.0 * fl.thetae * fl.thetae;
-    out.pre = fl.ne * (1.4142135623730951 * CUDART_PI) * out.nus / (3.0 * K2);
+    // n_e sqrt(2) pi nu_s e2_c / (3 K2) with K2 = 2 Theta^2 and nu_s / Theta^2
+    // = (2/9) nu_c sin(theta)
+    out.pre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0 * (2.0 / 9.0) * kE2C) * (nuc * sth);
     out.hkt = (kPlanck / (kEMass * kC * kC)) / fl.thetae;
+    out.inus = 1.0 / nus;
+    out.nus = nus.v;
+    const D3 ikU = ikB * Bcode;
+    out.ikU = ikU.v;
+    out.ikU2 = ikU * ikU;
     out.adl = lift(adl1);
     return true;
 }
@@ -142,17 +153,22 @@ __device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommo
     if (nup.v <= 0.0) nup = D3(1.0);
     if (sc.emits && nup.v != 1.0) {
         const D3 dlf = sc.adl * im.rg_over_nu[fi];
-        const D3 X = nup / sc.nus;
-        const D3 cb = cbrt(X);
-        const D3 sq = sqrt(cb) * (cb + 1.8877486253633869);  // X^1/2 + 2^(11/12) X^1/6
-        const D3 jn = sc.pre * (sq * sq) * exp(-cb) * kE2C;
-        const D3 ex = exp(sc.hkt * nup) - 1.0;
-        const D3 inup2 = 1.0 / (nup * nup);
+        const D3 X = nup * sc.inus;
+        // the tangents of X^1/3 and X^1/6 through 1/X = nu_s / nu_p, 1/nu_p =
+        // -nu / (k.u nu^2): d X^1/3 = X^1/3 / (3X), d sqrt(c) = sqrt(c) c^2 / (2X)
+        const double iX = sc.nus * (-sc.ikU * (im.freq[fi] * im.inv_freq2[fi]));
+        const double cv = cbrt(X.v);
+        const D3 cb = chain(X, cv, cv * iX * (1.0 / 3.0));
+        const double sv = sqrt(cv);
+        const D3 sq = chain(cb, sv, 0.5 * sv * (cv * cv * iX)) * (cb + 1.8877486253633869);  // X^1/2 + 2^(11/12) X^1/6
+        const D3 jn = sc.pre * (sq * sq) * fast_exp(-cb);
+        const D3 ex = fast_exp(sc.hkt * nup) - 1.0;
+        const D3 inup2 = sc.ikU2 * im.inv_freq2[fi];
         dtau = jn * (kE2CH * kC * kC / (2.0 * kE2C)) * ex * inup2 * dlf;
         S = jn * inup2 * dlf;
         return 1;
     }
-    const double ex = exp(sc.hkt.v * nup.v) - 1.0;
+    const double ex = fast_exp(sc.hkt.v * nup.v) - 1.0;
     return !(ex < CUDART_INF) ? 2 : 0;
 }
 
@@ -169,7 +185,7 @@ __device__ __forceinline__ void consume_term(int kind, const D3& S, const D3& dt
         tau += dt.v;
 #pragma unroll
         for (int q = 0; q < 4; ++q) dtg[q] += scalar_tangent(dt, ss, q);
-        const double e = exp(-tau);
+        const double e = fast_exp(-tau);
         const bool gate = tau < 6.907755278982137 && !(tau < 0.0);
         const double suffix = Itot - Ipart;
         const double eS = gate ? e : 0.0;

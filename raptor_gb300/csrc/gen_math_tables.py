@@ -100,14 +100,14 @@ def main():
     write_df_tables(os.path.dirname(os.path.abspath(__file__)))
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "math_tables.inc")
     lines = ["// Generated by gen_math_tables.py - do not edit.", "",
-             "// 2^(j/64), j = 0..63", "__device__ const double kExp2Table[64] = {"]
-    for j in range(64):
-        lines.append(f"    {float(dexp(LN2 * j / 64))!r},")
+             "// 2^(j/128), j = 0..127", "__device__ const double kExp2Table[128] = {"]
+    for j in range(128):
+        lines.append(f"    {float(dexp(LN2 * j / 128))!r},")
     lines.append("};")
-    lines += ["", "// (sin(pi n/128), cos(pi n/128)), n = 0..255 (period 2 in the argument)",
-              "__device__ const double2 kSinCosPiTable[256] = {"]
-    for n in range(256):
-        s, c = dsincos(PI * n / 128)
+    lines += ["", "// (sin(pi n/512), cos(pi n/512)), n = 0..1023 (period 2 in the argument)",
+              "__device__ const double2 kSinCosPiTable[1024] = {"]
+    for n in range(1024):
+        s, c = dsincos(PI * n / 512)
         lines.append(f"    {{{float(s)!r}, {float(c)!r}}},")
     lines.append("};")
     open(out, "w").write("\n".join(lines) + "\n")

@@ -169,7 +169,9 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
 // get_fluid_params for the FP64 sample and the FP64 adjoint's dual sample
 // (T = double or an FP64 dual): fluid_from_prims's quantities from one
 // reciprocal square root and two divisions where the template takes a
-// square root and six divisions (the mixed forms keep the template).  With
+// square root and six divisions (the FP32 samples of the mixed forms and the
+// mixed-DF adjoint keep the template: in FP32 the D^2 of a weak field
+// underflows).  With
 // w = 1 + |V.V| and P = -g^00 w: u^0 = sqrt(P), the 1/u^0 of b^i is rsqrt(P)
 // and Vfac = sqrt(w / -g^00) = w rsqrt(P).  In the R-beta model beta = h / D
 // with h = 2u/3 and D = b^2 + tiny, so trat = N / Q with

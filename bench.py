@@ -152,7 +152,7 @@ def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, re
     ms_image = t * 1e3 * (W * H) / len(pix)
     return ms_image, {"kind": kind, "cores": threads, "rays": int(len(pix)), "stride": stride,
                       "seconds": t, "times": times,
-                      "sample": f"every {stride}th pixel of the 1024x1024 image ({len(pix)} rays), "
+                      "sample": f"one pixel in {stride} of the 1024x1024 image ({len(pix)} rays), "
                                 f"{threads} OpenMP threads, extrapolated to the full image"}
 
 

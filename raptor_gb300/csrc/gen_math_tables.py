@@ -44,6 +44,15 @@ def dsincos(x):
             return s, c
 
 
+def sincospi_entry(n, half):
+    """sin and cos of pi n / half, exact at the multiples of pi/2, where the
+    series of the truncated pi leaves residues of order 1e-46 instead of 0."""
+    if (2 * n) % half == 0:
+        return [(Decimal(0), Decimal(1)), (Decimal(1), Decimal(0)),
+                (Decimal(0), Decimal(-1)), (Decimal(-1), Decimal(0))][(2 * n // half) % 4]
+    return dsincos(PI * n / half)
+
+
 def f32(x):
     """Round a Decimal to the nearest FP32 value (through an exact double
     near it; a double-rounding tie changes hi by one ulp and lo absorbs it)."""
@@ -70,7 +79,7 @@ def write_df_tables(here):
     lines += ["", "// (sin hi, sin lo, cos hi, cos lo) of pi n/128, n = 0..255",
               "__device__ const float4 kSinCosPiTableDF[256] = {"]
     for n in range(256):
-        s, c = dsincos(PI * n / 128)
+        s, c = sincospi_entry(n, 128)
         sh, sl = split(s)
         ch, cl = split(c)
         lines.append(f"    {{{ffmt(sh)}, {ffmt(sl)}, {ffmt(ch)}, {ffmt(cl)}}},")
@@ -107,7 +116,7 @@ def main():
     lines += ["", "// (sin(pi n/512), cos(pi n/512)), n = 0..1023 (period 2 in the argument)",
               "__device__ const double2 kSinCosPiTable[1024] = {"]
     for n in range(1024):
-        s, c = dsincos(PI * n / 512)
+        s, c = sincospi_entry(n, 512)
         lines.append(f"    {{{float(s)!r}, {float(c)!r}}},")
     lines.append("};")
     open(out, "w").write("\n".join(lines) + "\n")

@@ -65,6 +65,8 @@ def test_sincospi_table_correctly_rounded(src):
     pairs = re.findall(r"\{([-0-9.e]+), ([-0-9.e]+)\}", body)
     assert n == 1024 and len(pairs) == 1024
     pi = Decimal("3.141592653589793238462643383279502884197")
+    quarter = [(Decimal(0), Decimal(1)), (Decimal(1), Decimal(0)), (Decimal(0), Decimal(-1)), (Decimal(-1), Decimal(0))]
     for k in range(1024):
-        s, c = _sincos(pi * k / 512)
+        # exact at the multiples of pi/2 (the series of a truncated pi leaves ~1e-40 there)
+        s, c = quarter[k // 256] if k % 256 == 0 else _sincos(pi * k / 512)
         assert float(pairs[k][0]) == float(s) and float(pairs[k][1]) == float(c), k

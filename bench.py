@@ -110,13 +110,16 @@ def make_scene():
     return synth.make_torus(n1=GRID_N, n2=GRID_N, a=0.9375)
 
 
-def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, reps=1):
-    """Time the reference's CPU algorithm on a strided pixel sample of the
-    1024x1024 image.  Uses the reference build if one loads here, else the
-    C port.  Returns (ms per full image, detail dict)."""
-    from oracle import port, ref
-    kind = "port"
-    threads = nthreads or os.cpu_count() or 1
+_REF_SESSION = {}
+
+
+def _reference_session(dump):
+    """The reference's stock (-Ofast, makefile:13-15) build set up on this
+    dump through its own read_model / init_model / set_constants, or None
+    where the reference cannot be built here (cached per process)."""
+    from oracle import ref
+    if "s" in _REF_SESSION:
+        return _REF_SESSION["s"]
     sess = None
     if ref.available(GRID_N, GRID_N, opt="stock"):
         try:
@@ -129,31 +132,51 @@ def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, re
             with quiet():
                 sess = ref.RefSession(path, model, 1e19, INCL, 3.0, 3.0, 0.0, n1=GRID_N, n2=GRID_N, workdir=tmp,
                                       opt="stock")
-            kind = "reference"
-        except Exception:
+        except Exception as e:  # noqa: BLE001
+            print(f"reference build unusable, timing the port: {e}", file=sys.stderr)
             sess = None
-            kind = "port"
+    _REF_SESSION["s"] = sess
+    return sess
+
+
+def cpu_sample_run(dump, n_rays_target=None, seconds_target=12.0, nthreads=0, reps=1, with_port=False):
+    """Time the reference's CPU implementation of the path on a strided pixel
+    sample of the 1024x1024 image with all host threads: the reference's own
+    C sources in their stock build (OpenMP over the pixels, as core.c:105's
+    pragma would), or the C port where the reference cannot be built.  With
+    with_port, the port is also timed on the same pixels.  Returns (ms per
+    full image, detail dict)."""
+    from oracle import port
+    threads = nthreads or os.cpu_count() or 1
+    sess = _reference_session(dump)
+    kind = "reference" if sess is not None else "port"
     scene = port.Scene(dump.geom, dump.prims, W, H, inclination=INCL, stepsize=EPS)
 
-    def run(pix):
-        if sess is not None:
+    def run(pix, which):
+        if which == "reference":
             return sess.render_pixels(pix, FREQ, threads)[1]
         return scene.render([FREQ], pixels=pix, nthreads=threads)[1]
 
     # pilot to size the sample for ~seconds_target of wall time
     pilot = np.arange(0, W * H, 997, dtype=np.int32)
-    t_pilot = run(pilot)
+    t_pilot = run(pilot, kind)
     if n_rays_target is None:
         n_rays_target = int(len(pilot) * seconds_target / max(t_pilot, 1e-3))
     stride = max(1, int(W * H / max(n_rays_target, 1)))
     pix = np.arange(0, W * H, stride, dtype=np.int32)
-    times = [run(pix) for _ in range(reps)]
+    times = [run(pix, kind) for _ in range(reps)]
     t = min(times)
     ms_image = t * 1e3 * (W * H) / len(pix)
-    return ms_image, {"kind": kind, "cores": threads, "rays": int(len(pix)), "stride": stride,
-                      "seconds": t, "times": times,
-                      "sample": f"one pixel in {stride} of the 1024x1024 image ({len(pix)} rays), "
-                                f"{threads} OpenMP threads, extrapolated to the full image"}
+    what = ("the reference's own sources, stock -Ofast build (makefile:13-15), OpenMP pixel loop"
+            if kind == "reference" else "the C port of the reference's path (reference not buildable here)")
+    det = {"kind": kind, "cores": threads, "rays": int(len(pix)), "stride": stride, "seconds": t, "times": times,
+           "sample": f"one pixel in {stride} of the 1024x1024 image ({len(pix)} rays), {threads} OpenMP threads, "
+                     f"extrapolated to the full image; {what}"}
+    if with_port and kind == "reference":
+        tp = run(pix, "port")
+        det["port_same_pixels_ms_per_image"] = tp * 1e3 * (W * H) / len(pix)
+        det["port_over_reference_time"] = tp / t
+    return ms_image, det
 
 
 def run_reference(args, rank):
@@ -165,26 +188,29 @@ def run_reference(args, rank):
     # warm-up: one short run per requested warm-up step
     for _ in range(args.warmup):
         cpu_sample_run(dump, n_rays_target=4096)
-    for _ in range(args.steps):
-        v, detail = cpu_sample_run(dump, seconds_target=args.ref_seconds)
+    for k in range(args.steps):
+        v, detail = cpu_sample_run(dump, seconds_target=args.ref_seconds, with_port=(k == args.steps - 1))
         vals.append(v)
     value = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "ms/image", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(),
+            "config": workload_config(args.gpus),
             "cpu_baseline": {"value": value, "unit": "ms/image", "cores": detail["cores"], "kind": detail["kind"],
-                             "sample": detail["sample"]},
+                             "sample": detail["sample"],
+                             "port_same_pixels_ms_per_image": detail.get("port_same_pixels_ms_per_image"),
+                             "port_over_reference_time": detail.get("port_over_reference_time")},
             "e2e": {"value": value, "unit": "ms/image", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def workload_config():
+def workload_config(n_gpus=1):
     return {"workload": "1024x1024 image at 230 GHz of a seeded 512x512 Fishbone-Moncrief torus "
                         "(a=0.9375, MKS hslope=0.3, Rout=40), inclination 60 deg, RK4 eps=0.05, "
                         "M_unit=1e19 g, R_high=R_low=3",
             "image": [W, H], "grid": [GRID_N, GRID_N], "inclination_deg": INCL, "freq_hz": FREQ, "stepsize": EPS,
-            "integrator": "RK4", "l2": "flushed between timed renders (512 MiB write)"}
+            "integrator": "RK4", "l2": "flushed between timed renders (512 MiB write)",
+            "parallelism": f"replicas{n_gpus}"}
 
 
 def run_vjp_config4(reps=3):
@@ -387,6 +413,15 @@ def run_differentiable(dev, n_cells=4, reps=2):
     }
 
 
+def pixel_error_summary(pe):
+    """Per-pixel relative errors of a mixed form against the FP64 image
+    (emitting pixels): median, maximum, and the fractions above 1e-3 and
+    1e-2 (the maximum alone is set by the faintest pixels)."""
+    return {"pixel_err_median": float(np.median(pe)), "pixel_err_max": float(np.max(pe)),
+            "frac_pixels_above_1e-3": float(np.mean(pe > 1e-3)), "frac_pixels_above_1e-2": float(np.mean(pe > 1e-2)),
+            "pixels_compared": int(pe.size)}
+
+
 def run_inclination(eng, blib, dev, gid, incl, forms, steps):
     """The headline image at another inclination (the workload's second
     angle): each form rendered `steps` times after an L2 flush (device time,
@@ -410,7 +445,7 @@ def run_inclination(eng, blib, dev, gid, incl, forms, steps):
         if name != "fp64":
             pe = np.abs(g["img"][nz] - ref["img"][nz]) / np.abs(ref["img"][nz])
             row.update(speedup_vs_fp64=ref["ms"] / g["ms"], flux_err_vs_fp64=abs(g["flux"] - ref["flux"]) / ref["flux"],
-                       pixel_err_median=float(np.median(pe)), pixel_err_max=float(np.max(pe)))
+                       **pixel_error_summary(pe))
         out[name] = row
     return out
 
@@ -531,9 +566,10 @@ def run_engine(args, rank, world, local):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        ms_cpu, det = cpu_sample_run(dump, seconds_target=args.ref_seconds)
+        ms_cpu, det = cpu_sample_run(dump, seconds_target=args.ref_seconds, with_port=True)
         cpu = {"value": ms_cpu, "unit": "ms/image", "cores": det["cores"], "kind": det["kind"],
-               "sample": det["sample"]}
+               "sample": det["sample"], "port_same_pixels_ms_per_image": det.get("port_same_pixels_ms_per_image"),
+               "port_over_reference_time": det.get("port_over_reference_time")}
     eng.close()
     if rank != 0:
         return
@@ -542,7 +578,7 @@ def run_engine(args, rank, world, local):
         "metric": METRIC, "value": t_fp64 / n, "unit": "ms/image", "n_gpus": n, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_fp64, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fishbone-Moncrief torus)",
-        "config": dict(workload_config(), parallelism=f"replicas{n}"),
+        "config": workload_config(n),
         "e2e": ({"value": t_e2e / n, "unit": "ms/image", "h2d_bytes_per_step": e2e_h2d,
                  "d2h_bytes_per_step": int(e2e_stats["d2h_bytes"]),
                  "path": "raptor_gpu_upload_grid (pinned host prims) + raptor_gpu_render (host image out)"}
@@ -565,10 +601,9 @@ def run_engine(args, rank, world, local):
                      "rt_samples": st["rt_samples"], "max_ray_steps": st["max_ray_steps"], "kk_max": st["kk_max"],
                      "launch": [st["block_size"], st["blocks_per_sm"], st["refill_interval"]]},
             "mixed": {"ms_per_image": t_mixed, "speedup_vs_fp64": t_fp64 / t_mixed, "flux_err_vs_fp64": flux_err,
-                      "pixel_err_median": float(np.median(pix_err)), "pixel_err_max": float(np.max(pix_err))},
+                      **pixel_error_summary(pix_err)},
             "mixed_df": {"ms_per_image": t_mixed_df, "speedup_vs_fp64": t_fp64 / t_mixed_df,
-                         "flux_err_vs_fp64": flux_err_df, "pixel_err_median": float(np.median(pix_err_df)),
-                         "pixel_err_max": float(np.max(pix_err_df)), "kk_max": kk_df,
+                         "flux_err_vs_fp64": flux_err_df, **pixel_error_summary(pix_err_df), "kk_max": kk_df,
                          "geodesic": "double-float (FP32 pairs, 48-bit significand)",
                          "kernel_ms": k_df,
                          # the same algorithmic FLOP count as the FP64 form, per second of the DF kernel

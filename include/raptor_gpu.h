@@ -13,9 +13,10 @@
  *
  * Plain C types only.  The caller owns every host buffer; device memory
  * belongs to the context and never crosses this interface.  Every call
- * blocks until its results are on the host, returns RAPTOR_OK (0) or a
- * negative status, and never exits the process (unlike core.c:15 or
- * raptor_harm_model.c:84).  One context per host thread.
+ * blocks until its results are on the host, returns RAPTOR_OK (0), a
+ * positive warning (the results are complete) or a negative error, and never
+ * exits the process (unlike core.c:15 or raptor_harm_model.c:84).  One
+ * context per host thread.
  */
 #ifndef RAPTOR_GPU_H
 #define RAPTOR_GPU_H
@@ -37,6 +38,17 @@ extern "C" {
 #define RAPTOR_ERR_DEVICE (-3)   /* the kernels flagged an error (see last_error) */
 #define RAPTOR_ERR_NOMEM (-4)    /* device or pinned allocation failed */
 #define RAPTOR_ERR_NODEVICE (-5) /* no usable sm_103 device */
+/* (-6 is RAPTOR_ERR_NOALLOC_LIMIT, below) */
+#define RAPTOR_ERR_NONFINITE (-7) /* a render finished, but rays ended with a non-finite photon
+                                     state or intensity (the stats count them in n_nonfinite).
+                                     The outputs are written, each such pixel as its ray left
+                                     it; the reference renders these without notice (a camera
+                                     at inclination exactly 0 gives NaN wave vectors at
+                                     metric.c:662-668, 0 * inf, and an empty image). */
+#define RAPTOR_WARN_STEPCAP 1 /* a warning, not an error: the render is complete, but rays
+                                 stopped at the step cap (max_steps, parameters.h:182), as the
+                                 reference stops them without notice (integrator.c:228); the
+                                 stats count them in n_stepcap.  Text in last_error. */
 
 /* arithmetic forms */
 #define RAPTOR_PREC_FP64 0  /* everything FP64, the reference's arithmetic */
@@ -108,7 +120,7 @@ typedef struct raptor_gpu_stats {
     long long rt_samples; /* calls that passed the sigma cut (emission evaluated) */
     long long max_ray_steps;
     long long n_stepcap;  /* rays stopped by max_steps (parameters.h:182) */
-    long long n_nonfinite;
+    long long n_nonfinite; /* rays that ended with a non-finite photon state or intensity */
     double kk_max;        /* max |g k k| / (k^t)^2 over rays at termination */
     int block_size, blocks_per_sm, refill_interval, grid_blocks;
     int graph_replayed;
@@ -170,8 +182,9 @@ long long raptor_gpu_output_size(const raptor_image_desc *imgs, int n_imgs);
 long long raptor_gpu_spectrum_size(const raptor_image_desc *imgs, int n_imgs);
 
 /* Statistics of the last render or VJP on this context (for a VJP: the
- * adjoint pass's counters; kernel_ms is the adjoint pass, device_ms forward
- * plus adjoint). */
+ * adjoint pass's counters with the forward render's n_stepcap and
+ * n_nonfinite; kernel_ms is the adjoint pass, device_ms forward plus
+ * adjoint). */
 int raptor_gpu_get_stats(const raptor_gpu_ctx *ctx, raptor_gpu_stats *out);
 
 /* Per-step record of one ray, the engine's form of the reference's GEOD
@@ -209,13 +222,18 @@ int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precis
  *   d_I_out         device memory, raptor_gpu_output_size(imgs, n_imgs) doubles
  *   d_spectrum_out  device memory, raptor_gpu_spectrum_size doubles, or NULL
  *   stream          a cudaStream_t, or NULL for the default stream
- * Returns when the results are in device memory.  Its scratch (ray queue,
- * counters, descriptors: RAPTOR_NOALLOC_SCRATCH_BYTES) is one fixed device
- * array in the library that every GPU loading the library keeps until exit;
- * its device address is looked up on the first call on each device, so make
- * that first call before any stream capture.  All calls share the array:
- * calls whose GPU work overlaps race on it and must be serialised by the
- * caller.  A batch larger than RAPTOR_NOALLOC_MAX_IMAGES is rejected with
+ * The call synchronises `stream` and returns when the results are in device
+ * memory, with raptor_gpu_render's statuses.  It makes `device` current while
+ * it runs and gives the caller's current device back before it returns.  Its
+ * scratch (ray queue, counters, descriptors: RAPTOR_NOALLOC_SCRATCH_BYTES) is
+ * one fixed device array in the library that every GPU loading the library
+ * keeps until exit.  The first call on each device (and the first after that
+ * device's context was re-created, e.g. by cudaDeviceReset) looks up the
+ * array's device address with cudaGetSymbolAddress: make that first call
+ * before any stream capture begins.  All calls share the array, which keeps
+ * the last call's contents (each call clears its counters first): calls whose
+ * GPU work overlaps race on it and must be serialised by the caller.  A batch
+ * larger than RAPTOR_NOALLOC_MAX_IMAGES is rejected with
  * RAPTOR_ERR_NOALLOC_LIMIT; other bad arguments with RAPTOR_ERR_INVALID. */
 #define RAPTOR_NOALLOC_MAX_IMAGES 16
 #define RAPTOR_NOALLOC_SCRATCH_BYTES 16384

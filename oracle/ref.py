@@ -8,9 +8,11 @@ reference makefile's flags) is only timed.  This module is
 imported only by tests/, by tests/golden/make_golden.py and by bench.py's
 CPU-baseline leg; the engine never calls it.
 
-The reference sources exist only where they were mounted; on a machine
-without them `available()` is False and callers fall back to the C port
-(oracle/port.py).
+The reference's sources are read from oracle/_ref/src, a git-ignored copy
+that `stage()` (make -C oracle stage) takes from a reference checkout, so
+the same build runs wherever that directory travels; RAPTOR_REFERENCE_DIR
+names another source directory.  Without sources `available()` is False
+and callers fall back to the C port (oracle/port.py).
 """
 from __future__ import annotations
 
@@ -23,12 +25,20 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC_DIR = os.environ.get("RAPTOR_REFERENCE_DIR", "/root/reference")
+STAGED_DIR = os.path.join(HERE, "_ref", "src")
+REF_SRC_DIR = os.environ.get("RAPTOR_REFERENCE_DIR", STAGED_DIR)
 _LIBS: dict = {}
 
 
 def sources_present() -> bool:
     return os.path.isfile(os.path.join(REF_SRC_DIR, "integrator.c"))
+
+
+def stage(reference_dir: str) -> str:
+    """Copy the reference's C sources and headers from reference_dir into
+    oracle/_ref/src (git-ignored).  Returns the staged directory."""
+    subprocess.run(["make", "-s", "-C", HERE, "stage", f"REFERENCE={reference_dir}"], check=True)
+    return STAGED_DIR
 
 
 def lib_path(n1: int, n2: int, rk: str = "RK4", opt: str = "ieee", cam: str = "linear") -> str:

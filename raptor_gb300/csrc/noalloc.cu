@@ -17,11 +17,11 @@
 // All calls share it, so two calls whose work overlaps on the GPU (on
 // different streams, or from different host threads) race on it and must
 // be serialised by the caller.
+#include <cuda.h>  // CUcontext and CUresult only: the driver is reached through cudart
 #include <cuda_runtime.h>
 
 #include <cstring>
 #include <mutex>
-#include <vector>
 
 #include "engine_internal.h"
 #include "ray_kernel.cuh"
@@ -33,49 +33,87 @@ namespace {
 constexpr size_t kCountersBytes = 256;  // kCtrCount 64-bit counters, padded
 constexpr size_t kDescBytes = sizeof(DevImage) * RAPTOR_NOALLOC_MAX_IMAGES;
 constexpr size_t kMapBytes = sizeof(int) * 2 * RAPTOR_NOALLOC_MAX_IMAGES * RAPTOR_MAX_FREQS;
+static_assert(kCountersBytes >= kCtrCount * sizeof(unsigned long long), "counters do not fit");
 static_assert(kCountersBytes + kDescBytes + kMapBytes <= RAPTOR_NOALLOC_SCRATCH_BYTES,
               "no-alloc scratch too small for its stated limits");
 
 // The scratch.  In host code this name is only a host-side handle: the
-// device address comes from cudaGetSymbolAddress, taken once per device.
+// device address comes from cudaGetSymbolAddress, taken once per device
+// context (below).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[RAPTOR_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch on `device`, looked up the first time this
-// device is used (with the device current, as cudaGetSymbolAddress needs).
+// The symbol's device address, looked up once per device and again whenever
+// that device's context is a different one (the primary context was reset
+// and re-created, which reloads the module and may move the array).  The
+// context is told apart by its process-unique id, read through the driver
+// entry points cudart exposes, so the library needs no link to the driver.
+struct ScratchSlot {
+    unsigned long long ctx_id = 0;
+    unsigned char* addr = nullptr;
+};
+std::mutex g_setup_mu;
+ScratchSlot g_scratch[kMaxDevices];
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// The current context's id, or 0 if it cannot be read.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {  // under g_setup_mu
+        looked_up = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *f1 = nullptr, *f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+        cudaGetLastError();
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&c) == CUDA_SUCCESS && c && get_id(c, &id) == CUDA_SUCCESS) return id;
+    return 0;
+}
+
+// Device address of the scratch on `device`, which must be current: the
+// set-up on the first call on a device (and on the first call after its
+// context was re-created), a cached pointer on every other call.  Where
+// the context id cannot be read, the address is looked up on every call.
 cudaError_t scratch_address(int device, unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_addr[device]) {
+    const unsigned long long id = current_context_id();
+    ScratchSlot& s = g_scratch[device];
+    if (id == 0 || s.ctx_id != id || !s.addr) {
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        g_scratch_addr[device] = static_cast<unsigned char*>(p);
+        s.addr = static_cast<unsigned char*>(p);
+        s.ctx_id = id;
     }
-    *out = g_scratch_addr[device];
+    *out = s.addr;
     return cudaSuccess;
 }
 
-__global__ void noalloc_spectrum_kernel(const DevImage* __restrict__ imgs, const int* __restrict__ spec_img,
-                                        const int* __restrict__ spec_f, const double* __restrict__ out,
-                                        double* __restrict__ spectrum) {
-    __shared__ double red[256];
-    const DevImage& im = imgs[spec_img[blockIdx.x]];
-    const int f = spec_f[blockIdx.x];
-    const long long npix = (long long)im.width * im.height;
-    const double* o = out + im.out_offset + f;
-    double acc = 0.0;
-    for (long long k = threadIdx.x; k < npix; k += blockDim.x) acc += o[k * im.nfreq];
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
+// Makes `device` current for the call and gives the caller's current device
+// back on every return path.
+struct DeviceGuard {
+    int saved = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&saved) != cudaSuccess) saved = -1;
+        ok = cudaSetDevice(device) == cudaSuccess;
     }
-    if (threadIdx.x == 0) spectrum[blockIdx.x] = red[0];
-}
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
 
 }  // namespace
 
@@ -85,7 +123,11 @@ extern "C" int raptor_gpu_render_noalloc(int device, const double* d_cells, cons
     if (!d_cells || !geom || !imgs || !d_I_out || n_imgs < 1) return RAPTOR_ERR_INVALID;
     if (n_imgs > RAPTOR_NOALLOC_MAX_IMAGES) return RAPTOR_ERR_NOALLOC_LIMIT;
     if (device < 0 || device >= kMaxDevices) return RAPTOR_ERR_INVALID;
-    if (cudaSetDevice(device) != cudaSuccess) return RAPTOR_ERR_NODEVICE;
+    DeviceGuard guard(device);
+    if (!guard.ok) {
+        cudaGetLastError();
+        return RAPTOR_ERR_NODEVICE;
+    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // Per-image constants, built on the host exactly as raptor_gpu_render
@@ -114,7 +156,10 @@ extern "C" int raptor_gpu_render_noalloc(int device, const double* d_cells, cons
         for (int f = 0; f < imgs[k].n_freq; ++f) h_map[nspec + s++] = f;
 
     unsigned char* scratch = nullptr;
-    if (scratch_address(device, &scratch) != cudaSuccess) return RAPTOR_ERR_CUDA;
+    if (scratch_address(device, &scratch) != cudaSuccess) {
+        cudaGetLastError();
+        return RAPTOR_ERR_CUDA;
+    }
     unsigned long long* d_ctr = reinterpret_cast<unsigned long long*>(scratch);
     DevImage* d_desc = reinterpret_cast<DevImage*>(scratch + kCountersBytes);
     int* d_map = reinterpret_cast<int*>(scratch + kCountersBytes + kDescBytes);
@@ -125,27 +170,29 @@ extern "C" int raptor_gpu_render_noalloc(int device, const double* d_cells, cons
         cudaMemcpyAsync(d_map, h_map, sizeof(int) * 2 * nspec, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return RAPTOR_ERR_CUDA;
 
+    // the FP64 form's default kernel and launch shape, as raptor_gpu_render
+    // picks them without tuning
     const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(max_nf, false, &fnp);
+    RayLaunchFn fn = pick_ray_kernel(max_nf, RAPTOR_PREC_FP64, &fnp);
     int occ = 1, sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fnp, 128, 0) != cudaSuccess)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fnp, kRayMaxBlock, 0) != cudaSuccess)
         return RAPTOR_ERR_CUDA;
     LaunchShape ls;
-    ls.block = 128;
+    ls.block = kRayMaxBlock;
     ls.bps = occ > 0 ? occ : 1;
     ls.grid = sms * ls.bps;
-    ls.refill = 1;
+    ls.refill = kDefaultRefill;
     fn(ls, st, d_desc, n_imgs, 0, rays, d_ctr, d_I_out, TraceSpec{-1, nullptr, 0});
     if (cudaGetLastError() != cudaSuccess) return RAPTOR_ERR_CUDA;
     if (d_spectrum_out) {
-        noalloc_spectrum_kernel<<<nspec, 256, 0, st>>>(d_desc, d_map, d_map + nspec, d_I_out, d_spectrum_out);
+        spectrum_kernel<<<nspec, 256, 0, st>>>(d_desc, d_map, d_map + nspec, d_I_out, d_spectrum_out);
         if (cudaGetLastError() != cudaSuccess) return RAPTOR_ERR_CUDA;
     }
     unsigned long long ctr[kCtrCount];
     if (cudaMemcpyAsync(ctr, d_ctr, sizeof ctr, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return RAPTOR_ERR_CUDA;
-    if ((long long)ctr[kCtrRays] != rays) return RAPTOR_ERR_DEVICE;
-    return RAPTOR_OK;
+    return render_status(nullptr, (long long)ctr[kCtrRays], rays, (long long)ctr[kCtrNonFinite],
+                         (long long)ctr[kCtrStepCap]);
 }

@@ -492,9 +492,8 @@ LaunchShape default_shape(raptor_gpu_ctx* ctx, const void* fn, int form) {
     int bps = ctx->opt.blocks_per_sm > 0 ? std::min(ctx->opt.blocks_per_sm, occ) : occ;
     ls.grid = ctx->num_sms * bps;
     ls.bps = bps;
-    // lanes refill every 8 steps (FP64 geodesic: 1.3 % faster than every step
-    // at 1024^2) or 16 (mixed-DF: 2 % faster than 8)
-    ls.refill = ctx->opt.refill_interval > 0 ? ctx->opt.refill_interval : (form == RAPTOR_PREC_MIXED_DF ? 16 : 8);
+    ls.refill = ctx->opt.refill_interval > 0 ? ctx->opt.refill_interval
+                                             : (form == RAPTOR_PREC_MIXED_DF ? kDefaultRefillDF : kDefaultRefill);
     return ls;
 }
 
@@ -540,6 +539,22 @@ int collect_stats(raptor_gpu_ctx* ctx, bool timed) {
         CK(cudaEventElapsedTime(&ms, ctx->evA, ctx->evB));
         s.device_ms = ms;
     }
+    return RAPTOR_OK;
+}
+
+// Status of a finished render from its counters (ray retirement checked
+// first): rays that ended non-finite make it an error, rays stopped by the
+// step cap a warning; the outputs are complete either way.
+int render_status(raptor_gpu_ctx* ctx, long long rays, long long expected, long long n_nonfinite,
+                  long long n_stepcap) {
+    if (rays != expected)
+        return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "ray kernel retired %lld rays, expected %lld", rays, expected);
+    if (n_nonfinite > 0)
+        return ctx_fail(ctx, RAPTOR_ERR_NONFINITE,
+                        "%lld of %lld rays ended with a non-finite photon state or intensity", n_nonfinite, rays);
+    if (n_stepcap > 0)
+        return ctx_fail(ctx, RAPTOR_WARN_STEPCAP, "%lld of %lld rays stopped at the step cap of %.0f steps",
+                        n_stepcap, rays, kMaxSteps);
     return RAPTOR_OK;
 }
 
@@ -635,9 +650,7 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     s.grid_blocks = ls.grid;
     s.graph_replayed = replayed ? 1 : 0;
     s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (s.rays != re - rb)
-        return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "ray kernel retired %lld rays, expected %lld", s.rays, re - rb);
-    return RAPTOR_OK;
+    return render_status(ctx, s.rays, re - rb, s.n_nonfinite, s.n_stepcap);
 }
 
 extern "C" int raptor_gpu_render(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs, int precision,

@@ -360,6 +360,7 @@ __device__ __forceinline__ void finish_ray(const DevImage& im, const RayState<NF
                                            double* __restrict__ out, RayCounters& c) {
     double* o = out + im.out_offset + (long long)s.pix * im.nfreq;
     const PixelScale ps = pixel_scale(im, s.pix % im.width);
+    bool finite = s.p.rp == s.p.rp && isfinite(s.y[5]);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
         if (f >= im.nfreq) break;
@@ -367,11 +368,12 @@ __device__ __forceinline__ void finish_ray(const DevImage& im, const RayState<NF
         if constexpr (MIXED) v = ((double)s.If[f] + (double)s.Ic[f]) * kE2C;
         else v = s.I[f];
         o[f] = scale_output(im, ps, v, f);
+        finite = finite && isfinite(o[f]);
     }
     c.steps += (unsigned long long)s.steps;
     c.rays += 1;
     if ((double)s.steps >= kMaxSteps) ++c.cap;
-    if (!(s.p.rp == s.p.rp) || !isfinite(s.y[5])) ++c.nan;
+    if (!finite) ++c.nan;  // a non-finite photon state or intensity
     c.max_steps = max(c.max_steps, (unsigned long long)s.steps);
     const double kk = null_drift(s.p, im.geo, s.y);
     if (kk == kk) c.kk_max = fmax(c.kk_max, kk);

@@ -175,15 +175,17 @@ __device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayState
                                               RayCounters& c) {
     double* o = out + im.out_offset + (long long)s.pix * im.nfreq;
     const PixelScale ps = pixel_scale(im, s.pix % im.width);
+    bool finite = s.p.rp.hi == s.p.rp.hi && isfinite(s.y[5].hi);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
         if (f >= im.nfreq) break;
         o[f] = scale_output(im, ps, ((double)s.If[f] + (double)s.Ic[f]) * kE2C, f);
+        finite = finite && isfinite(o[f]);
     }
     c.steps += (unsigned long long)s.steps;
     c.rays += 1;
     if ((double)s.steps >= kMaxSteps) ++c.cap;
-    if (!(s.p.rp.hi == s.p.rp.hi) || !isfinite(s.y[5].hi)) ++c.nan;
+    if (!finite) ++c.nan;  // a non-finite photon state or intensity
     c.max_steps = max(c.max_steps, (unsigned long long)s.steps);
     double yd[8];
 #pragma unroll

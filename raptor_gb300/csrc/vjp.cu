@@ -823,12 +823,15 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     s.rt_samples = (long long)ctr[kCtrRtSamples];
     s.vjp_terms = (long long)ctr[kCtrVjpEmit];
     s.vjp_gated_terms = (long long)ctr[kCtrVjpGate];
-    (void)fwd_ctr;
+    s.n_nonfinite = (long long)fwd_ctr[kCtrNonFinite];
+    s.n_stepcap = (long long)fwd_ctr[kCtrStepCap];
     s.block_size = kVjpBlock;
     s.grid_blocks = grid;
     s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if ((long long)ctr[kCtrRays] != b.total_rays)
         return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "vjp kernel retired %lld rays, expected %lld",
                         (long long)ctr[kCtrRays], b.total_rays);
-    return RAPTOR_OK;
+    // the forward render's status: its non-finite rays make the gradients
+    // meaningless, its step-capped rays are the reference's own behaviour
+    return render_status(ctx, (long long)fwd_ctr[kCtrRays], b.total_rays, s.n_nonfinite, s.n_stepcap);
 }

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import warnings
 from typing import Sequence
 
 import numpy as np
@@ -29,17 +30,26 @@ CAM_LINEAR = 0
 CAM_LOG = 1
 TRACE_WIDTH = 16
 
-STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "DEVICE", -4: "NOMEM", -5: "NODEVICE"}
+STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "DEVICE", -4: "NOMEM", -5: "NODEVICE", -6: "NOALLOC_LIMIT",
+          -7: "NONFINITE", 1: "WARN_STEPCAP"}
+ERR_NONFINITE = -7
+WARN_STEPCAP = 1
 
 EXPORTED = ("raptor_gpu_init", "raptor_gpu_destroy", "raptor_gpu_last_error", "raptor_gpu_upload_grid",
             "raptor_gpu_render", "raptor_gpu_render_range", "raptor_gpu_output_size",
-            "raptor_gpu_spectrum_size", "raptor_gpu_get_stats", "raptor_gpu_vjp", "raptor_gpu_trace_ray")
+            "raptor_gpu_spectrum_size", "raptor_gpu_get_stats", "raptor_gpu_vjp", "raptor_gpu_trace_ray",
+            "raptor_gpu_render_noalloc")
 
 
 class EngineError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"{STATUS.get(code, code)}: {msg}")
         self.code = code
+
+
+class EngineWarning(UserWarning):
+    """A positive status: the call's results are complete (for example, rays
+    stopped at the step cap, as the reference stops them)."""
 
 
 class Options(ctypes.Structure):
@@ -147,6 +157,7 @@ class Engine:
             raise EngineError(rc, "raptor_gpu_init failed (no usable sm_103 device?)")
         self.h = h
         self.grids = {}
+        self.last_status = 0
 
     def close(self):
         if getattr(self, "h", None):
@@ -160,8 +171,15 @@ class Engine:
             pass
 
     def _check(self, rc):
-        if rc != 0:
+        """Negative statuses raise EngineError; positive ones (warnings, the
+        results complete) issue an EngineWarning.  The status is kept in
+        last_status."""
+        self.last_status = rc
+        if rc < 0:
             raise EngineError(rc, self.lib.raptor_gpu_last_error(self.h).decode())
+        if rc > 0:
+            warnings.warn(EngineWarning(f"{STATUS.get(rc, rc)}: {self.lib.raptor_gpu_last_error(self.h).decode()}"),
+                          stacklevel=3)
 
     def upload_grid(self, geom: GridGeom, prims: np.ndarray, grid_id: int = -1) -> int:
         prims = np.ascontiguousarray(prims, dtype=np.float64)

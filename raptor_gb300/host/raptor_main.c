@@ -61,9 +61,13 @@ static int calculate_image_gpu(const raptor_model *m, const raptor_dump *d, cons
             img.freq[f] = freq[f];
         rc = raptor_gpu_render(ctx, &img, 1, m->precision, field, spectrum);
     }
-    if (rc != RAPTOR_OK) {
+    if (rc < 0) {
         fprintf(stderr, "engine error (%d): %s\n", rc, raptor_gpu_last_error(ctx));
     } else {
+        /* a positive status is a warning: the image is complete */
+        if (rc > 0)
+            fprintf(stderr, "engine warning (%d): %s\n", rc, raptor_gpu_last_error(ctx));
+        rc = RAPTOR_OK;
         raptor_gpu_stats st;
         raptor_gpu_get_stats(ctx, &st);
         printf("Done: 1e+02 %%, speed: %.3g [geodesics/sec] (%lld steps, kernel %.1f ms)\n",

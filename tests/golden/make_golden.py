@@ -51,6 +51,8 @@ def quiet():
     try:
         yield
     finally:
+        # flush C stdio's buffers while they still point at /dev/null
+        ctypes.CDLL(None).fflush(None)
         os.dup2(saved[0], 1)
         os.dup2(saved[1], 2)
         os.close(dn)

@@ -19,22 +19,34 @@ from tests.parity import assert_fp64_parity
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_render_matches_render(torus64):
-    torch = pytest.importorskip("torch")
+def _noalloc_lib():
     from raptor_gb300 import engine
     lib = engine.load()
     lib.raptor_gpu_render_noalloc.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(engine.GridGeomC),
                                               ctypes.POINTER(engine.ImageDesc), ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p]
     lib.raptor_gpu_render_noalloc.restype = ctypes.c_int
+    return lib
+
+
+@pytest.mark.parametrize("freqs", [([230e9], [230e9]), ([86e9, 230e9, 345e9], [140e9])],
+                         ids=["one_frequency", "three_and_one_frequencies"])
+def test_noalloc_render_matches_render(torus64, freqs):
+    """Two images per call; the second case gives the first image three
+    frequencies, so the spectrum map has image and frequency halves of
+    different lengths and the render takes the multi-frequency kernel."""
+    torch = pytest.importorskip("torch")
+    from raptor_gb300 import engine
+    lib = _noalloc_lib()
 
     # the reference result through the ordinary entry point
     eng = engine.Engine()
     gid = eng.upload_grid(torus64.geom, torus64.prims)
-    descs = [engine.image_desc(20, 14, [230e9], grid=gid, inclination=60.0),
-             engine.image_desc(9, 11, [230e9], grid=gid, inclination=150.0, m_unit=4e19)]
+    descs = [engine.image_desc(20, 14, freqs[0], grid=gid, inclination=60.0),
+             engine.image_desc(9, 11, freqs[1], grid=gid, inclination=150.0, m_unit=4e19)]
     want, want_spec = eng.render(descs, engine.PREC_FP64)
     eng.close()
+    n0 = 20 * 14 * len(freqs[0])
 
     # the caller's own device memory: grid as [n1][n2][8] cells, outputs
     g = torus64.geom
@@ -51,9 +63,10 @@ def test_noalloc_render_matches_render(torus64):
         rc = lib.raptor_gpu_render_noalloc(0, cells.data_ptr(), ctypes.byref(geom), arr, 2, out.data_ptr(),
                                            spec.data_ptr(), stream)
         assert rc == 0, f"call {call}: status {rc}"
+        assert torch.cuda.current_device() == 0
         got = out.cpu().numpy()
-        assert_fp64_parity(got[:280], want[:280], f"noalloc image 0, call {call}")
-        assert_fp64_parity(got[280:], want[280:], f"noalloc image 1, call {call}")
+        assert_fp64_parity(got[:n0], want[:n0], f"noalloc image 0, call {call}")
+        assert_fp64_parity(got[n0:], want[n0:], f"noalloc image 1, call {call}")
         np.testing.assert_allclose(spec.cpu().numpy(), want_spec, rtol=1e-6)
 
     # a batch beyond the stated maximum is refused, and nothing is launched

@@ -45,6 +45,24 @@ NOMINAL_FP64_TFLOPS = 1.25
 TRAFFIC_FP64_1024 = 17052160
 
 
+# ncu smsp__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum of one
+# mixed-DF ray-kernel launch (ray_kernel_df<1>) on the 1024x1024 workload:
+# the FP32 thread-instructions the double-float geodesic and the FP32 sample
+# execute (None: not captured for this build)
+FP32_INST_DF_1024 = None
+
+
+def df_roofline(kernel_ms, peak_tinst):
+    """The mixed-DF kernel against the FP32 pipe: FP32 thread-instructions
+    per launch (ncu) over the kernel's CUDA-event time, against an FFMA
+    throughput probe on the same GPU."""
+    inst = FP32_INST_DF_1024 if (W, H, GRID_N) == (1024, 1024, 512) else None
+    achieved = inst / (kernel_ms * 1e-3) / 1e12 if inst else None
+    return {"bound": "fp32", "achieved": achieved, "peak": peak_tinst, "unit": "T FP32 thread-inst/s",
+            "frac": achieved / peak_tinst if achieved and peak_tinst > 0 else None, "fp32_inst_per_launch": inst,
+            "peak_source": "measured FFMA loop on this GPU (FP32 lanes: 152 SMs x 128 x clock)"}
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -216,9 +234,9 @@ def workload_config(n_gpus=1):
 def run_vjp_config4(reps=3):
     """Adjoint configuration: 256x256 image of the 256x256 torus, loss = L2
     distance to a target at M_unit x 1.3, R = 4, i = 62 deg.  Reports, for
-    the FP64 form and for the mixed-DF form, the forward and VJP (forward
-    pass + adjoint pass) device times; the mixed-DF gradients are compared
-    with the FP64 ones."""
+    the FP64, mixed and mixed-DF forms, the forward and VJP (forward pass +
+    that form's adjoint pass) device times; the mixed and mixed-DF gradients
+    are compared with the FP64 ones."""
     from raptor_gb300 import engine, synth
     d = synth.make_torus(n1=256, n2=256)
     eng = engine.Engine()
@@ -229,7 +247,7 @@ def run_vjp_config4(reps=3):
     keys = ("d_m_unit", "d_r_high", "d_r_low", "d_inclination")
     out = {"config": "256x256 image, 256x256 torus, i=60, 230 GHz; loss to target at M_unit*1.3, R=4, i=62"}
     grads = {}
-    for prec, name in ((engine.PREC_FP64, "fp64"), (engine.PREC_MIXED_DF, "mixed_df")):
+    for prec, name in ((engine.PREC_FP64, "fp64"), (engine.PREC_MIXED, "mixed"), (engine.PREC_MIXED_DF, "mixed_df")):
         fwd, vjp = [], []
         for _ in range(reps):
             img, _ = eng.render(desc, prec)
@@ -238,8 +256,9 @@ def run_vjp_config4(reps=3):
             vjp.append(eng.stats()["device_ms"])
         f, v = min(fwd), min(vjp)
         out[name] = {"fwd_ms": f, "vjp_ms": v, "ratio": v / f, "grad": {k: grads[name][k] for k in keys}}
-    out["mixed_df"]["grad_rel_diff_vs_fp64"] = {
-        k: abs(grads["mixed_df"][k] - grads["fp64"][k]) / abs(grads["fp64"][k]) for k in keys}
+    for name in ("mixed", "mixed_df"):
+        out[name]["grad_rel_diff_vs_fp64"] = {
+            k: abs(grads[name][k] - grads["fp64"][k]) / abs(grads["fp64"][k]) for k in keys}
     eng.close()
     # the FP64 numbers stay at the top level
     out.update(fwd_ms=out["fp64"]["fwd_ms"], vjp_ms=out["fp64"]["vjp_ms"], ratio=out["fp64"]["ratio"])
@@ -295,15 +314,20 @@ def _loss_delta(op, om, target):
     return 0.5 * float(np.sum((op - om) * (op + om - 2.0 * target)))
 
 
-def run_differentiable(dev, n_cells=4, reps=2):
+def run_differentiable(dev, n_cells=4, reps=2, incl_hs=(1e-4, 1e-6, 1e-7)):
     """Large differentiable batch: a 2048x2048 image at 86/140/230/345/690 GHz
-    (with its spectrum) of the 512x512 torus.  Forward in the mixed form, then
-    the VJP of L = 1/2 |O - O_target|^2 (target at M_unit x 1.3, R = 4,
-    i = 62 deg) with respect to the scalars and the per-cell rho, u and
-    ln Theta_e fields.  Reports the forward and adjoint device times, the
-    engine's peak device memory, and agreement with central differences of
-    the FP64 forward (Richardson-extrapolated for the inclination) on the four
-    scalars and on rho and u of the n_cells cells with the largest gradient."""
+    (with its spectrum) of the 512x512 torus, and the VJP of
+    L = 1/2 |O - O_target|^2 (target at M_unit x 1.3, R = 4, i = 62 deg) with
+    respect to the four scalars and the per-cell rho, u and ln Theta_e
+    fields, in each form as a forward render and that form's adjoint pass:
+    mixed (the workload's: FP64 geodesic, FP32 transfer; its adjoint keeps
+    the FP64 path with FP32 tangents and the FP32 dual sample), FP64, and
+    mixed-DF.  Reports forward, adjoint and VJP device times, the engine's
+    peak device memory, and each form's gradients against central
+    differences of the FP64 forward: the four scalars (h = 1e-4 relative,
+    and the inclination also at the smaller incl_hs, where the piecewise
+    smooth loss reaches its derivative) and rho and u of the n_cells cells
+    with the largest gradient."""
     from raptor_gb300 import engine
     d = make_scene()
     freqs = [86e9, 140e9, 230e9, 345e9, 690e9]
@@ -313,29 +337,27 @@ def run_differentiable(dev, n_cells=4, reps=2):
     gid = eng.upload_grid(d.geom, d.prims)
     mk = lambda **o: engine.image_desc(n, n, freqs, grid=gid, **dict(base, **o))  # noqa: E731
     target, _ = eng.render(mk(m_unit=1.3e19, r_high=4.0, r_low=4.0, inclination=62.0), engine.PREC_MIXED)
-    fwd_ms = []
-    for _ in range(reps):
-        img, spec = eng.render(mk(), engine.PREC_MIXED)
-        fwd_ms.append(eng.stats()["device_ms"])
-    dl = img - target
-    adj_ms, vjp_ms = [], []
-    for _ in range(reps):
-        _, g = eng.vjp(mk(), dl, engine.PREC_MIXED)
-        st = eng.stats()
-        adj_ms.append(st["kernel_ms"])
-        vjp_ms.append(st["device_ms"])
+    forms = (("mixed", engine.PREC_MIXED), ("fp64", engine.PREC_FP64), ("mixed_df", engine.PREC_MIXED_DF))
+    res, grads = {}, {}
+    for name, prec in forms:
+        fwd_ms, adj_ms, vjp_ms = [], [], []
+        for _ in range(reps):
+            img, _ = eng.render(mk(), prec)
+            fwd_ms.append(eng.stats()["device_ms"])
+            _, g = eng.vjp(mk(), img - target, prec)
+            st = eng.stats()
+            adj_ms.append(st["kernel_ms"])
+            vjp_ms.append(st["device_ms"])
+        grads[name] = g
+        f, a, v = min(fwd_ms), min(adj_ms), min(vjp_ms)
+        res[name] = {"forward_ms": f, "adjoint_kernel_ms": a, "vjp_total_ms": v, "adjoint_over_forward": a / f,
+                     "vjp_total_over_forward": v / f}
+    res["fp64"]["adjoint"] = "FP64 geodesic with FP64 tangents, FP64 dual sample (sample pool)"
+    res["mixed"]["adjoint"] = "FP64 geodesic with FP32 tangents, FP32 dual sample"
+    res["mixed_df"]["adjoint"] = "double-float geodesic with FP32 tangents, FP32 dual sample"
     peak = eng.stats()["peak_device_bytes"]
-    # the same with the mixed-DF forward and its adjoint
-    fwd_df, adj_df, vjp_df = [], [], []
-    for _ in range(reps):
-        eng.render(mk(), engine.PREC_MIXED_DF)
-        fwd_df.append(eng.stats()["device_ms"])
-        _, gdf = eng.vjp(mk(), dl, engine.PREC_MIXED_DF)
-        st = eng.stats()
-        adj_df.append(st["kernel_ms"])
-        vjp_df.append(st["device_ms"])
 
-    # finite differences of the FP64 forward
+    # central differences of the FP64 forward
     def fd_scalar(key, rel, richardson):
         diffs = []
         for r in ((rel, rel / 2) if richardson else (rel,)):
@@ -345,25 +367,22 @@ def run_differentiable(dev, n_cells=4, reps=2):
             diffs.append(_loss_delta(op, om, target) / (2 * h))
         return diffs[0] if not richardson else (4 * diffs[1] - diffs[0]) / 3
 
+    def versus(fd, key):
+        return {"fd": fd, **{f"vjp_{nm}": grads[nm][key] for nm, _ in forms},
+                **{f"rel_err_{nm}": abs(grads[nm][key] - fd) / abs(fd) for nm, _ in forms}}
+
     t0 = time.perf_counter()
     scal = {}
-    for key, gk in (("m_unit", "d_m_unit"), ("r_high", "d_r_high"), ("r_low", "d_r_low"),
-                    ("inclination", "d_inclination")):
-        fd = fd_scalar(key, 1e-4, key == "inclination")
-        scal[key] = {"vjp": g[gk], "fd": fd, "rel_err": abs(g[gk] - fd) / abs(fd),
-                     "vjp_df": gdf[gk], "rel_err_df": abs(gdf[gk] - fd) / abs(fd)}
+    for key, gk in (("m_unit", "d_m_unit"), ("r_high", "d_r_high"), ("r_low", "d_r_low")):
+        scal[key] = versus(fd_scalar(key, 1e-4, False), gk)
     # the loss is only piecewise smooth in the inclination (clamps, min() in the
     # step size, cell-index changes along every ray): its difference quotient
     # reaches the derivative only as h shrinks
-    for rel in (1e-6, 1e-7):
-        fd = fd_scalar("inclination", rel, False)
-        scal[f"inclination_h{rel:g}"] = {"vjp": g["d_inclination"], "fd": fd,
-                                         "rel_err": abs(g["d_inclination"] - fd) / abs(fd),
-                                         "vjp_df": gdf["d_inclination"],
-                                         "rel_err_df": abs(gdf["d_inclination"] - fd) / abs(fd)}
+    for rel in incl_hs:
+        scal[f"inclination_h{rel:g}"] = versus(fd_scalar("inclination", rel, rel >= 1e-4), "d_inclination")
     cells = {}
-    order = np.argsort(-np.abs(g["d_rho"]).ravel())[:n_cells]
-    fd_all, vjp_all, vjp_all_df = [], [], []
+    order = np.argsort(-np.abs(grads["mixed"]["d_rho"]).ravel())[:n_cells]
+    fd_all, got_all = [], {nm: [] for nm, _ in forms}
     for flat in order:
         i, j = divmod(int(flat), d.geom.n2)
         for q, field in ((0, "d_rho"), (1, "d_u")):
@@ -376,50 +395,61 @@ def run_differentiable(dev, n_cells=4, reps=2):
             eng.upload_grid(d.geom, pr, grid_id=gid)
             om, _ = eng.render(mk(), engine.PREC_FP64)
             fd = _loss_delta(op, om, target) / (2e-4 * v)
-            cells[f"{field}[{i},{j}]"] = {"vjp": float(g[field][i, j]), "vjp_df": float(gdf[field][i, j]),
-                                          "fd": fd}
+            cells[f"{field}[{i},{j}]"] = {"fd": fd, **{f"vjp_{nm}": float(grads[nm][field][i, j]) for nm, _ in forms}}
             fd_all.append(fd)
-            vjp_all.append(float(g[field][i, j]))
-            vjp_all_df.append(float(gdf[field][i, j]))
+            for nm, _ in forms:
+                got_all[nm].append(float(grads[nm][field][i, j]))
     eng.upload_grid(d.geom, d.prims, grid_id=gid)
     fd_s = time.perf_counter() - t0
     scale = max(abs(x) for x in fd_all)
-    cell_err = max(abs(a - b) for a, b in zip(vjp_all, fd_all)) / scale
-    cell_err_df = max(abs(a - b) for a, b in zip(vjp_all_df, fd_all)) / scale
+    for nm, _ in forms:
+        res[nm]["cell_max_err_over_scale"] = max(abs(a - b) for a, b in zip(got_all[nm], fd_all)) / scale
+        res[nm]["scalar_max_rel_err"] = max(
+            scal[k][f"rel_err_{nm}"] for k in ("m_unit", "r_high", "r_low", f"inclination_h{min(incl_hs):g}"))
     # uniform Theta_e factor = change of T_p/T_e at R_high = R_low = R
     R = base["r_high"]
     tg = 0.5 * ((1.0 + 2.0 / 3.0 * (R + 1.0) / (R + 2.0)) + 4.0 / 3.0)
     dlnT_dR = (1.0 / 3.0) / (R + 2.0) ** 2 / (tg - 1.0) - 1.0 / (1.0 + R)
-    th_sum = float(np.sum(g["d_lnthetae"]))
-    th_want = (g["d_r_high"] + g["d_r_low"]) / dlnT_dR
+    for nm, _ in forms:
+        g = grads[nm]
+        th_sum = float(np.sum(g["d_lnthetae"]))
+        th_want = (g["d_r_high"] + g["d_r_low"]) / dlnT_dR
+        res[nm]["thetae_sum_identity_rel_err"] = abs(th_sum - th_want) / abs(th_want)
     eng.close()
-    f, a, v = min(fwd_ms), min(adj_ms), min(vjp_ms)
+    m = res["mixed"]
     return {
-        "metric": "2048² x 5-frequency differentiable render: adjoint/forward time, peak device memory, "
+        "metric": "2048² x 5-frequency differentiable render: VJP/forward time, peak device memory, "
                   "finite-difference agreement",
         "config": {"workload": "2048x2048 image at 86/140/230/345/690 GHz with spectrum, 512x512 torus a=0.9375, "
                                "i=60, M_unit=1e19, R_high=R_low=3; loss to target at M_unit*1.3, R=4, i=62",
-                   "forward": "mixed", "adjoint": "fp64 (forward-mode tangents + suffix identity, no checkpoints)"},
-        "forward_ms": f, "adjoint_kernel_ms": a, "vjp_total_ms": v, "adjoint_over_forward": a / f,
-        "vjp_total_over_forward": v / f, "peak_device_bytes": peak,
-        "mixed_df": {"forward_ms": min(fwd_df), "adjoint_kernel_ms": min(adj_df), "vjp_total_ms": min(vjp_df),
-                     "vjp_total_over_forward": min(vjp_df) / min(fwd_df),
-                     "adjoint": "double-float geodesic and tangent, FP32 dual sample",
-                     "cell_max_err_over_scale": cell_err_df},
+                   "forward": "mixed", "adjoint": m["adjoint"] + " (forward-mode tangents + suffix identity, "
+                                                               "no checkpoints)"},
+        "forward_ms": m["forward_ms"], "adjoint_kernel_ms": m["adjoint_kernel_ms"], "vjp_total_ms": m["vjp_total_ms"],
+        "adjoint_over_forward": m["adjoint_over_forward"], "vjp_total_over_forward": m["vjp_total_over_forward"],
+        "peak_device_bytes": peak, "forms": res,
         "grad_values": int(3 * d.geom.n1 * d.geom.n2 + 4),
-        "fd": {"scalars": scal, "cells": cells, "cell_max_err_over_scale": cell_err,
-               "thetae_field_sum": th_sum, "thetae_sum_identity": th_want,
-               "thetae_rel_err": abs(th_sum - th_want) / abs(th_want), "seconds": fd_s},
+        "fd": {"scalars": scal, "cells": cells, "seconds": fd_s, "h_rel": 1e-4},
     }
 
 
-def pixel_error_summary(pe):
-    """Per-pixel relative errors of a mixed form against the FP64 image
-    (emitting pixels): median, maximum, and the fractions above 1e-3 and
-    1e-2 (the maximum alone is set by the faintest pixels)."""
+def pixel_error_summary(img, ref):
+    """Per-pixel relative errors of a mixed form against the FP64 image: over
+    the emitting pixels the median, maximum and the fractions above 1e-3 and
+    1e-2; the same fractions over the pixels within six decades of the
+    brightest, which carry all but ~2e-6 of the flux (most emitting pixels
+    lie below that, some 30 decades down, where the FP32 emissivity's
+    exp(-X^1/3) underflows and relative errors reach 1); and the summed
+    absolute error over the flux."""
+    nz = ref != 0
+    pe = np.abs(img[nz] - ref[nz]) / np.abs(ref[nz])
+    br = ref >= 1e-6 * ref.max()
+    pb = np.abs(img[br] - ref[br]) / np.abs(ref[br])
     return {"pixel_err_median": float(np.median(pe)), "pixel_err_max": float(np.max(pe)),
             "frac_pixels_above_1e-3": float(np.mean(pe > 1e-3)), "frac_pixels_above_1e-2": float(np.mean(pe > 1e-2)),
-            "pixels_compared": int(pe.size)}
+            "pixels_compared": int(pe.size),
+            "bright_frac_above_1e-3": float(np.mean(pb > 1e-3)), "bright_frac_above_1e-2": float(np.mean(pb > 1e-2)),
+            "bright_pixel_err_max": float(np.max(pb)), "bright_pixels": int(pb.size),
+            "abs_err_sum_over_flux": float(np.sum(np.abs(img - ref)) / np.sum(ref))}
 
 
 def run_inclination(eng, blib, dev, gid, incl, forms, steps):
@@ -438,14 +468,12 @@ def run_inclination(eng, blib, dev, gid, incl, forms, steps):
         st = eng.stats()
         got[name] = dict(img=img, flux=float(spec[0]), ms=float(np.mean(ms)), kk=st["kk_max"], steps=st["steps"])
     ref = got["fp64"]
-    nz = ref["img"] != 0
     out = {"inclination_deg": incl}
     for name, g in got.items():
         row = {"ms_per_image": g["ms"], "kk_max": g["kk"], "steps": g["steps"]}
         if name != "fp64":
-            pe = np.abs(g["img"][nz] - ref["img"][nz]) / np.abs(ref["img"][nz])
             row.update(speedup_vs_fp64=ref["ms"] / g["ms"], flux_err_vs_fp64=abs(g["flux"] - ref["flux"]) / ref["flux"],
-                       **pixel_error_summary(pe))
+                       **pixel_error_summary(g["img"], ref["img"]))
         out[name] = row
     return out
 
@@ -458,6 +486,7 @@ def run_engine(args, rank, world, local):
     lib = eng.lib
     blib = ctypes.CDLL(os.path.join(ROOT, "raptor_gb300", "_lib", "libraptor_benchutil.so"))
     blib.raptor_bench_fp64_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    blib.raptor_bench_fp32_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     blib.raptor_bench_flush_l2.argtypes = [ctypes.c_int, ctypes.c_longlong]
     gid = eng.upload_grid(dump.geom, dump.prims)
     # each rank renders its own image (weak scaling): inclination offset per rank
@@ -513,10 +542,7 @@ def run_engine(args, rank, world, local):
     imgmx, specmx = eng.render(desc, engine.PREC_MIXED)
     imgdf, specdf = eng.render(desc, engine.PREC_MIXED_DF)
     kk_df = eng.stats()["kk_max"]
-    nz = img64 != 0
-    pix_err = np.abs(imgmx[nz] - img64[nz]) / np.abs(img64[nz])
     flux_err = abs(specmx[0] - spec64[0]) / spec64[0]
-    pix_err_df = np.abs(imgdf[nz] - img64[nz]) / np.abs(img64[nz])
     flux_err_df = abs(specdf[0] - spec64[0]) / spec64[0]
 
     # end to end through the C ABI with host buffers: grid upload (pinned) + render + image read-back
@@ -542,9 +568,11 @@ def run_engine(args, rank, world, local):
         barrier()
     e2e_stats = eng.stats()
 
-    # FP64 DFMA peak of this GPU (roofline denominator)
+    # FP64 DFMA and FP32 FFMA peaks of this GPU (roofline denominators)
     peak = ctypes.c_double(0.0)
     blib.raptor_bench_fp64_peak(dev, 5, ctypes.byref(peak))
+    peak32 = ctypes.c_double(0.0)
+    blib.raptor_bench_fp32_peak(dev, 5, ctypes.byref(peak32))
 
     st = results["fp64"]["stats"]
     t_fp64 = maxed(float(np.mean(results["fp64"]["device_ms"])))
@@ -558,11 +586,13 @@ def run_engine(args, rank, world, local):
     flop = workload.image_flops(st["rays"], st["steps"], st["rt_samples"], 1, rk4=True)
     achieved = flop / (k_fp64 * 1e-3) / 1e12
 
-    vjp = batch = incl17 = None
+    vjp = batch = incl17 = diff = None
     if not args.no_e2e:
         incl17 = run_inclination(eng, blib, dev, gid, 17.0, forms, args.steps)
         vjp = run_vjp_config4()
         batch = run_batch_config3(dev)
+        if not args.no_differentiable:
+            diff = run_differentiable(dev, n_cells=2, reps=1, incl_hs=(1e-7,))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -601,19 +631,20 @@ def run_engine(args, rank, world, local):
                      "rt_samples": st["rt_samples"], "max_ray_steps": st["max_ray_steps"], "kk_max": st["kk_max"],
                      "launch": [st["block_size"], st["blocks_per_sm"], st["refill_interval"]]},
             "mixed": {"ms_per_image": t_mixed, "speedup_vs_fp64": t_fp64 / t_mixed, "flux_err_vs_fp64": flux_err,
-                      **pixel_error_summary(pix_err)},
+                      **pixel_error_summary(imgmx, img64)},
             "mixed_df": {"ms_per_image": t_mixed_df, "speedup_vs_fp64": t_fp64 / t_mixed_df,
-                         "flux_err_vs_fp64": flux_err_df, **pixel_error_summary(pix_err_df), "kk_max": kk_df,
+                         "flux_err_vs_fp64": flux_err_df, **pixel_error_summary(imgdf, img64), "kk_max": kk_df,
                          "geodesic": "double-float (FP32 pairs, 48-bit significand)",
                          "kernel_ms": k_df,
                          # the same algorithmic FLOP count as the FP64 form, per second of the DF kernel
                          "algorithmic_tflops": flop / (k_df * 1e-3) / 1e12,
-                         "vs_fp64_dfma_peak": (flop / (k_df * 1e-3) / 1e12) / peak.value if peak.value > 0 else None,
+                         "roofline": df_roofline(k_df, peak32.value),
                          "launch": [results["mixed_df"]["stats"][k] for k in
                                     ("block_size", "blocks_per_sm", "refill_interval")]},
             "inclination_17": incl17,
             "vjp": vjp,
             "batch": batch,
+            "differentiable": diff,
         },
     }
     if cpu:
@@ -630,6 +661,8 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-differentiable", action="store_true",
+                    help="leave out the 2048x2048 5-frequency VJP leg (about two minutes)")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--workload", choices=("1024", "profile", "differentiable", "adjoint"), default="1024",
                     help="profile: a 256x256 image on a 256x256 torus, render timings only (for ncu captures); "

@@ -5,6 +5,8 @@
 
 Products (git-ignored, in-tree):
     raptor_gb300/_lib/libraptor_gpu.so   the C-ABI engine (include/raptor_gpu.h)
+    raptor_gb300/_lib/libraptor_gpu_checked.so  the same with device-side bounds
+                                          checks (-DRAPTOR_CHECKED, csrc/checked.cuh)
     raptor_gb300/_lib/libraptor_benchutil.so  FP64 peak probe and L2 flush for bench.py
     raptor_gb300/_lib/raptor_gb300       C host program, drop-in for `./RAPTOR`
 Translation units compile in parallel; one -gencode (sm_103a) only.
@@ -26,6 +28,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(ROOT, "_build", "obj")
 LIB = os.path.join(LIBDIR, "libraptor_gpu.so")
+LIB_CHECKED = os.path.join(LIBDIR, "libraptor_gpu_checked.so")
 BENCH_LIB = os.path.join(LIBDIR, "libraptor_benchutil.so")
 HOST_BIN = os.path.join(LIBDIR, "raptor_gb300")
 
@@ -55,11 +58,11 @@ def _headers():
            [os.path.join(INCLUDE, "raptor_gpu.h")]
 
 
-def _compile(src: str, verbose: bool) -> str:
-    obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+def _compile(src: str, verbose: bool, checked: bool = False) -> str:
+    obj = os.path.join(OBJDIR + ("_checked" if checked else ""), os.path.basename(src) + ".o")
     if not _deps_newer(obj, [src] + _headers()):
         return obj
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-DRAPTOR_CHECKED"] if checked else []) + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,18 +71,20 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
-def build_library(verbose: bool = False) -> str:
-    os.makedirs(OBJDIR, exist_ok=True)
+def build_library(verbose: bool = False, checked: bool = False) -> str:
+    """The engine library; checked: the bounds-checked build."""
+    lib = LIB_CHECKED if checked else LIB
+    os.makedirs(OBJDIR + ("_checked" if checked else ""), exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in CU_SOURCES]
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if _deps_newer(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        objs = list(ex.map(lambda s: _compile(s, verbose, checked), srcs))
+    if _deps_newer(lib, objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    return LIB
+    return lib
 
 
 def build_bench_util(verbose: bool = False) -> str:
@@ -110,17 +115,19 @@ def build_host(verbose: bool = False) -> str:
 
 
 def build(verbose: bool = False) -> str:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
         f_lib = ex.submit(build_library, verbose)
+        f_chk = ex.submit(build_library, verbose, True)
         f_bench = ex.submit(build_bench_util, verbose)
         lib = f_lib.result()
+        f_chk.result()
         f_bench.result()
     build_host(verbose)
     return lib
 
 
 def clean():
-    for p in (LIBDIR, OBJDIR):
+    for p in (LIBDIR, OBJDIR, OBJDIR + "_checked"):
         if os.path.isdir(p):
             shutil.rmtree(p)
 

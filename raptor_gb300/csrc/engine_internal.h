@@ -80,6 +80,7 @@ struct raptor_gpu_ctx {
     long long device_bytes = 0, peak_device_bytes = 0;  // cudaMalloc'd by this context
     cudaGraphExec_t graph_exec = nullptr;       // captured render, replayed while graph_key repeats
     std::string graph_key;
+    unsigned long long check_word = 0;  // the last render's check word (checked build)
     char err[512] = {0};
 };
 
@@ -96,7 +97,9 @@ LaunchShape choose_shape(raptor_gpu_ctx* ctx, const Batch& b, int form, RayLaunc
 int enqueue_render(raptor_gpu_ctx* ctx, const Batch& b, int form, long long rb, long long re,
                    const LaunchShape& ls, RayLaunchFn fn, bool timed, raptor::TraceSpec tr = {-1, nullptr, 0});
 int collect_stats(raptor_gpu_ctx* ctx, bool timed);
-// RAPTOR_ERR_DEVICE if the kernel retired other than `expected` rays, else
-// RAPTOR_ERR_NONFINITE / RAPTOR_WARN_STEPCAP / RAPTOR_OK from the counts
+// RAPTOR_ERR_DEVICE if the checked build recorded a failed check (check,
+// the counters' check word) or the kernel retired other than `expected`
+// rays, else RAPTOR_ERR_NONFINITE / RAPTOR_WARN_STEPCAP / RAPTOR_OK from the
+// counts
 int render_status(raptor_gpu_ctx* ctx, long long rays, long long expected, long long n_nonfinite,
-                  long long n_stepcap);
+                  long long n_stepcap, unsigned long long check);

@@ -3,6 +3,7 @@
 // metric.c:650-727 and BL_to_KS_u GRmath.c:135-184 that is common to all
 // pixels, set_units grmhd.c:17-33, set_constants utilities.c:17-26).
 #pragma once
+#include "checked.cuh"
 #include "kerr_mks.cuh"
 
 namespace raptor {
@@ -64,6 +65,10 @@ struct DevImage {
     GeoDF geo_df;
     DF inv_stepsize_df, cutoff_inner_df;
     DF startx1_df, startx2_df, stopx1_df, stopx2_df, idx1_df, idx2_df;
+    // the checked build's bounds (checked.cuh): one past the batch's last
+    // output double, and the word a failed check is recorded in
+    long long out_end;
+    unsigned long long* check_word;
 };
 
 // Per-step record of one traced ray (the analogue of the reference's GEOD

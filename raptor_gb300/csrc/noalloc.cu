@@ -163,6 +163,10 @@ extern "C" int raptor_gpu_render_noalloc(int device, const double* d_cells, cons
     unsigned long long* d_ctr = reinterpret_cast<unsigned long long*>(scratch);
     DevImage* d_desc = reinterpret_cast<DevImage*>(scratch + kCountersBytes);
     int* d_map = reinterpret_cast<int*>(scratch + kCountersBytes + kDescBytes);
+    for (int k = 0; k < n_imgs; ++k) {
+        h_desc[k].out_end = outlen;
+        h_desc[k].check_word = d_ctr + kCtrCheck;
+    }
 
     // the counters (ray queue first) must start at zero on every call
     if (cudaMemsetAsync(d_ctr, 0, kCountersBytes, st) != cudaSuccess ||
@@ -194,5 +198,5 @@ extern "C" int raptor_gpu_render_noalloc(int device, const double* d_cells, cons
         cudaStreamSynchronize(st) != cudaSuccess)
         return RAPTOR_ERR_CUDA;
     return render_status(nullptr, (long long)ctr[kCtrRays], rays, (long long)ctr[kCtrNonFinite],
-                         (long long)ctr[kCtrStepCap]);
+                         (long long)ctr[kCtrStepCap], ctr[kCtrCheck]);
 }

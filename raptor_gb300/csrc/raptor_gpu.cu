@@ -469,6 +469,10 @@ int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs
         }
         ctx->h_imgs_cap = n_imgs;
     }
+    for (int k = 0; k < n_imgs; ++k) {
+        b.host[k].out_end = b.out_len;
+        b.host[k].check_word = ctx->d_counters + kCtrCheck;
+    }
     memcpy(ctx->h_imgs, b.host.data(), sizeof(DevImage) * n_imgs);
     std::vector<int> map(2 * b.spec_len);
     for (int s = 0; s < b.spec_len; ++s) {
@@ -527,6 +531,7 @@ int collect_stats(raptor_gpu_ctx* ctx, bool timed) {
     s.n_stepcap = (long long)c[kCtrStepCap];
     s.n_nonfinite = (long long)c[kCtrNonFinite];
     s.max_ray_steps = (long long)c[kCtrMaxSteps];
+    ctx->check_word = c[kCtrCheck];
     s.vjp_terms = 0;  // render statistics: no adjoint terms
     s.vjp_gated_terms = 0;
     double kk;
@@ -542,11 +547,15 @@ int collect_stats(raptor_gpu_ctx* ctx, bool timed) {
     return RAPTOR_OK;
 }
 
-// Status of a finished render from its counters (ray retirement checked
-// first): rays that ended non-finite make it an error, rays stopped by the
-// step cap a warning; the outputs are complete either way.
+// Status of a finished render from its counters: a failed check of the
+// checked build, or a ray count other than expected, is a device error;
+// rays that ended non-finite make it an error, rays stopped by the step cap
+// a warning; the outputs are complete in these last two cases.
 int render_status(raptor_gpu_ctx* ctx, long long rays, long long expected, long long n_nonfinite,
-                  long long n_stepcap) {
+                  long long n_stepcap, unsigned long long check) {
+    if (check)
+        return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "checked build: %s (value %lld)", check_name(check),
+                        (long long)(check & 0x00ffffffffffffffull));
     if (rays != expected)
         return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "ray kernel retired %lld rays, expected %lld", rays, expected);
     if (n_nonfinite > 0)
@@ -650,7 +659,7 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     s.grid_blocks = ls.grid;
     s.graph_replayed = replayed ? 1 : 0;
     s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    return render_status(ctx, s.rays, re - rb, s.n_nonfinite, s.n_stepcap);
+    return render_status(ctx, s.rays, re - rb, s.n_nonfinite, s.n_stepcap, ctx->check_word);
 }
 
 extern "C" int raptor_gpu_render(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs, int precision,

@@ -30,6 +30,7 @@ enum : int {
     kCtrKkMax = 8,  // bits of a non-negative double, atomicMax as integer
     kCtrVjpEmit = 9,  // adjoint pass: emitting (sample, frequency) pairs
     kCtrVjpGate = 10, // adjoint pass: terms inside the tau gate
+    kCtrCheck = 11,   // the checked build's first failed check (checked.cuh), 0 if none
     kCtrCount = 16
 };
 
@@ -330,13 +331,19 @@ struct RayCounters {
     }
 };
 
-// A lane takes ray rid: its image, pixel, initial photon and zeroed transfer state.
+// A lane takes ray rid: its image, pixel, initial photon and zeroed transfer
+// state.  Returns the image, or null where the checked build finds the ray
+// outside the batch (the lane then drops it).
 template <int NF, bool MIXED>
 __device__ __forceinline__ const DevImage* start_ray(const DevImage* __restrict__ imgs, int n_imgs, long long rid,
                                                      RayState<NF, MIXED>& s) {
     s.img = find_image(imgs, n_imgs, rid);
+    if (!chk(s.img >= 0 && s.img < n_imgs, imgs[0].check_word, kChkImage, s.img)) return nullptr;
     const DevImage* im = imgs + s.img;
     s.pix = (int)(rid - im->ray_begin);
+    if (!chk(rid >= im->ray_begin && rid - im->ray_begin < (long long)im->width * im->height, im->check_word,
+             kChkPixel, rid))
+        return nullptr;
     s.rid = rid;
     const int px = s.pix % im->width, py = s.pix / im->width;
     init_photon(*im, camera_of(*im), px, py, s.y, s.beta);
@@ -358,12 +365,14 @@ __device__ __forceinline__ const DevImage* start_ray(const DevImage* __restrict_
 template <int NF, bool MIXED>
 __device__ __forceinline__ void finish_ray(const DevImage& im, const RayState<NF, MIXED>& s,
                                            double* __restrict__ out, RayCounters& c) {
-    double* o = out + im.out_offset + (long long)s.pix * im.nfreq;
+    const long long oi = im.out_offset + (long long)s.pix * im.nfreq;
+    const bool in_bounds = chk(oi >= 0 && oi + im.nfreq <= im.out_end, im.check_word, kChkOutput, oi);
+    double* o = out + oi;
     const PixelScale ps = pixel_scale(im, s.pix % im.width);
     bool finite = s.p.rp == s.p.rp && isfinite(s.y[5]);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-        if (f >= im.nfreq) break;
+        if (f >= im.nfreq || !in_bounds) break;
         double v;
         if constexpr (MIXED) v = ((double)s.If[f] + (double)s.Ic[f]) * kE2C;
         else v = s.I[f];
@@ -425,9 +434,12 @@ __global__ void __launch_bounds__(kRayMaxBlock, kRayMinBlocks)
             if (!active && live) {
                 const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
                 if (rid < ray_end) {
-                    im = start_ray(imgs, n_imgs, rid, s);
-                    active = true;
-                    if (TRACE && rid == tr.ray) trace_record<NF, MIXED>(tr, s, 0.0, 0);
+                    const DevImage* ri = start_ray(imgs, n_imgs, rid, s);
+                    if (ri) {
+                        im = ri;
+                        active = true;
+                        if (TRACE && rid == tr.ray) trace_record<NF, MIXED>(tr, s, 0.0, 0);
+                    }
                 } else {
                     live = false;
                 }
@@ -548,8 +560,9 @@ struct PoolLayout {
     static constexpr int kIn = 16;
     static constexpr int kOut = 1 + 2 * NF;
     static constexpr int kFields = kIn > kOut ? kIn : kOut;
-    // + the next-ticket links and image indices (two ints per entry)
-    static constexpr int kWarpDoubles = kFields * kPoolCap + kPoolCap;
+    // + the next-ticket links and image indices (two ints per entry), and in
+    // the checked build the owner lane of each entry
+    static constexpr int kWarpDoubles = kFields * kPoolCap + kPoolCap + (kChecked ? kPoolCap / 2 : 0);
 };
 
 template <int NF>
@@ -563,6 +576,8 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
     double* const fld = pool_mem + (threadIdx.x >> 5) * L::kWarpDoubles;
     int* const nxt = reinterpret_cast<int*>(fld + L::kFields * C);
     int* const timg = nxt + C;
+    int* const towner = timg + C;  // checked build only
+    unsigned long long* const cw = imgs[0].check_word;
     RayState<NF, false> s;
     int mode = 0;  // 0 idle, 1 stepping, 2 ended with tickets outstanding
     bool live = true;
@@ -583,8 +598,11 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
             if (mode == 0 && live) {
                 const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
                 if (rid < ray_end) {
-                    im = start_ray(imgs, n_imgs, rid, s);
-                    mode = 1;
+                    const DevImage* ri = start_ray(imgs, n_imgs, rid, s);
+                    if (ri) {
+                        im = ri;
+                        mode = 1;
+                    }
                 } else {
                     live = false;
                 }
@@ -608,6 +626,11 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
             }
         }
         const int t = ring.append(want, nxt, lane);
+        if (kChecked) {
+            chk(ring.tail - ring.head <= (unsigned)C, cw, kChkRing, (long long)(ring.tail - ring.head));
+            chk(ring.qn >= 0 && ring.qn <= C, cw, kChkList, ring.qn);
+            if (t >= 0) towner[t] = lane;
+        }
         if (t >= 0) {
             double* e = fld + t;
             e[0] = fabs(dl);
@@ -628,6 +651,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
         }
 
         const unsigned n = ring.batch(mode == 2, mode == 1);
+        chk(n <= 32u, cw, kChkBatch, n);
         if (n) {
             __syncwarp();
             if ((unsigned)lane < n) {
@@ -669,6 +693,7 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
                 const int ta = ring.ready();
                 if (!__any_sync(kFull, ta >= 0)) break;
                 if (ta >= 0) {
+                    if (kChecked) chk(towner[ta] == lane, cw, kChkList, ta);
                     const double* e = fld + ta;
                     double dtau[NF], jn[NF];
 #pragma unroll

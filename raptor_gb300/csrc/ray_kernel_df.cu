@@ -97,6 +97,9 @@ __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], 
     if (j < 0) { j = 0; d2 = 0.0f; }
     else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = 1.0f; }
     else d2 = add_f(t2, (float)-j).hi;
+    if (!chk(i >= 0 && i <= im.n1 - 2 && j >= 0 && j <= im.n2 - 2, im.check_word, kChkCell,
+             (long long)i * im.n2 + j))
+        i = j = 0;
     float v[8];
     interp_prims_at(im.cells32, im.n2, i * im.n2 + j, d1, d2, v);
     const float k[4] = {y[4].hi, y[5].hi, y[6].hi, y[7].hi};
@@ -122,13 +125,18 @@ __device__ __forceinline__ void trace_record_df(const TraceSpec& tr, const RaySt
     r[15] = 0.0;
 }
 
-// A lane takes ray rid: camera set-up in FP64 (once per ray), then the DF state.
+// A lane takes ray rid: camera set-up in FP64 (once per ray), then the DF
+// state.  Null where the checked build finds the ray outside the batch.
 template <int NF>
 __device__ __forceinline__ const DevImage* start_ray_df(const DevImage* __restrict__ imgs, int n_imgs, long long rid,
                                                         RayStateDF<NF>& s) {
     s.img = find_image(imgs, n_imgs, rid);
+    if (!chk(s.img >= 0 && s.img < n_imgs, imgs[0].check_word, kChkImage, s.img)) return nullptr;
     const DevImage* im = imgs + s.img;
     s.pix = (int)(rid - im->ray_begin);
+    if (!chk(rid >= im->ray_begin && rid - im->ray_begin < (long long)im->width * im->height, im->check_word,
+             kChkPixel, rid))
+        return nullptr;
     s.rid = rid;
     double y0[8], beta;
     init_photon(*im, camera_of(*im), s.pix % im->width, s.pix / im->width, y0, beta);
@@ -173,12 +181,14 @@ __device__ __forceinline__ int advance_ray_df(const DevImage& im, RayStateDF<NF>
 template <int NF>
 __device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayStateDF<NF>& s, double* __restrict__ out,
                                               RayCounters& c) {
-    double* o = out + im.out_offset + (long long)s.pix * im.nfreq;
+    const long long oi = im.out_offset + (long long)s.pix * im.nfreq;
+    const bool in_bounds = chk(oi >= 0 && oi + im.nfreq <= im.out_end, im.check_word, kChkOutput, oi);
+    double* o = out + oi;
     const PixelScale ps = pixel_scale(im, s.pix % im.width);
     bool finite = s.p.rp.hi == s.p.rp.hi && isfinite(s.y[5].hi);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-        if (f >= im.nfreq) break;
+        if (f >= im.nfreq || !in_bounds) break;
         o[f] = scale_output(im, ps, ((double)s.If[f] + (double)s.Ic[f]) * kE2C, f);
         finite = finite && isfinite(o[f]);
     }
@@ -232,9 +242,12 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
             if (!active && live) {
                 const long long rid = ray_begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
                 if (rid < ray_end) {
-                    im = start_ray_df(imgs, n_imgs, rid, s);
-                    active = true;
-                    if (TRACE && rid == tr.ray) trace_record_df<NF>(tr, s, 0.0, 0);
+                    const DevImage* ri = start_ray_df(imgs, n_imgs, rid, s);
+                    if (ri) {
+                        im = ri;
+                        active = true;
+                        if (TRACE && rid == tr.ray) trace_record_df<NF>(tr, s, 0.0, 0);
+                    }
                 } else {
                     live = false;
                 }

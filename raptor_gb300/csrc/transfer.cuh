@@ -41,6 +41,9 @@ __device__ __forceinline__ CellCoef cell_coef(const DevImage& im, double x1, dou
     if (j < 0) { j = 0; d2 = 0.0; }
     else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = 1.0; }
     else d2 = t2 - (double)j;
+    if (!chk(i >= 0 && i <= im.n1 - 2 && j >= 0 && j <= im.n2 - 2, im.check_word, kChkCell,
+             (long long)i * im.n2 + j))
+        i = j = 0;
     cc.base = i * im.n2 + j;
     cc.d1 = d1;
     cc.d2 = d2;

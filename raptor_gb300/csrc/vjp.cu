@@ -423,7 +423,9 @@ struct Layout {
     static constexpr int kOut = 7 + 8 * NF;
     static constexpr bool kSharedOut = NF == 1;
     static constexpr int kSharedRows = kSharedOut ? (kOut > kIn ? kOut : kIn) : kIn;
-    static constexpr int kWarpDoubles = kSharedRows * C + ((2 + NF) * C + 1) / 2;
+    // + the ints (and in the checked build each entry's owner lane)
+    static constexpr int kInts = (2 + NF + (kChecked ? 1 : 0)) * C;
+    static constexpr int kWarpDoubles = kSharedRows * C + (kInts + 1) / 2;
     static constexpr int kScratchRows = kSharedOut ? 0 : kOut;  // per warp, in the scratch buffer
 };
 }  // namespace vpool
@@ -443,6 +445,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     int* const nxt = reinterpret_cast<int*>(fld + L::kSharedRows * C);
     int* const tbase = nxt + C;
     int* const tkind = tbase + C;  // [NF][C]
+    int* const towner = tkind + NF * C;  // checked build only
+    unsigned long long* const cw = imp->check_word;
     // evaluated results: the ticket rows themselves, or this warp's scratch slice
     double* const res = L::kSharedOut ? fld
                                       : scratch + (size_t)(blockIdx.x * (kVjpBlock / 32) + (threadIdx.x >> 5)) *
@@ -536,6 +540,11 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             }
         }
         const int t = ring.append(want, nxt, lane);
+        if (kChecked) {
+            chk(ring.tail - ring.head <= (unsigned)C, cw, kChkRing, (long long)(ring.tail - ring.head));
+            chk(ring.qn >= 0 && ring.qn <= C, cw, kChkList, ring.qn);
+            if (t >= 0) towner[t] = lane;
+        }
         if (t >= 0) {
             double* e = fld + t;
             e[0] = adl.v;
@@ -552,6 +561,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
         }
 
         const unsigned n = ring.batch(mode == 2, mode == 1);
+        chk(n <= 32u, cw, kChkBatch, n);
         if (n) {
             __syncwarp();
             if ((unsigned)lane < n) {
@@ -609,6 +619,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 const int ta = ring.ready();
                 if (!__any_sync(kFull, ta >= 0)) break;
                 if (ta >= 0) {
+                    if (kChecked) chk(towner[ta] == lane, cw, kChkList, ta);
                     const double* o = res + ta;
                     if (tkind[ta] >= 0) {
                         SampleScalars ss;
@@ -765,13 +776,15 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     CK(cudaMemsetAsync(ctx->d_counters, 0, kCtrCount * sizeof(unsigned long long), ctx->stream));
 
     const CamT<D1> cam = camera_tangent(him, img->inclination, gs.geom.a, gs.geom.hslope);
-    // the adjoint of the form that rendered: FP64 duals for the FP64 and
-    // mixed forms, DF / FP32 duals for the mixed-DF form (vjp_df.cu)
+    // the adjoint of the form that rendered: FP64 duals for the FP64 form;
+    // for the mixed and mixed-DF forms their own geodesic with FP32
+    // tangents and the FP32 dual sample (vjp_df.cu)
     int occ = 1;
     const void* kp = nullptr;
     int scratch_rows = 0;
-    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF
-                                ? pick_vjp_df(b.max_nf, &kp)
+    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp)
+                            : precision == RAPTOR_PREC_MIXED
+                                ? pick_vjp_mixed(b.max_nf, &kp)
                                 : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows);
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
     const int grid = ctx->num_sms * std::max(occ, 1);
@@ -825,13 +838,15 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     s.vjp_gated_terms = (long long)ctr[kCtrVjpGate];
     s.n_nonfinite = (long long)fwd_ctr[kCtrNonFinite];
     s.n_stepcap = (long long)fwd_ctr[kCtrStepCap];
+    const unsigned long long check = fwd_ctr[kCtrCheck] ? fwd_ctr[kCtrCheck] : ctr[kCtrCheck];
     s.block_size = kVjpBlock;
     s.grid_blocks = grid;
     s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (check) return render_status(ctx, b.total_rays, b.total_rays, 0, 0, check);
     if ((long long)ctr[kCtrRays] != b.total_rays)
         return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "vjp kernel retired %lld rays, expected %lld",
                         (long long)ctr[kCtrRays], b.total_rays);
     // the forward render's status: its non-finite rays make the gradients
     // meaningless, its step-capped rays are the reference's own behaviour
-    return render_status(ctx, (long long)fwd_ctr[kCtrRays], b.total_rays, s.n_nonfinite, s.n_stepcap);
+    return render_status(ctx, (long long)fwd_ctr[kCtrRays], b.total_rays, s.n_nonfinite, s.n_stepcap, 0);
 }

@@ -1,5 +1,5 @@
-// Pieces shared by the two adjoint kernels (vjp.cu: FP64; vjp_df.cu:
-// mixed-DF): the inclination dual, the sample's three dual directions and
+// Pieces shared by the adjoint kernels (vjp.cu: FP64; vjp_df.cu: mixed-DF
+// and mixed): the inclination dual, the sample's three dual directions and
 // the scalar factors that map them onto the parameters, and the launch
 // interface.
 #pragma once
@@ -115,7 +115,9 @@ constexpr int kVjpRefill = 8;  // geodesic steps between lane refills of the mix
 using VjpLaunchFn = void (*)(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                              const double* dl, unsigned long long* counters, double* gscal, double* g_rho,
                              double* g_u, double* g_th, int refill, double* scratch);
-// the mixed-DF adjoint for nf frequencies (vjp_df.cu); *fn gets the kernel
+// the mixed-DF and the mixed adjoints for nf frequencies (vjp_df.cu); *fn
+// gets the kernel
 VjpLaunchFn pick_vjp_df(int nf, const void** fn);
+VjpLaunchFn pick_vjp_mixed(int nf, const void** fn);
 
 }  // namespace raptor

@@ -1,19 +1,24 @@
-// The adjoint pass of the mixed-DF form: the derivative of what
-// ray_kernel_df renders.  Same method as vjp.cu (one forward sweep per ray,
-// exact reverse-mode sample sensitivities from the suffix identity
+// The adjoint passes whose transfer sample runs in FP32: the derivative of
+// what the mixed-DF form (ray_kernel_df) and the mixed form (ray_kernel<NF,
+// true>) render.  Same method as vjp.cu (one forward sweep per ray, exact
+// reverse-mode sample sensitivities from the suffix identity
 // dI/d delta_k = -(I - I_<k) with the forward image's I, forward-mode
-// tangents for the four scalars, per-cell atomic scatter), in GB300's fast
-// arithmetic:
-//  * the geodesic as DF with its inclination tangent in FP32 (Dual<1, DF,
-//    float>; the tangent needs ~1e-5, not the path's 1e-14) through the same
-//    templated code as every other form (step size, rolled RK4, point
-//    transcendentals, Christoffels), so the path is ray_kernel_df's;
+// tangents for the four scalars, per-cell atomic scatter), with the sample
+// in FP32 as both forward forms compute it:
 //  * the sample as Dual<3, float>, the FP32 transfer of the mixed forms
 //    (rt_sample_fp32_core: emissivity without e2_c, absorptivity through
 //    expm1) along the three directions of vjp_common.cuh (inclination, ln
-//    Theta_e, ln B), accumulated per ray in FP32.
-// FP64 is used once per ray (camera set-up, the forward image's I, the
-// scalar gradients) and for the per-cell atomics.
+//    Theta_e, ln B), accumulated per ray in FP32;
+//  * the geodesic in the arithmetic of the form's forward render, through
+//    the same templated code as every other form (step size, rolled RK4,
+//    point transcendentals, Christoffels), so the path is the forward's:
+//    - mixed-DF (vjp_kernel_df): DF values with FP32 inclination tangents
+//      (Dual<1, DF, float>; the tangent needs ~1e-5, not the path's 1e-14);
+//    - mixed (vjp_kernel_mixed): FP64 values with FP32 inclination tangents
+//      (Dual<1, double, float>): the FP64 path of the mixed forward, with
+//      the tangent's arithmetic off the FP64 pipe.
+// FP64 is otherwise used once per ray (camera set-up, the forward image's I,
+// the scalar gradients) and for the per-cell atomics.
 #include <cuda_runtime.h>
 
 #include "df64.cuh"
@@ -33,9 +38,16 @@ __device__ __forceinline__ void mks_point(DD1 x1, DD1 x2, const GeoDF& g, MksPoi
     mks_point_rolled(x1, x2, g, p);
 }
 
+// A geodesic dual as FP32 value and tangent (the leading part of a DF value)
 __device__ __forceinline__ F1 to_f1(const DD1& x) {
     F1 r(x.v.hi);
     r.d[0] = x.d[0];
+    return r;
+}
+template <class TD>
+__device__ __forceinline__ F1 to_f1(const Dual<1, double, TD>& x) {
+    F1 r((float)x.v);
+    r.d[0] = (float)x.d[0];
     return r;
 }
 __device__ __forceinline__ F3 liftf(const F1& a) {
@@ -45,7 +57,7 @@ __device__ __forceinline__ F3 liftf(const F1& a) {
 }
 
 // The sample's metric (metric.c:94-137, 207-231) in FP32 with its
-// inclination tangent, from the point's leading parts (as metric_f32 in
+// inclination tangent, from the DF point's leading parts (as metric_f32 in
 // ray_kernel_df.cu).
 __device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<DD1>& pd, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
@@ -94,27 +106,18 @@ struct SampleCommonF {
     float d1, d2;    // bilinear offsets
 };
 
-__device__ bool sample_common_f(const DevImage& im, const DD1 y[8], const MksPointT<DD1>& pd, const DD1& adl,
-                                SampleCommonF& out) {
-    const MetricT<F3> g = metric_f3(pd, im.geo_df);
-    // Xtoij (grmhd.c:46-71) from the DF position; the offsets carry the
-    // inclination tangent unless clamped
-    const DF t1 = (y[1].v - im.startx1_df) * im.idx1_df - 0.5;
-    const DF t2 = (y[2].v - im.startx2_df) * im.idx2_df - 0.5;
-    int i = df_trunc_i(t1), j = df_trunc_i(t2);
-    F3 d1(0.0f), d2(0.0f);
-    if (i < 0) i = 0;
-    else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F3(1.0f); }
-    else { d1 = F3(add_f(t1, (float)-i).hi); d1.d[kSIncl] = y[1].d[0] * im.idx1_df.hi; }
-    if (j < 0) j = 0;
-    else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F3(1.0f); }
-    else { d2 = F3(add_f(t2, (float)-j).hi); d2.d[kSIncl] = y[2].d[0] * im.idx2_df.hi; }
-    out.base = i * im.n2 + j;
+// The FP32 sample (rt_sample_fp32_core's fluid, tetrad projection and
+// emission prefactors) from its FP32 metric, the first of its four cells and
+// the bilinear offsets, the wave vector and |d lambda|, each with its
+// inclination tangent.
+__device__ bool sample_common_f(const DevImage& im, const MetricT<F3>& g, int base, const F3& d1, const F3& d2,
+                                const F3 (&k)[4], const F3& adl, SampleCommonF& out) {
+    out.base = base;
     out.d1 = d1.v;
     out.d2 = d2.v;
     const F3 c0 = (1.0f - d1) * (1.0f - d2), c1 = (1.0f - d1) * d2, c2 = d1 * (1.0f - d2), c3 = d1 * d2;
     float a[8], b[8], e[8], f[8];
-    const float* cp = im.cells32 + (size_t)out.base * 8;
+    const float* cp = im.cells32 + (size_t)base * 8;
     load_cell(cp, a);
     load_cell(cp + 8, b);
     load_cell(cp + (size_t)im.n2 * 8, e);
@@ -134,7 +137,6 @@ __device__ bool sample_common_f(const DevImage& im, const DD1 y[8], const MksPoi
     fl.thetae.d[kSLnTh] = fl.thetae.v;
     fl.B.d[kSLnB] = fl.B.v - 1.e-20f;  // B = sqrt(Bsq) B_unit + tiny: the part that scales
 
-    const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
     F3 kd[4];
     lowerT(g, k, kd);
     const F3* U = fl.ucon;
@@ -148,7 +150,7 @@ __device__ bool sample_common_f(const DevImage& im, const DD1 y[8], const MksPoi
     out.emits = (fabsf(sth.v) >= 1.e-10f) && (fl.thetae.v > 1e-4f);
     out.jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
     out.xpre = (float)(kPlanck / (kEMass * kC * kC)) / fl.thetae;
-    out.adl = liftf(to_f1(adl));
+    out.adl = adl;
     return true;
 }
 
@@ -169,20 +171,121 @@ __device__ __forceinline__ bool sample_freq_f(const DevImage& im, const SampleCo
     return true;
 }
 
-// stepsize (integrator.c:109-122) for the dual DF state
-__device__ __forceinline__ DD1 step_size_dd1(const DevImage& im, const DD1 y[8]) {
-    const DF t = df_const(1.e-40);
-    const DD1 m2 = fmin(y[2], 1.0 - y[2]);
-    const DD1 i13 = (fabs(y[5]) + t) + (fabs(y[7]) + t);
-    const DD1 i2 = fabs(y[6]) + t;
-    return -fmax(m2 / ((m2 * i13 + i2) * im.inv_stepsize_df), 1e-12);
-}
+// ------------------------------------------------------------ the two forms
+// What the adjoint body needs of a form's geodesic: the state type (a value
+// with its inclination tangent), its constants, the step size, the stopping
+// and sampling tests in the forward kernel's arithmetic, and the sample's
+// FP32 inputs from the state.
 
-template <int NF>
+// Mixed-DF: the geodesic of ray_kernel_df.
+struct FormDF {
+    using S = DD1;
+    using Th = float;  // d x2 / d lambda as the theta-turn test reads it
+    __device__ static const GeoDF& geo(const DevImage& im) { return im.geo_df; }
+    __device__ static S from_camera(const D1& y) {
+        S s(df_const(y.v));
+        s.d[0] = (float)y.d[0];
+        return s;
+    }
+    // stepsize (integrator.c:109-122) as step_size_df
+    __device__ static S step(const DevImage& im, const S y[8]) {
+        const DF t = df_const(1.e-40);
+        const S m2 = fmin(y[2], 1.0 - y[2]);
+        const S i13 = (fabs(y[5]) + t) + (fabs(y[7]) + t);
+        const S i2 = fabs(y[6]) + t;
+        return -fmax(m2 / ((m2 * i13 + i2) * im.inv_stepsize_df), 1e-12);
+    }
+    __device__ static bool alive(const DevImage& im, const MksPointT<S>& p, int steps, int stop) {
+        const DF r = p.rp.v;
+        return r < df_const(kCutoffOuter) && r > im.cutoff_inner_df && steps < (int)kMaxSteps && !stop;
+    }
+    __device__ static Th theta_rate(const S& y6) { return y6.v.hi; }
+    __device__ static bool turned(Th prev, Th now) {
+        return (prev < 0.0f && now > 0.0f) || (prev > 0.0f && now < 0.0f);
+    }
+    __device__ static bool escaped(const DevImage& im, const S y[8]) {
+        return y[1].v > im.stopx1_df && y[5].v.hi < 0.0f;
+    }
+    __device__ static bool in_grid(const DevImage& im, const S y[8]) {
+        return y[1].v < im.stopx1_df && y[1].v > im.startx1_df && y[2].v > im.startx2_df && y[2].v < im.stopx2_df;
+    }
+    // rt_sample_df's inputs: Xtoij (grmhd.c:46-71) from the DF position,
+    // the offsets carrying the inclination tangent unless clamped
+    __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
+                                  SampleCommonF& out) {
+        const MetricT<F3> g = metric_f3(p, im.geo_df);
+        const DF t1 = (y[1].v - im.startx1_df) * im.idx1_df - 0.5;
+        const DF t2 = (y[2].v - im.startx2_df) * im.idx2_df - 0.5;
+        int i = df_trunc_i(t1), j = df_trunc_i(t2);
+        F3 d1(0.0f), d2(0.0f);
+        if (i < 0) i = 0;
+        else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F3(1.0f); }
+        else { d1 = F3(add_f(t1, (float)-i).hi); d1.d[kSIncl] = y[1].d[0] * im.idx1_df.hi; }
+        if (j < 0) j = 0;
+        else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F3(1.0f); }
+        else { d2 = F3(add_f(t2, (float)-j).hi); d2.d[kSIncl] = y[2].d[0] * im.idx2_df.hi; }
+        if (!chk(i >= 0 && i <= im.n1 - 2 && j >= 0 && j <= im.n2 - 2, im.check_word, kChkCell,
+                 (long long)i * im.n2 + j))
+            i = j = 0;
+        const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
+        return sample_common_f(im, g, i * im.n2 + j, d1, d2, k, liftf(to_f1(adl)), out);
+    }
+};
+
+// Mixed: the FP64 geodesic of ray_kernel<NF, true>, with the inclination
+// tangent in TD.
+template <class TD>
+struct FormMixed {
+    using S = Dual<1, double, TD>;
+    using Th = double;
+    __device__ static const Geo& geo(const DevImage& im) { return im.geo; }
+    __device__ static S from_camera(const D1& y) {
+        S s(y.v);
+        s.d[0] = (TD)y.d[0];
+        return s;
+    }
+    __device__ static S step(const DevImage& im, const S y[8]) { return step_size(im, y); }
+    // the while-condition of integrator.c:228-229, as advance_ray
+    __device__ static bool alive(const DevImage& im, const MksPointT<S>& p, int steps, int stop) {
+        const double r = p.rp.v;
+        return r < kCutoffOuter && r > im.cutoff_inner && (double)steps < kMaxSteps && !stop;
+    }
+    __device__ static Th theta_rate(const S& y6) { return y6.v; }
+    __device__ static bool turned(Th prev, Th now) { return prev * now < 0.0; }
+    __device__ static bool escaped(const DevImage& im, const S y[8]) { return y[1].v > im.stopx1 && y[5].v < 0.0; }
+    __device__ static bool in_grid(const DevImage& im, const S y[8]) {
+        return y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2;
+    }
+    // rt_sample_fp32's inputs: the metric in FP64 (with its tangent) rounded
+    // to FP32, Xtoij in FP64 (cell_coef), the wave vector rounded to FP32
+    __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
+                                  SampleCommonF& out) {
+        MetricDDT<S> gd;
+        MetricUUT<S> gu;
+        mks_metric(p, im.geo, gd, gu);
+        MetricT<F3> g;
+        g.d00 = liftf(to_f1(gd.g00)); g.d01 = liftf(to_f1(gd.g01)); g.d03 = liftf(to_f1(gd.g03));
+        g.d11 = liftf(to_f1(gd.g11)); g.d13 = liftf(to_f1(gd.g13)); g.d22 = liftf(to_f1(gd.g22));
+        g.d33 = liftf(to_f1(gd.g33));
+        g.u00 = liftf(to_f1(gu.g00)); g.u01 = liftf(to_f1(gu.g01)); g.u11 = liftf(to_f1(gu.g11));
+        g.u13 = liftf(to_f1(gu.g13)); g.u22 = liftf(to_f1(gu.g22)); g.u33 = liftf(to_f1(gu.g33));
+        const CellCoef cc = cell_coef(im, y[1].v, y[2].v);
+        const int i = cc.base / im.n2, j = cc.base - i * im.n2;
+        F3 d1((float)cc.d1), d2((float)cc.d2);
+        const double t1 = (y[1].v - im.startx1) * im.idx1 - 0.5;
+        const double t2 = (y[2].v - im.startx2) * im.idx2 - 0.5;
+        if ((int)t1 == i) d1.d[kSIncl] = (float)y[1].d[0] * (float)im.idx1;  // not clamped
+        if ((int)t2 == j) d2.d[kSIncl] = (float)y[2].d[0] * (float)im.idx2;
+        const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
+        return sample_common_f(im, g, cc.base, d1, d2, k, liftf(to_f1(adl)), out);
+    }
+};
+
+template <int NF, class F>
 struct AdjState {
-    DD1 y[8];
-    MksPointT<DD1> p;
-    float thdot_prev;
+    typename F::S y[8];
+    MksPointT<typename F::S> p;
+    typename F::Th thdot_prev;
     int bsign, steps, turns, stop, pix;
     float tau[NF], Ipart[NF], Itot[NF], w[NF];
     float dtg[NF][4];
@@ -196,23 +299,21 @@ __device__ __forceinline__ double pow2_double(int e) {
     return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
-#ifndef RAPTOR_VJP_DF_MIN_BLOCKS
-#define RAPTOR_VJP_DF_MIN_BLOCKS 2
-#endif
-
-template <int NF>
-__global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
-    vjp_kernel_df(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
-                  const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
-                  double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                  double* __restrict__ g_th, int refill_interval) {
-    const DevImage& im = *imp;
+// The adjoint pass: lanes take rays from the queue and refill every
+// refill_interval steps, as the forward kernels do.
+template <int NF, class F>
+__device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>& cam, const double* __restrict__ fwd,
+                                             const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
+                                             double* __restrict__ gscal, double* __restrict__ g_rho,
+                                             double* __restrict__ g_u, double* __restrict__ g_th,
+                                             int refill_interval) {
+    using S = typename F::S;
+    using G = typename std::remove_cv<typename std::remove_reference<decltype(F::geo(im))>::type>::type;
     const int lane = threadIdx.x & 31;
     const long long nrays = (long long)im.width * im.height;
-    const DF cut_outer = df_const(kCutoffOuter);
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
-    AdjState<NF> s;
+    AdjState<NF, F> s;
     bool active = false, live = true;
     while (true) {
         const unsigned need = __ballot_sync(kFull, !active && live);
@@ -230,12 +331,9 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                     double beta;
                     init_photon(im, cam, px, py, y0, beta);  // FP64 duals, once per ray
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        s.y[i] = DD1(df_const(y0[i].v));
-                        s.y[i].d[0] = (float)y0[i].d[0];
-                    }
+                    for (int i = 0; i < 8; ++i) s.y[i] = F::from_camera(y0[i]);
                     s.bsign = (beta < 0.0) ? -1 : ((beta > 0.0) ? 1 : 0);
-                    mks_point(s.y[1], s.y[2], im.geo_df, s.p);
+                    mks_point(s.y[1], s.y[2], F::geo(im), s.p);
                     const PixelScale ps = pixel_scale(im, px);
                     // The loss weights dL/dO * dO/dI can sit far outside FP32's range (the
                     // log-polar camera's dO/dI carries 1/D^2); scale them by a power of two
@@ -271,7 +369,7 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                     s.steps = 0;
                     s.turns = 0;
                     s.stop = 0;
-                    s.thdot_prev = 0.0f;
+                    s.thdot_prev = 0;
                     active = true;
                 } else {
                     live = false;
@@ -281,25 +379,22 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
         if (!__any_sync(kFull, active)) break;
         if (!active) continue;
         for (int it = 0; it < refill_interval; ++it) {
-            const DF r = s.p.rp.v;
-            bool done = !(r < cut_outer && r > im.cutoff_inner_df && s.steps < (int)kMaxSteps && !s.stop);
+            bool done = !F::alive(im, s.p, s.steps, s.stop);
             if (!done) {
-                const float th = s.y[6].v.hi;
-                if (((s.thdot_prev < 0.0f && th > 0.0f) || (s.thdot_prev > 0.0f && th < 0.0f)) && s.steps > 2)
-                    s.turns += 1;
+                const typename F::Th th = F::theta_rate(s.y[6]);
+                if (F::turned(s.thdot_prev, th) && s.steps > 2) s.turns += 1;
                 s.thdot_prev = th;
                 if ((s.bsign < 0 && s.turns > kMaxOrder) || (s.bsign > 0 && s.turns > kMaxOrder + 1)) s.stop = 1;
-                const DD1 dl = step_size_dd1(im, s.y);
-                if (im.integrator == 2) rk2_step<DD1, GeoDF, false>(im.geo_df, s.y, s.p, dl);
-                else rk4_step_rolled<DD1, GeoDF, false>(im.geo_df, s.y, s.p, dl);
+                const S dl = F::step(im, s.y);
+                if (im.integrator == 2) rk2_step<S, G, false>(F::geo(im), s.y, s.p, dl);
+                else rk4_step_rolled<S, G, false>(F::geo(im), s.y, s.p, dl);
                 s.steps += 1;
-                if (s.y[1].v > im.stopx1_df && s.y[5].v.hi < 0.0f) {
+                if (F::escaped(im, s.y)) {
                     done = true;
-                } else if (s.y[1].v < im.stopx1_df && s.y[1].v > im.startx1_df && s.y[2].v > im.startx2_df &&
-                           s.y[2].v < im.stopx2_df) {
+                } else if (F::in_grid(im, s.y)) {
                     ++n_calls;
                     SampleCommonF sc;
-                    if (sample_common_f(im, s.y, s.p, fabs(dl), sc)) {
+                    if (F::sample(im, s.y, s.p, fabs(dl), sc)) {
                         ++n_samples;
                         float Gr = 0.0f, Gt = 0.0f;
                         // one copy of the frequency body (the per-frequency
@@ -307,8 +402,8 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
 #pragma unroll 1
                         for (int f = 0; f < NF; ++f) {
                             if (f >= im.nfreq) break;
-                            F3 S, dt;
-                            if (!sample_freq_f(im, sc, f, S, dt)) continue;
+                            F3 S3, dt;
+                            if (!sample_freq_f(im, sc, f, S3, dt)) continue;
                             ++n_emit;
                             s.tau[f] += dt.v;
 #pragma unroll
@@ -317,15 +412,15 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
                             const bool gate = s.tau[f] < 6.9077553f && !(s.tau[f] < 0.0f);
                             const float suffix = s.Itot[f] - s.Ipart[f];
                             const float eS = gate ? e : 0.0f;
-                            Gr += s.w[f] * (eS * rho_tangent(S, sc.ss) - suffix * rho_tangent(dt, sc.ss));
-                            Gt += s.w[f] * (eS * S.d[kSLnTh] - suffix * dt.d[kSLnTh]);
+                            Gr += s.w[f] * (eS * rho_tangent(S3, sc.ss) - suffix * rho_tangent(dt, sc.ss));
+                            Gt += s.w[f] * (eS * S3.d[kSLnTh] - suffix * dt.d[kSLnTh]);
                             if (gate) {
                                 ++n_gate;
                                 const float we = s.w[f] * e;
 #pragma unroll
                                 for (int q = 0; q < 4; ++q)
-                                    s.dIw[q] += we * (scalar_tangent(S, sc.ss, q) - S.v * s.dtg[f][q]);
-                                s.Ipart[f] += S.v * e;
+                                    s.dIw[q] += we * (scalar_tangent(S3, sc.ss, q) - S3.v * s.dtg[f][q]);
+                                s.Ipart[f] += S3.v * e;
                             }
                         }
                         const float Gu = Gt * sc.ss.dlnth[1];
@@ -388,11 +483,50 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
     }
 }
 
+#ifndef RAPTOR_VJP_DF_MIN_BLOCKS
+#define RAPTOR_VJP_DF_MIN_BLOCKS 2
+#endif
+#ifndef RAPTOR_VJP_MIXED_MIN_BLOCKS
+#define RAPTOR_VJP_MIXED_MIN_BLOCKS 2
+#endif
+// The mixed adjoint's inclination tangent: FP32 (1), which keeps its
+// arithmetic off the FP64 pipe, or FP64 (0).
+#ifndef RAPTOR_VJP_MIXED_TANGENT_FP32
+#define RAPTOR_VJP_MIXED_TANGENT_FP32 1
+#endif
+using MixedTangent = std::conditional<RAPTOR_VJP_MIXED_TANGENT_FP32 != 0, float, double>::type;
+
+template <int NF>
+__global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
+    vjp_kernel_df(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
+                  const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
+                  double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
+                  double* __restrict__ g_th, int refill_interval) {
+    vjp_f32_body<NF, FormDF>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval);
+}
+
+template <int NF>
+__global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_MIXED_MIN_BLOCKS)
+    vjp_kernel_mixed(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
+                     const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
+                     double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
+                     double* __restrict__ g_th, int refill_interval) {
+    vjp_f32_body<NF, FormMixed<MixedTangent>>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th,
+                                              refill_interval);
+}
+
 template <int NF>
 void launch_vjp_df(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                    const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
                    int refill, double*) {
     vjp_kernel_df<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
+}
+
+template <int NF>
+void launch_vjp_mixed(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
+                      const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
+                      int refill, double*) {
+    vjp_kernel_mixed<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
 }
 
 }  // namespace
@@ -401,6 +535,12 @@ VjpLaunchFn pick_vjp_df(int nf, const void** fn) {
     if (nf <= 1) { *fn = (const void*)vjp_kernel_df<1>; return launch_vjp_df<1>; }
     *fn = (const void*)vjp_kernel_df<kMaxFreqs>;
     return launch_vjp_df<kMaxFreqs>;
+}
+
+VjpLaunchFn pick_vjp_mixed(int nf, const void** fn) {
+    if (nf <= 1) { *fn = (const void*)vjp_kernel_mixed<1>; return launch_vjp_mixed<1>; }
+    *fn = (const void*)vjp_kernel_mixed<kMaxFreqs>;
+    return launch_vjp_mixed<kMaxFreqs>;
 }
 
 }  // namespace raptor

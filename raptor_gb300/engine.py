@@ -18,6 +18,8 @@ import numpy as np
 from .synth import GridGeom
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libraptor_gpu.so")
+# the same engine with device-side bounds checks (csrc/checked.cuh)
+CHECKED_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libraptor_gpu_checked.so")
 
 RAPTOR_MAX_FREQS = 8
 RAPTOR_MAX_GRIDS = 16
@@ -93,14 +95,14 @@ class GradC(ctypes.Structure):
                 ("d_u", ctypes.POINTER(ctypes.c_double)), ("d_lnthetae", ctypes.POINTER(ctypes.c_double))]
 
 
-_LIB = None
+_LIBS: dict = {}
 
 
 def load(path: str = LIB_PATH) -> ctypes.CDLL:
-    """Load the in-tree engine library; raises if it was not built."""
-    global _LIB
-    if _LIB is not None:
-        return _LIB
+    """Load the in-tree engine library (or, with CHECKED_LIB_PATH, its
+    bounds-checked build); raises if it was not built."""
+    if path in _LIBS:
+        return _LIBS[path]
     if not os.path.exists(path):
         raise FileNotFoundError(f"{path} is missing: run `python -m raptor_gb300.build` "
                                 "(the engine has no CPU fallback)")
@@ -124,7 +126,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.raptor_gpu_vjp.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, P(D), P(D), P(GradC)]
     lib.raptor_gpu_trace_ray.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          P(D), P(ctypes.c_int)]
-    _LIB = lib
+    _LIBS[path] = lib
     return lib
 
 
@@ -148,8 +150,10 @@ class Engine:
     """One engine context on one CUDA device."""
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, refill_interval: int = 0,
-                 autotune: int = 0, use_graph: int = 0, no_sample_pool: int = 0):
-        self.lib = load()
+                 autotune: int = 0, use_graph: int = 0, no_sample_pool: int = 0, checked: bool = False):
+        """checked: use the bounds-checked build of the library, where a
+        failed device-side index check fails the call with RAPTOR_ERR_DEVICE."""
+        self.lib = load(CHECKED_LIB_PATH if checked else LIB_PATH)
         opt = Options(device, block_size, blocks_per_sm, refill_interval, autotune, use_graph, no_sample_pool)
         h = ctypes.c_void_p()
         rc = self.lib.raptor_gpu_init(ctypes.byref(opt), ctypes.byref(h))

@@ -1,10 +1,14 @@
 """Finite-difference gradients of an image loss from the reference build
 (oracle/_ref, IEEE semantics), for checking raptor_gpu_vjp.
 
-    python tests/golden/make_vjp_fd.py [--threads 8]
+    python tests/golden/make_vjp_fd.py [--threads 8] [--config 4|5]
 
-Configuration (BASELINE configuration 4): 256x256 image, 230 GHz, i = 60 deg,
-a = 0.9375 torus at 256x256, M_unit = 1e19, R_high = R_low = 3, RK4 eps 0.05.
+Configuration 4 (the adjoint configuration): 256x256 image, 230 GHz,
+i = 60 deg, a = 0.9375 torus at 256x256, M_unit = 1e19, R_high = R_low = 3,
+RK4 eps 0.05; 32 cells.  Configuration 5, reduced in rays (the large
+differentiable batch keeps its five frequencies 86/140/230/345/690 GHz and
+its 512x512 torus, on a 128x128 image): 8 cells, written to
+tests/golden/vjp_fd_c5_512.npz.
 Loss L = 1/2 sum (O - O_target)^2 over the nu^3-scaled image O, the target
 rendered at M_unit x 1.3, R_high = R_low = 4, i = 62 deg.  Central differences
 with relative step h = 1e-4 on M_unit, R_high, R_low, the inclination, and on
@@ -34,40 +38,47 @@ from oracle import ref  # noqa: E402
 from raptor_gb300 import harm, synth  # noqa: E402
 from tests.golden.make_golden import quiet  # noqa: E402
 
-N = 256
-W = H = 256
-FREQ = 230e9
 BASE = dict(m_unit=1e19, r_high=3.0, r_low=3.0, incl=60.0)
 TARGET = dict(m_unit=1.3e19, r_high=4.0, r_low=4.0, incl=62.0)
 REL_H = 1e-4
-N_CELLS = 32
+# configuration: grid size, image size, frequencies, cells, output file
+CONFIGS = {
+    4: dict(n=256, w=256, freqs=(230e9,), n_cells=32, out="vjp_fd_256.npz"),
+    5: dict(n=512, w=128, freqs=(86e9, 140e9, 230e9, 345e9, 690e9), n_cells=8, out="vjp_fd_c5_512.npz"),
+}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--config", type=int, choices=sorted(CONFIGS), default=4)
     ap.add_argument("--parts", default="scalars,cells,incl_small")
     a = ap.parse_args()
+    cfg = CONFIGS[a.config]
+    N, W, FREQS, N_CELLS = cfg["n"], cfg["w"], cfg["freqs"], cfg["n_cells"]
+    H = W
     parts = set(a.parts.split(","))
-    dst = os.path.join(ROOT, "tests", "golden", "vjp_fd_256.npz")
+    dst = os.path.join(ROOT, "tests", "golden", cfg["out"])
     res = dict(np.load(dst)) if os.path.exists(dst) else {}
     tmp = tempfile.mkdtemp(prefix="rgv_", dir="/tmp")
     d = synth.make_torus(n1=N, n2=N)
     path = os.path.join(tmp, "t.dump")
     harm.write_dump(path, d)
-    model = harm.ModelIn(IMG_WIDTH=W, IMG_HEIGHT=H, FREQ_MIN=FREQ, FREQ_MAX=FREQ, STEPSIZE=0.05)
+    model = harm.ModelIn(IMG_WIDTH=W, IMG_HEIGHT=H, FREQ_MIN=FREQS[0], FREQ_MAX=FREQS[0], STEPSIZE=0.05)
     pix = np.arange(W * H, dtype=np.int32)
     lib = ref.load(N, N, "RK4")
     lib.ref_scale_prim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
 
     def render(prm, scale=None):
+        """[W*H][F] image, frequency fastest (one reference pass per
+        frequency: the reference build renders one at a time)."""
         with quiet():
             s = ref.RefSession(path, model, prm["m_unit"], prm["incl"], prm["r_high"], prm["r_low"], 0.0,
                                n1=N, n2=N, workdir=tmp)
             if scale:
                 assert lib.ref_scale_prim(*scale) == 0
-            img, _ = s.render_pixels(pix, FREQ, a.threads)
-        return img
+            img = np.stack([s.render_pixels(pix, f, a.threads)[0] for f in FREQS], axis=1)
+        return img if len(FREQS) > 1 else img[:, 0]
 
     target = render(TARGET)
 
@@ -114,6 +125,8 @@ def main():
         print("cell", i, j, fd_rho[c], fd_u[c], flush=True)
     if "cells" in parts:
         res.update(cells=cells, fd_rho=fd_rho, fd_u=fd_u)
+    res["freqs"] = np.array(FREQS)
+    res["image"] = np.array([W, H, N])
     np.savez_compressed(dst, **res)
 
 

@@ -8,8 +8,8 @@ its staged sources could be built on this machine.  The 64-image batch
 on a seeded eighth of every image's pixels.  The FP64 bar is
 tests/parity.py's: per pixel <= 1e-6 except <= 0.1 % grazing pixels, flux
 <= 1e-6.  The two mixed forms are held to the 1e-4 flux bar, and their
-fractions of pixels above 1e-3 and 1e-2 relative error from the FP64 image
-are bounded.
+fractions of bright pixels above 1e-3 and 1e-2 relative error from the FP64
+image are bounded.
 """
 import numpy as np
 import pytest
@@ -87,19 +87,27 @@ def test_1024_every_pixel_against_reference(torus512, renders, incl, tmp_path):
 @pytest.mark.parametrize("incl", [60.0, 17.0])
 def test_1024_mixed_forms_error_fractions(renders, incl):
     """Mixed (FP64 geodesic, FP32 transfer) and mixed-DF (double-float
-    geodesic, FP32 transfer) against the FP64 image: total flux within 1e-4;
-    at most 1 % of the emitting pixels off by more than 1e-3 and 0.1 % by
-    more than 1e-2 (faint pixels, where FP32 rounding of a few samples is a
-    large share of a small intensity)."""
+    geodesic, FP32 transfer) against the FP64 image.  Total flux within
+    1e-4, and the summed absolute pixel error too (no cancellation between
+    pixels).  Per pixel: of the pixels within six decades of the brightest
+    (which carry all but ~2e-6 of the flux), at most 1 % off by more than
+    1e-3 and 0.1 % by more than 1e-2.  The fainter pixels are not bounded:
+    most emitting pixels of this image lie below 1e-6 of the peak, 5 % below
+    1e-30, and there the emissivity's exp(-X^1/3) underflows in FP32 while
+    FP64 still resolves it, so their relative errors reach 100 % on
+    intensities 30 decades below what any pixel that matters carries."""
     from raptor_gb300 import engine
     i64, s64 = renders[incl][engine.PREC_FP64]
-    nz = i64 != 0
+    bright = i64 >= 1e-6 * i64.max()
     for prec in (engine.PREC_MIXED, engine.PREC_MIXED_DF):
         img, spec = renders[incl][prec]
         assert abs(spec - s64) / s64 <= FLUX_RTOL_MIXED, prec
-        err = pixel_errors(img[nz], i64[nz])
+        l1 = float(np.sum(np.abs(img - i64)) / np.sum(i64))
+        err = pixel_errors(img[bright], i64[bright])
         f3, f2 = float(np.mean(err > 1e-3)), float(np.mean(err > 1e-2))
-        assert f3 <= 1e-2 and f2 <= 1e-3, (prec, f3, f2, float(np.median(err)))
+        info = (prec, l1, f3, f2, float(np.median(err)), int(bright.sum()))
+        assert l1 <= FLUX_RTOL_MIXED, info
+        assert f3 <= 1e-2 and f2 <= 1e-3, info
 
 
 def test_batch_every_image_against_port():

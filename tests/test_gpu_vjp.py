@@ -3,8 +3,9 @@ FP64 forward render (small case), and of the reference build rerun at
 perturbed parameters (tests/golden/vjp_fd_256.npz: 256x256 image of the
 256x256 torus, loss to a target at M_unit x 1.3, R = 4, i = 62 deg).
 
-Agreement bar: 1e-3 relative; per-cell gradients 1e-3 of the largest per-cell
-finite difference.  M_unit, R_high and R_low are compared with
+Agreement bar: 1e-3 relative; a per-cell gradient to 1e-3 of its own
+finite difference, or of 1e-3 of the largest per-cell difference where its
+own is smaller than that.  M_unit, R_high and R_low are compared with
 Richardson-extrapolated differences (4 D(h/2) - D(h)) / 3 at h = 1e-4
 relative.  The image loss is only piecewise smooth in the inclination (clamps,
 the min() of the step size and cell-index changes along 65,536 rays), so its
@@ -30,10 +31,17 @@ def _loss(eng, engine, desc, target):
 
 
 class Mismatches(list):
-    def check(self, name, got, want, scale=None):
+    def check(self, name, got, want, scale=None, tol=TOL):
         scale = abs(want) if scale is None else scale
-        if not abs(got - want) <= TOL * scale:
+        if not abs(got - want) <= tol * scale:
             self.append(f"{name}: vjp {got:.6e} vs finite difference {want:.6e}")
+
+    def check_cell(self, name, got, want, largest, tol=TOL):
+        """A per-cell gradient against its own difference quotient, floored
+        at 1e-3 of the largest cell's (below that, the difference quotient of
+        a 1e-4 perturbation is dominated by the loss's rounding and by the
+        discrete decisions the perturbation flips)."""
+        self.check(name, got, want, max(abs(want), 1e-3 * largest), tol)
 
 
 def test_vjp_against_engine_finite_differences(torus64):
@@ -77,13 +85,17 @@ def test_vjp_against_engine_finite_differences(torus64):
     scale = max(abs(x) for x in fds)
     assert scale > 0
     for n, a, b in zip(names, gots, fds):
-        bad.check(n, a, b, scale)
+        bad.check_cell(n, a, b, scale)
     eng.close()
     assert not bad, "\n".join(bad)
 
 
-def test_vjp_against_reference_finite_differences(torus256):
-    """The reference rerun at perturbed parameters (configuration 4)."""
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "mixed", "mixed_df"])
+def test_vjp_against_reference_finite_differences(torus256, prec):
+    """The reference rerun at perturbed parameters (configuration 4), for
+    each form's VJP: its forward render and its adjoint pass (FP64; mixed:
+    FP64 geodesic with FP32 tangents and the FP32 dual sample; mixed-DF:
+    double-float geodesic, FP32 tangents and sample), all at the 1e-3 bar."""
     from raptor_gb300 import engine
     z = load_golden("vjp_fd_256.npz")
     eng = engine.Engine()
@@ -94,7 +106,8 @@ def test_vjp_against_reference_finite_differences(torus256):
     img, _ = eng.render(desc, engine.PREC_FP64)
     dl = img - target
     assert 0.5 * np.sum(dl ** 2) == pytest.approx(z["L0"][0], rel=1e-6)
-    _, g = eng.vjp(desc, dl, engine.PREC_FP64)
+    fimg, g = eng.vjp(desc, dl, prec)
+    assert np.abs(fimg - img).max() <= (0.0 if prec == 0 else 1e-4) * np.abs(img).max()
     bad = Mismatches()
     bad.check("M_unit", g["d_m_unit"], z["rich_m_unit"][0])
     bad.check("R_high", g["d_r_high"], z["rich_r_high"][0])
@@ -113,8 +126,8 @@ def test_vjp_against_reference_finite_differences(torus256):
     cells = z["cells"]
     scale = max(np.max(np.abs(z["fd_rho"])), np.max(np.abs(z["fd_u"])))
     for k, (i, j) in enumerate(cells):
-        bad.check(f"rho[{i},{j}]", g["d_rho"][i, j], z["fd_rho"][k], scale)
-        bad.check(f"u[{i},{j}]", g["d_u"][i, j], z["fd_u"][k], scale)
+        bad.check_cell(f"rho[{i},{j}]", g["d_rho"][i, j], z["fd_rho"][k], scale)
+        bad.check_cell(f"u[{i},{j}]", g["d_u"][i, j], z["fd_u"][k], scale)
     assert eng.stats()["rays"] == 256 * 256
     eng.close()
     assert not bad, "\n".join(bad)
@@ -147,29 +160,42 @@ def test_vjp_thetae_field_sums_to_temperature_ratio_gradient(torus64):
     assert total == pytest.approx(want, rel=1e-9)
 
 
-def test_vjp_mixed_forward(torus64):
-    """precision = mixed: the forward image comes from the FP32-transfer form,
-    the adjoint stays FP64, so the gradients agree with the FP64 VJP to the
-    mixed form's image accuracy."""
+@pytest.mark.parametrize("freqs", [[230e9], [86e9, 230e9, 345e9]])
+def test_vjp_mixed(torus64, freqs):
+    """precision = mixed: the mixed forward (FP64 geodesic, FP32 transfer)
+    and its adjoint (the same FP64 path with FP32 inclination tangents, the
+    FP32 dual sample).  Same steps and samples as the FP64 adjoint; gradients
+    within 2e-3 of the FP64 adjoint's (scalars) and 2e-3 of scale (per-cell
+    fields), the bar of the mixed-DF adjoint, which shares the sample; the
+    Theta_e identity to FP32 accumulation accuracy."""
     from raptor_gb300 import engine
     eng = engine.Engine()
     gid = eng.upload_grid(torus64.geom, torus64.prims)
-    desc = engine.image_desc(48, 48, [230e9], grid=gid, inclination=60.0, m_unit=1e19, r_high=3.0, r_low=3.0)
-    tdesc = engine.image_desc(48, 48, [230e9], grid=gid, inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0)
+    R = 3.0
+    kw = dict(grid=gid, inclination=60.0, m_unit=1e19, r_high=R, r_low=R)
+    desc = engine.image_desc(48, 48, freqs, **kw)
+    tdesc = engine.image_desc(48, 48, freqs, **dict(kw, inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0))
     target, _ = eng.render(tdesc, engine.PREC_FP64)
     img, _ = eng.render(desc, engine.PREC_FP64)
     dl = img - target
     i64, g64 = eng.vjp(desc, dl, engine.PREC_FP64)
+    s64 = eng.stats()
     i32, g32 = eng.vjp(desc, dl, engine.PREC_MIXED)
+    s32 = eng.stats()
     eng.close()
     assert np.array_equal(i64, img)
     assert np.abs(i32 - img).max() <= 1e-4 * np.abs(img).max()
+    for key in ("rays", "steps", "rt_calls", "rt_samples"):
+        assert s32[key] == s64[key], key
     for k in ("d_m_unit", "d_r_high", "d_r_low", "d_inclination"):
-        assert g32[k] == pytest.approx(g64[k], rel=1e-3), k
+        assert g32[k] == pytest.approx(g64[k], rel=2e-3), k
     for k in ("d_rho", "d_u", "d_lnthetae"):
         scale = np.abs(g64[k]).max()
-        assert scale > 0
-        assert np.abs(g32[k] - g64[k]).max() <= 1e-3 * scale, k
+        assert scale > 0 and np.all(np.isfinite(g32[k]))
+        assert np.abs(g32[k] - g64[k]).max() <= 2e-3 * scale, k
+    total = float(np.sum(g32["d_lnthetae"]))
+    want = (g32["d_r_high"] + g32["d_r_low"]) / _dln_thetae_unit_dR(R)
+    assert total == pytest.approx(want, rel=1e-4)
 
 
 @pytest.mark.parametrize("freqs", [[230e9], [86e9, 230e9, 345e9]])
@@ -211,8 +237,8 @@ def test_vjp_log_camera_and_rk2(torus64, camera, integrator):
     """The adjoint through the log-polar camera (its output factor enters
     dO/dI) and through RK2 steps: M_unit and inclination gradients against
     the engine's own central differences (h = 1e-6 relative, where the loss
-    is smooth on this small image), and the mixed-DF adjoint against the
-    FP64 one."""
+    is smooth on this small image), and the mixed-DF and mixed adjoints
+    against the FP64 one."""
     from raptor_gb300 import engine
     eng = engine.Engine()
     gid = eng.upload_grid(torus64.geom, torus64.prims)
@@ -223,6 +249,7 @@ def test_vjp_log_camera_and_rk2(torus64, camera, integrator):
     img, _ = eng.render(mk(), engine.PREC_FP64)
     _, g = eng.vjp(mk(), img - target, engine.PREC_FP64)
     _, gdf = eng.vjp(mk(), img - target, engine.PREC_MIXED_DF)
+    _, gmx = eng.vjp(mk(), img - target, engine.PREC_MIXED)
     bad = Mismatches()
     for key, attr in (("m_unit", "d_m_unit"), ("inclination", "d_inclination")):
         h = 1e-6 * kw[key]
@@ -230,6 +257,7 @@ def test_vjp_log_camera_and_rk2(torus64, camera, integrator):
         lm = _loss(eng, engine, mk(**{key: kw[key] - h}), target)
         bad.check(key, g[attr], (lp - lm) / (2 * h))
         bad.check(key + " (mixed-DF)", gdf[attr], g[attr])
+        bad.check(key + " (mixed)", gmx[attr], g[attr])
     eng.close()
     assert not bad, "\n".join(bad)
 

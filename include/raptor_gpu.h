@@ -201,11 +201,24 @@ int raptor_gpu_trace_ray(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
 /* Vector-Jacobian product of one image: given dL_dI [W*H][n_freq] (same
  * layout and nu^3 scaling as I_out), returns dL/d(M_UNIT, R_HIGH, R_LOW,
  * INCLINATION) and, if the pointers are set, the per-cell gradients on the
- * image's grid.  precision selects the form of the forward render whose image
- * the adjoint uses (any of the three); the adjoint pass itself runs in FP64.  I_out receives the forward image (may be NULL).
+ * image's grid.  precision selects the form: the forward render in that form
+ * and that form's adjoint pass (FP64: FP64 tangents and dual sample; mixed:
+ * the FP64 geodesic with FP32 tangents and the FP32 dual sample; mixed-DF:
+ * the double-float geodesic with FP32 tangents and sample).  I_out receives
+ * the forward image (may be NULL).
  * No counterpart in the reference, which has no derivatives. */
 int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
                    const double *dL_dI, double *I_out, raptor_grad *grad);
+
+/* The same, restricted to the image's rays [ray_begin, ray_begin+ray_count)
+ * (pixel x + y*W): the forward image holds those pixels only (0 elsewhere)
+ * and the gradients are those rays' contributions.  Gradients are sums over
+ * rays, so the gradients of disjoint ranges add up to raptor_gpu_vjp's; a
+ * caller splitting one image across processes or devices sums them (scalars
+ * and per-cell arrays alike).  No counterpart in the reference. */
+int raptor_gpu_vjp_range(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
+                         long long ray_begin, long long ray_count, const double *dL_dI, double *I_out,
+                         raptor_grad *grad);
 
 /* ---- Render without allocating device memory ----
  * No counterpart in the reference: it exists for callers that cannot call

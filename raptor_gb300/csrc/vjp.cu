@@ -290,10 +290,9 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-               double* __restrict__ g_th) {
+               double* __restrict__ g_th, RayRange rr) {
     const DevImage& im = *imp;
     const int lane = threadIdx.x & 31;
-    const long long nrays = (long long)im.width * im.height;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0;
     bool live = true;
@@ -306,8 +305,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
         base = __shfl_sync(kFull, base, leader);
         long long rid = -1;
         if (live) {
-            rid = (long long)(base + __popc(want & ((1u << lane) - 1u)));
-            if (rid >= nrays) {
+            rid = rr.begin + (long long)(base + __popc(want & ((1u << lane) - 1u)));
+            if (rid >= rr.end) {
                 live = false;
                 rid = -1;
             }
@@ -435,7 +434,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel_pool(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                     const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                     double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                    double* __restrict__ g_th, int refill_interval, double* __restrict__ scratch) {
+                    double* __restrict__ g_th, int refill_interval, double* __restrict__ scratch, RayRange rr) {
     using namespace vpool;
     using L = Layout<NF>;
     __shared__ double pool_mem[(kVjpBlock / 32) * L::kWarpDoubles];
@@ -451,7 +450,6 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     double* const res = L::kSharedOut ? fld
                                       : scratch + (size_t)(blockIdx.x * (kVjpBlock / 32) + (threadIdx.x >> 5)) *
                                                       L::kScratchRows * C;
-    const long long nrays = (long long)im.width * im.height;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
 
@@ -476,8 +474,8 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
             base = __shfl_sync(kFull, base, leader);
             if (mode == 0 && live) {
-                const long long rid = (long long)(base + __popc(need & ((1u << lane) - 1u)));
-                if (rid < nrays) {
+                const long long rid = rr.begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
+                if (rid < rr.end) {
                     const int pix = (int)rid;
                     init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
                     mks_point(y[1], y[2], im.geo, p);
@@ -690,15 +688,15 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 template <int NF>
 void launch_vjp_pool(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                      const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                     int refill, double* scratch) {
-    vjp_kernel_pool<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch);
+                     int refill, double* scratch, RayRange rr) {
+    vjp_kernel_pool<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch, rr);
 }
 
 template <int NF>
 void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                 const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                int, double*) {
-    vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt);
+                int, double*, RayRange rr) {
+    vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, rr);
 }
 
 // pool: the sample-pool kernel; *scratch_rows gets the scratch rows (of
@@ -738,8 +736,8 @@ VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows)
             return ctx_fail(ctx, RAPTOR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));  \
     } while (0)
 
-extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, const double* dL_dI,
-                              double* I_out, raptor_grad* grad) {
+static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, long long ray_begin,
+                    long long ray_count, const double* dL_dI, double* I_out, raptor_grad* grad) {
     if (!ctx) return RAPTOR_ERR_INVALID;
     ctx->err[0] = 0;
     if (!img || !dL_dI || !grad) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: null image, dL_dI or grad");
@@ -754,12 +752,16 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     const DevImage& him = b.host[0];
     const GridSlot& gs = ctx->grids[img->grid];
     const long long ncell = (long long)gs.geom.n1 * gs.geom.n2;
+    if (ray_begin < 0 || ray_count < 0 || ray_begin > b.total_rays)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: ray range [%lld, +%lld) outside the image", ray_begin,
+                        ray_count);
+    const long long rb = ray_begin, re = ray_count > b.total_rays - rb ? b.total_rays : rb + ray_count;
 
-    // forward render (its image is the I of the suffix identity)
+    // forward render of the range (its image is the I of the suffix identity)
     const void* fnp = nullptr;
     RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp, !ctx->opt.no_sample_pool);
     LaunchShape ls = choose_shape(ctx, b, precision, fn, fnp);
-    rc = enqueue_render(ctx, b, precision, 0, b.total_rays, ls, fn, true);
+    rc = enqueue_render(ctx, b, precision, rb, re, ls, fn, true);
     if (rc) return rc;
 
     const size_t nout = (size_t)b.out_len;
@@ -802,7 +804,7 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     double* gth = fields ? ctx->d_grad + 4 + 2 * ncell : nullptr;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     vfn(grid, ctx->stream, ctx->d_imgs, cam, ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc, grho, gu, gth,
-        kVjpRefill, ctx->d_vjp_scratch);
+        kVjpRefill, ctx->d_vjp_scratch, RayRange{rb, re});
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     double scal[4];
@@ -842,11 +844,23 @@ extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img,
     s.block_size = kVjpBlock;
     s.grid_blocks = grid;
     s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (check) return render_status(ctx, b.total_rays, b.total_rays, 0, 0, check);
-    if ((long long)ctr[kCtrRays] != b.total_rays)
+    if (check) return render_status(ctx, re - rb, re - rb, 0, 0, check);
+    if ((long long)ctr[kCtrRays] != re - rb)
         return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "vjp kernel retired %lld rays, expected %lld",
-                        (long long)ctr[kCtrRays], b.total_rays);
+                        (long long)ctr[kCtrRays], re - rb);
     // the forward render's status: its non-finite rays make the gradients
     // meaningless, its step-capped rays are the reference's own behaviour
-    return render_status(ctx, (long long)fwd_ctr[kCtrRays], b.total_rays, s.n_nonfinite, s.n_stepcap, 0);
+    return render_status(ctx, (long long)fwd_ctr[kCtrRays], re - rb, s.n_nonfinite, s.n_stepcap, 0);
+}
+
+extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, const double* dL_dI,
+                              double* I_out, raptor_grad* grad) {
+    return vjp_impl(ctx, img, precision, 0, (long long)1 << 62, dL_dI, I_out, grad);
+}
+
+extern "C" int raptor_gpu_vjp_range(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision,
+                                    long long ray_begin, long long ray_count, const double* dL_dI, double* I_out,
+                                    raptor_grad* grad) {
+    if (ray_begin < 0 || ray_count < 0) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: negative ray range");
+    return vjp_impl(ctx, img, precision, ray_begin, ray_count, dL_dI, I_out, grad);
 }

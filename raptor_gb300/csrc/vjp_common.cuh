@@ -106,15 +106,20 @@ __device__ __forceinline__ T rho_tangent(const Dl& x, const SampleScalarsT<T>& s
 constexpr int kVjpBlock = 128;
 constexpr int kVjpRefill = 8;  // geodesic steps between lane refills of the mixed-DF adjoint
 
+// The rays [begin, end) of an image (pixel x + y W) an adjoint pass covers.
+struct RayRange {
+    long long begin, end;
+};
+
 // Launch of the adjoint pass: grid blocks of kVjpBlock threads on stream st
 // for image im (device pointer), camera constants with their inclination
 // tangent, the forward image fwd and dL/dI dl (device, image layout);
 // accumulates into counters, gscal[4] and the per-cell arrays (which may be
 // null); lanes take new rays every refill steps; scratch is the sample
-// pool's result buffer where the kernel has one.
+// pool's result buffer where the kernel has one; rr the rays to cover.
 using VjpLaunchFn = void (*)(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                              const double* dl, unsigned long long* counters, double* gscal, double* g_rho,
-                             double* g_u, double* g_th, int refill, double* scratch);
+                             double* g_u, double* g_th, int refill, double* scratch, RayRange rr);
 // the mixed-DF and the mixed adjoints for nf frequencies (vjp_df.cu); *fn
 // gets the kernel
 VjpLaunchFn pick_vjp_df(int nf, const void** fn);

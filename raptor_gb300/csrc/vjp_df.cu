@@ -306,11 +306,10 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                                              const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                                              double* __restrict__ gscal, double* __restrict__ g_rho,
                                              double* __restrict__ g_u, double* __restrict__ g_th,
-                                             int refill_interval) {
+                                             int refill_interval, RayRange rr) {
     using S = typename F::S;
     using G = typename std::remove_cv<typename std::remove_reference<decltype(F::geo(im))>::type>::type;
     const int lane = threadIdx.x & 31;
-    const long long nrays = (long long)im.width * im.height;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
     AdjState<NF, F> s;
@@ -323,8 +322,8 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
             if (lane == leader) base = atomicAdd(&counters[kCtrQueue], (unsigned long long)__popc(need));
             base = __shfl_sync(kFull, base, leader);
             if (!active && live) {
-                const long long rid = (long long)(base + __popc(need & ((1u << lane) - 1u)));
-                if (rid < nrays) {
+                const long long rid = rr.begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
+                if (rid < rr.end) {
                     s.pix = (int)rid;
                     const int px = s.pix % im.width, py = s.pix / im.width;
                     D1 y0[8];
@@ -501,8 +500,8 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
     vjp_kernel_df(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                   const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                   double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                  double* __restrict__ g_th, int refill_interval) {
-    vjp_f32_body<NF, FormDF>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval);
+                  double* __restrict__ g_th, int refill_interval, RayRange rr) {
+    vjp_f32_body<NF, FormDF>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval, rr);
 }
 
 template <int NF>
@@ -510,23 +509,23 @@ __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_MIXED_MIN_BLOCKS)
     vjp_kernel_mixed(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                      const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                      double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                     double* __restrict__ g_th, int refill_interval) {
+                     double* __restrict__ g_th, int refill_interval, RayRange rr) {
     vjp_f32_body<NF, FormMixed<MixedTangent>>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th,
-                                              refill_interval);
+                                              refill_interval, rr);
 }
 
 template <int NF>
 void launch_vjp_df(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                    const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                   int refill, double*) {
-    vjp_kernel_df<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
+                   int refill, double*, RayRange rr) {
+    vjp_kernel_df<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
 }
 
 template <int NF>
 void launch_vjp_mixed(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                       const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                      int refill, double*) {
-    vjp_kernel_mixed<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill);
+                      int refill, double*, RayRange rr) {
+    vjp_kernel_mixed<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
 }
 
 }  // namespace

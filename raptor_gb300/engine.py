@@ -40,7 +40,7 @@ WARN_STEPCAP = 1
 EXPORTED = ("raptor_gpu_init", "raptor_gpu_destroy", "raptor_gpu_last_error", "raptor_gpu_upload_grid",
             "raptor_gpu_render", "raptor_gpu_render_range", "raptor_gpu_output_size",
             "raptor_gpu_spectrum_size", "raptor_gpu_get_stats", "raptor_gpu_vjp", "raptor_gpu_trace_ray",
-            "raptor_gpu_render_noalloc")
+            "raptor_gpu_vjp_range", "raptor_gpu_render_noalloc")
 
 
 class EngineError(RuntimeError):
@@ -124,6 +124,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.raptor_gpu_spectrum_size.restype = ctypes.c_longlong
     lib.raptor_gpu_get_stats.argtypes = [ctypes.c_void_p, P(Stats)]
     lib.raptor_gpu_vjp.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, P(D), P(D), P(GradC)]
+    lib.raptor_gpu_vjp_range.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, ctypes.c_longlong,
+                                         ctypes.c_longlong, P(D), P(D), P(GradC)]
     lib.raptor_gpu_trace_ray.argtypes = [ctypes.c_void_p, P(ImageDesc), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          P(D), P(ctypes.c_int)]
     _LIBS[path] = lib
@@ -230,7 +232,10 @@ class Engine:
                                                   _dp(rec), ctypes.byref(n)))
         return rec[:n.value]
 
-    def vjp(self, img: ImageDesc, dL_dI: np.ndarray, precision=PREC_FP64, want_fields=True):
+    def vjp(self, img: ImageDesc, dL_dI: np.ndarray, precision=PREC_FP64, want_fields=True, ray_begin=None,
+            ray_count=None):
+        """Forward image and gradients of L given dL/dI (raptor_gpu_vjp); with
+        ray_begin / ray_count, of those rays only (raptor_gpu_vjp_range)."""
         geom = self.grids[img.grid]
         dldi = np.ascontiguousarray(dL_dI, dtype=np.float64)
         out = np.empty(img.width * img.height * img.n_freq)
@@ -238,8 +243,14 @@ class Engine:
         d_u = np.zeros(geom.n1 * geom.n2) if want_fields else None
         d_th = np.zeros(geom.n1 * geom.n2) if want_fields else None
         g = GradC(0, 0, 0, 0, _dp(d_rho), _dp(d_u), _dp(d_th))
-        self._check(self.lib.raptor_gpu_vjp(self.h, ctypes.byref(img), precision, _dp(dldi), _dp(out),
-                                            ctypes.byref(g)))
+        if ray_begin is None:
+            self._check(self.lib.raptor_gpu_vjp(self.h, ctypes.byref(img), precision, _dp(dldi), _dp(out),
+                                                ctypes.byref(g)))
+        else:
+            self._check(self.lib.raptor_gpu_vjp_range(
+                self.h, ctypes.byref(img), precision, ray_begin,
+                ray_count if ray_count is not None else img.width * img.height - ray_begin, _dp(dldi), _dp(out),
+                ctypes.byref(g)))
         res = dict(d_m_unit=g.d_m_unit, d_r_high=g.d_r_high, d_r_low=g.d_r_low, d_inclination=g.d_inclination)
         if want_fields:
             res["d_rho"] = d_rho.reshape(geom.n1, geom.n2)

@@ -290,3 +290,31 @@ def test_vjp_sample_pool_matches_in_place(torus256, camera, integrator, freqs):
     for key in ("d_rho", "d_u", "d_lnthetae"):
         scale = float(np.abs(g1[key]).max())
         assert scale > 0.0 and float(np.abs(g0[key] - g1[key]).max()) <= 1e-12 * scale, key
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "mixed", "mixed_df"])
+def test_vjp_ranges_add_up(torus64, prec):
+    """raptor_gpu_vjp_range: the gradients of disjoint ray ranges add up to
+    the whole image's (every gradient is a sum over rays; the per-cell
+    atomics add in another order), and the partial forward images to the
+    whole forward image - the split raptor_gb300/shard.py makes across
+    processes."""
+    from raptor_gb300 import engine
+    eng = engine.Engine()
+    gid = eng.upload_grid(torus64.geom, torus64.prims)
+    desc = engine.image_desc(30, 26, [86e9, 230e9], grid=gid, inclination=55.0)
+    target, _ = eng.render(engine.image_desc(30, 26, [86e9, 230e9], grid=gid, inclination=57.0, m_unit=1.2e19),
+                           engine.PREC_FP64)
+    img, _ = eng.render(desc, engine.PREC_FP64)
+    dl = img - target
+    full_img, full = eng.vjp(desc, dl, prec)
+    cuts = [0, 97, 401, 30 * 26]
+    parts = [eng.vjp(desc, dl, prec, ray_begin=a, ray_count=b - a) for a, b in zip(cuts, cuts[1:])]
+    assert eng.stats()["rays"] == cuts[-1] - cuts[-2]
+    eng.close()
+    np.testing.assert_allclose(sum(p[0] for p in parts), full_img, rtol=1e-12, atol=0)
+    for k in ("d_m_unit", "d_r_high", "d_r_low", "d_inclination"):
+        assert sum(p[1][k] for p in parts) == pytest.approx(full[k], rel=1e-9), k
+    for k in ("d_rho", "d_u", "d_lnthetae"):
+        scale = float(np.abs(full[k]).max())
+        assert float(np.abs(sum(p[1][k] for p in parts) - full[k]).max()) <= 1e-9 * scale, k

@@ -58,3 +58,53 @@ def test_two_rank_render_and_merge(tmp_path):
     d = synth.make_torus(n1=64, n2=64)
     ref, _ = oport.Scene(d.geom, d.prims, 12, 12, inclination=50.0).render([230e9], nthreads=1)
     assert np.array_equal(np.load(out), ref[:, 0])
+
+
+def _grad_worker(rank, world, port, out_path):
+    """Each rank's gradients from its own ray range (per-ray contributions of
+    the oracle port's image standing in for the adjoint, which needs a GPU),
+    merged over the two ranks."""
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    g = _range_grads(*shard.ray_range(12 * 12, world, rank))
+    full = shard.merge_grads(g)
+    if rank == 0:
+        np.savez(out_path, **{k: np.asarray(v) for k, v in full.items()})
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def _range_grads(b, e):
+    """Additive per-ray stand-in gradients of the rays [b, e) of a 12x12
+    image: ray k adds its intensity I_k times fixed weights to the four
+    scalars and to cells k mod 64 of a 8x8 grid."""
+    from oracle import port as oport
+    from raptor_gb300 import synth
+    d = synth.make_torus(n1=64, n2=64)
+    vals, _ = oport.Scene(d.geom, d.prims, 12, 12, inclination=50.0).render([230e9], pixels=np.arange(b, e),
+                                                                           nthreads=1)
+    g = {k: 0.0 for k in shard.SCALARS}
+    fields = {k: np.zeros((8, 8)) for k in shard.FIELDS}
+    for k, v in zip(range(b, e), vals[:, 0]):
+        for q, name in enumerate(shard.SCALARS):
+            g[name] += (q + 1) * v
+        for q, name in enumerate(shard.FIELDS):
+            fields[name].flat[k % 64] += (q + 2) * v
+    g.update(fields)
+    return g
+
+
+def test_two_rank_gradient_merge(tmp_path):
+    """merge_grads over two gloo ranks equals the single-process gradients of
+    the whole image (the adjoint's gradients are sums over rays)."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    out = str(tmp_path / "grads.npz")
+    mp.spawn(_grad_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    got = np.load(out)
+    want = _range_grads(0, 144)
+    for k in shard.SCALARS:
+        assert float(got[k]) == pytest.approx(want[k], rel=1e-13), k
+    for k in shard.FIELDS:
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-13, atol=0)

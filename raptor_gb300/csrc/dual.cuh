@@ -100,7 +100,7 @@ __host__ __device__ inline Dual<N, T, TD> operator*(const Dual<N, T, TD>& a, con
 }
 template <int N, class T, class TD>
 __host__ __device__ inline Dual<N, T, TD> operator/(const Dual<N, T, TD>& a, const Dual<N, T, TD>& b) {
-    const T ib = scalar_cast<T>(1.0) / b.v;
+    const T ib = recip(b.v);
     Dual<N, T, TD> r;
     r.v = a.v * ib;
     const TD rv = tan_cast<TD>(r.v), ibd = tan_cast<TD>(ib);

@@ -59,7 +59,7 @@ __device__ __forceinline__ void point_reciprocals(const R& Sg, const R& thp, Mks
     p.Sg = Sg;
     p.thp = thp;
     const R q1 = p.rp * thp, q2 = q1 * p.s, q3 = q2 * Sg;
-    const R iq3 = 1.0 / q3;
+    const R iq3 = recip(q3);
     p.iS = iq3 * q2;
     const R iq2 = iq3 * Sg;
     p.isn = iq2 * q1;
@@ -220,7 +220,7 @@ __device__ __forceinline__ void mks_metric(const MksPointT<R>& p, const G& g, Me
     d.g13 = mas2 * opzr;
     d.g22 = rho2 * hfac * hfac;
     d.g33 = s2 * (rho2 + g.a2 * s2 * opz);
-    const R ir = (g.R0 == 0.0) ? p.irp : 1.0 / r;  // r == rp exactly when R0 == 0
+    const R ir = (g.R0 == 0.0) ? p.irp : recip(r);  // r == rp exactly when R0 == 0
     u.g00 = -1.0 - z;
     u.g01 = 2.0 * irho2;
     u.g11 = irho2 * (r * (r - 2.0) + g.a2) * (ir * ir);

@@ -125,14 +125,15 @@ __device__ __forceinline__ void init_photon(const DevImage& im, const CamT<R>& c
 
 // stepsize (integrator.c:109-122) with the reciprocals folded:
 // 1/(eps/|k|) = |k|/eps; the tiny^2 guards keep the reference's limits.
-// 1 / (i1 + i2/m2 + i3) is formed as m2 / (m2 (i1 + i3) + i2), one division.
+// 1 / (i1 + i2/m2 + i3) is formed as m2 / (m2 (i1 + i3) + i2), one
+// reciprocal.
 template <class R>
 __device__ __forceinline__ R step_size(const DevImage& im, const R y[8]) {
     const double t = 1.e-40;
     const R m2 = fmin(y[2], 1.0 - y[2]);
     const R i13 = (fabs(y[5]) + t) + (fabs(y[7]) + t);
     const R i2 = fabs(y[6]) + t;
-    return -fmax(m2 / ((m2 * i13 + i2) * im.inv_stepsize), 1e-12);
+    return -fmax(m2 * recip((m2 * i13 + i2) * im.inv_stepsize), 1e-12);
 }
 
 template <class R, class G>

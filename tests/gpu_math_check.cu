@@ -46,6 +46,14 @@ __global__ void eval_df(const double* x, int n, double* out) {
     out[4 * i + 3] = fabs(raptor::df_to_double(q) - qd) / fabs(qd);
 }
 
+// fast_rcp (fp64_math.cuh) against the IEEE quotient 1/x
+__global__ void eval_rcp(const double* x, int n, double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[2 * i] = raptor::fast_rcp(x[i]);
+    out[2 * i + 1] = 1.0 / x[i];
+}
+
 static double ulps(double a, double b) {
     if (a == b) return 0;
     if (!std::isfinite(a) || !std::isfinite(b)) return 1e30;
@@ -89,8 +97,20 @@ int main() {
         df_c = fmax(df_c, o[4 * i + 2]);
         if (std::isfinite(o[4 * i + 3])) df_q = fmax(df_q, o[4 * i + 3]);
     }
+    // reciprocals over magnitudes 2^-500 .. 2^500 of both signs
+    std::vector<double> rx(n);
+    for (int i = 0; i < n; ++i) {
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        const double u = (s >> 11) * (1.0 / 9007199254740992.0);
+        rx[i] = ((s >> 3) & 1 ? -1.0 : 1.0) * ldexp(1.0 + u, (int)((s >> 40) % 1001) - 500);
+    }
+    cudaMemcpy(dx, rx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    eval_rcp<<<(n + 255) / 256, 256>>>(dx, n, dout);
+    cudaMemcpy(o.data(), dout, 2 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+    double rcp_u = 0;
+    for (int i = 0; i < n; ++i) rcp_u = fmax(rcp_u, ulps(o[2 * i], o[2 * i + 1]));
     printf("exp_ulp %g sin_ulp %g cos_ulp %g sin_abs %g cos_abs %g df_exp_rel %g df_sin_abs %g df_cos_abs %g "
-           "df_div_rel %g err %s\n",
-           me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, cudaGetErrorString(cudaGetLastError()));
+           "df_div_rel %g rcp_ulp %g err %s\n",
+           me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, rcp_u, cudaGetErrorString(cudaGetLastError()));
     return 0;
 }

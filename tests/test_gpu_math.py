@@ -3,7 +3,9 @@ against CUDA's exp and sincospi, on the GPU: <= 2 ulp, and sin/cos within
 2.3e-16 absolute near their zeros (where ulp counts are meaningless).  The
 double-float versions (csrc/df64.cuh) against the same FP64 functions:
 exp, sin and cos within 2e-14 (a few units of the 48-bit significand), the
-division (one correction step, ~2^-45) within 5e-14."""
+division (one correction step, ~2^-45) within 5e-14.  The FP64 reciprocal
+(csrc/fp64_math.cuh fast_rcp: the hardware approximation and two
+Newton-Raphson steps) within 1 ulp of the IEEE quotient."""
 import os
 import subprocess
 
@@ -27,3 +29,4 @@ def test_fast_math_against_cuda(tmp_path):
     assert float(vals["df_exp_rel"]) <= 2e-14
     assert float(vals["df_sin_abs"]) <= 2e-14 and float(vals["df_cos_abs"]) <= 2e-14
     assert float(vals["df_div_rel"]) <= 5e-14
+    assert float(vals["rcp_ulp"]) <= 1

@@ -584,6 +584,7 @@ def run_engine(args, rank, world, local):
     k_df = float(np.mean(results["mixed_df"]["kernel_ms"]))
     from raptor_gb300 import workload
     flop = workload.image_flops(st["rays"], st["steps"], st["rt_samples"], 1, rk4=True)
+    flop_sym = workload.image_flops_symmetric(st["steps"], st["rt_samples"], 1)
     achieved = flop / (k_fp64 * 1e-3) / 1e12
 
     vjp = batch = incl17 = diff = None
@@ -623,7 +624,11 @@ def run_engine(args, rank, world, local):
                      "traffic_unit": "bytes per launch",
                      "peak_source": "measured DFMA loop on this GPU (MEASURED_PEAKS.json has no FP64 figure); "
                                     f"nominal {NOMINAL_FP64_TFLOPS} TFLOP/s",
-                     "flop_per_launch": flop, "kernel_ms": k_fp64},
+                     "flop_per_launch": flop, "kernel_ms": k_fp64,
+                     # the same with the symmetric hand count of the algorithm
+                     # (1,260 per RK4 step, 316 + 63 F per sample)
+                     "flop_per_launch_symmetric": flop_sym,
+                     "frac_symmetric": (flop_sym / (k_fp64 * 1e-3) / 1e12) / peak.value if peak.value > 0 else None},
         "clocks": clocks,
         "forms": {
             "fp64": {"ms_per_image": t_fp64, "kernel_ms": k_fp64, "rays_per_s": W * H / (t_fp64 * 1e-3),

@@ -21,19 +21,23 @@ namespace raptor {
 
 #include "math_tables.inc"
 
-// 1/x for normal x: the hardware's approximate FP64 reciprocal
-// (rcp.approx.ftz.f64, about 20 correct bits from the high word) refined by
-// two Newton-Raphson steps y <- y + y (1 - x y), each of which squares the
-// relative error; within an ulp of the correctly rounded quotient (tested on
-// the GPU by tests/test_gpu_math.py).  Five FP64-pipe instructions where an
-// IEEE division takes about twice as many.
+// 1/x: the hardware's approximate FP64 reciprocal (rcp.approx.ftz.f64,
+// about 20 correct bits from the high word) refined by two Newton-Raphson
+// steps y <- y + y (1 - x y), each of which squares the relative error;
+// within an ulp of the correctly rounded quotient for normal x (tested on
+// the GPU by tests/test_gpu_math.py).  Zero, infinity and NaN take the
+// approximation itself (infinity, zero, NaN, as IEEE division gives them;
+// subnormal x gives infinity).  Five FP64-pipe instructions and an integer
+// test where an IEEE division takes about twice as many.
 __device__ __forceinline__ double fast_rcp(double x) {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
     double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    return fma(y, e, y);
+    const double y1 = fma(y, e, y);
+    e = fma(-x, y1, 1.0);
+    const double y2 = fma(y1, e, y1);
+    const unsigned ex = (unsigned)__double2hiint(x) & 0x7ff00000u;
+    return (ex == 0u || ex == 0x7ff00000u) ? y : y2;
 }
 
 // 1/x in the templated geodesic and dual code: fast_rcp for FP64, FP32

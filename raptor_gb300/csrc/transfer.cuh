@@ -219,10 +219,10 @@ __device__ __forceinline__ bool fluid_fast(const T v[8], const MetricT<T>& g, co
     const T Q = h2 + D2;
     const T A = r_high * h2 + r_low * D2 + Q;
     const T C = A + Q;
-    const T iAC = 1.0 / (A * C);
+    const T iAC = recip(A * C);
     const T two_temp_gam = 0.5 * ((1.0 + 2.0 / 3.0 * (A * A * iAC)) + 4.0 / 3.0);
     const T Thetae_unit = (two_temp_gam - 1.0) * (kPMass / kEMass) * (Q * C * iAC);
-    const T irho = 1.0 / rho;
+    const T irho = recip(rho);
     fl.irho = irho;
     T th = (uu * irho) * Thetae_unit;
     if (th < 0.0) th = T(tiny);
@@ -269,7 +269,7 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     // pitch_angle (radiative_transfer.c:32-47): cosine, clamped to [-1, 1].
     // 1/(k.u |B|) gives the cosine's 1/(|k.u| |B|) (|B| > 0) and 1/(k.u).
     const double Bn = fl.B * im.inv_B_unit;
-    const double ikB = 1.0 / (kU * Bn);
+    const double ikB = recip(kU * Bn);
     double pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) * fabs(ikB);
     if (fabs(pitch) > 1.0) pitch /= fabs(pitch);
     const double sth = sqrt(1.0 - pitch * pitch);
@@ -281,9 +281,9 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     // once per sample (nu_s / Theta^2 taken as (2/9) nu_c sin(theta))
     const double jpre = fl.ne * (1.4142135623730951 * CUDART_PI / 6.0 * (2.0 / 9.0) * kE2C) * (nuc * sth);
     // h nu / (k T) = nu h / (m_e c^2 Theta_e)
-    const double hkt = (kPlanck / (kEMass * kC * kC)) / fl.thetae;
+    const double hkt = (kPlanck / (kEMass * kC * kC)) * recip(fl.thetae);
     // 1/nu_s, and 1/nu_p^2 = (1/(k.u))^2 / nu^2, once per sample
-    const double inus = 1.0 / nus;
+    const double inus = recip(nus);
     const double ikU = ikB * Bn;
     const double ikU2 = ikU * ikU;
     // one copy of the frequency body (5 frequencies: 7 % faster than unrolled)

@@ -16,6 +16,13 @@ tests/test_flop_count.py).  Convention: each +, -, *, / and each libm call
 
 FLOP_RAY_SETUP = 138
 FLOP_RK4_STEP = 1648
+# The survey's hand count of the same algorithm with the connection's
+# symmetry used (40 unique symbols, symmetric contraction): 1,260 per RK4
+# step and 316 + 63 F per sample.  A lower bar for "achieved", reported
+# beside the operation count above.
+FLOP_RK4_STEP_SYMMETRIC = 1260
+FLOP_SAMPLE_BASE_SYMMETRIC = 316
+FLOP_SAMPLE_PER_FREQ_SYMMETRIC = 63
 FLOP_RK2_STEP = 814
 FLOP_SAMPLE_BASE = 388
 FLOP_SAMPLE_PER_FREQ = 109
@@ -25,3 +32,9 @@ def image_flops(rays: int, steps: int, samples: int, n_freq: int, rk4: bool = Tr
     """FP64 operations the reference's algorithm spends on one render."""
     step = FLOP_RK4_STEP if rk4 else FLOP_RK2_STEP
     return float(FLOP_RAY_SETUP * rays + step * steps + (FLOP_SAMPLE_BASE + FLOP_SAMPLE_PER_FREQ * n_freq) * samples)
+
+
+def image_flops_symmetric(steps: int, samples: int, n_freq: int) -> float:
+    """The same render's work by the symmetric hand count (RK4)."""
+    return float(FLOP_RK4_STEP_SYMMETRIC * steps +
+                 (FLOP_SAMPLE_BASE_SYMMETRIC + FLOP_SAMPLE_PER_FREQ_SYMMETRIC * n_freq) * samples)

@@ -104,11 +104,16 @@ int main() {
         const double u = (s >> 11) * (1.0 / 9007199254740992.0);
         rx[i] = ((s >> 3) & 1 ? -1.0 : 1.0) * ldexp(1.0 + u, (int)((s >> 40) % 1001) - 500);
     }
+    const double special[] = {0.0, -0.0, INFINITY, -INFINITY, NAN};
+    for (int k = 0; k < 5; ++k) rx[k] = special[k];
     cudaMemcpy(dx, rx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
     eval_rcp<<<(n + 255) / 256, 256>>>(dx, n, dout);
     cudaMemcpy(o.data(), dout, 2 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
     double rcp_u = 0;
-    for (int i = 0; i < n; ++i) rcp_u = fmax(rcp_u, ulps(o[2 * i], o[2 * i + 1]));
+    for (int k = 0; k < 4; ++k)  // IEEE's infinities and zeros, signs included
+        if (!(o[2 * k] == o[2 * k + 1]) || std::signbit(o[2 * k]) != std::signbit(o[2 * k + 1])) rcp_u = 1e30;
+    if (!(o[8] != o[8])) rcp_u = 1e30;  // NaN stays NaN
+    for (int i = 5; i < n; ++i) rcp_u = fmax(rcp_u, ulps(o[2 * i], o[2 * i + 1]));
     printf("exp_ulp %g sin_ulp %g cos_ulp %g sin_abs %g cos_abs %g df_exp_rel %g df_sin_abs %g df_cos_abs %g "
            "df_div_rel %g rcp_ulp %g err %s\n",
            me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, rcp_u, cudaGetErrorString(cudaGetLastError()));

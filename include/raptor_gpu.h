@@ -60,6 +60,11 @@ extern "C" {
 #define RAPTOR_RK4 4
 #define RAPTOR_RK2 2
 
+/* emission models: the fits that emission_coeff (j_nu.c:20-26) returns */
+#define RAPTOR_EMISSION_THERMAL 0 /* thermal synchrotron, j_nu.c:130-153, 188-200 (the reference's) */
+#define RAPTOR_EMISSION_KAPPA 1   /* kappa distribution, kappa = 3.5, j_nu.c:28-106 (defined in the
+                                     reference but not called by it); FP64 form, renders only */
+
 /* camera maps (parameters.h:54-55) */
 #define RAPTOR_CAM_LINEAR 0 /* LINEAR_IMPACT_CAM: uniform grid of impact parameters (integrator.c:186-190) */
 #define RAPTOR_CAM_LOG 1    /* LOG_IMPACT_CAM: log-polar grid, x -> radius, y -> angle (integrator.c:191-198) */
@@ -107,6 +112,7 @@ typedef struct raptor_image_desc {
     int n_freq;                   /* 1..RAPTOR_MAX_FREQS */
     double freq[RAPTOR_MAX_FREQS]; /* Hz */
     int camera;                   /* RAPTOR_CAM_LINEAR (0) or RAPTOR_CAM_LOG */
+    int emission;                 /* RAPTOR_EMISSION_THERMAL (0) or RAPTOR_EMISSION_KAPPA */
 } raptor_image_desc;
 
 typedef struct raptor_gpu_stats {
@@ -249,7 +255,7 @@ int raptor_gpu_vjp_range(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
  * larger than RAPTOR_NOALLOC_MAX_IMAGES is rejected with
  * RAPTOR_ERR_NOALLOC_LIMIT; other bad arguments with RAPTOR_ERR_INVALID. */
 #define RAPTOR_NOALLOC_MAX_IMAGES 16
-#define RAPTOR_NOALLOC_SCRATCH_BYTES 16384
+#define RAPTOR_NOALLOC_SCRATCH_BYTES 20480
 #define RAPTOR_ERR_NOALLOC_LIMIT (-6)
 int raptor_gpu_render_noalloc(int device, const double *d_cells, const raptor_grid_geom *geom,
                               const raptor_image_desc *imgs, int n_imgs, double *d_I_out, double *d_spectrum_out,

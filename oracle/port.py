@@ -28,7 +28,7 @@ class PortScene(ctypes.Structure):
                 ("inclination", ctypes.c_double), ("stepsize", ctypes.c_double),
                 ("mbh", ctypes.c_double), ("m_unit", ctypes.c_double),
                 ("r_high", ctypes.c_double), ("r_low", ctypes.c_double),
-                ("integrator", ctypes.c_int), ("camera", ctypes.c_int)]
+                ("integrator", ctypes.c_int), ("camera", ctypes.c_int), ("emission", ctypes.c_int)]
 
 
 class PortRayStats(ctypes.Structure):
@@ -65,6 +65,11 @@ def load() -> ctypes.CDLL:
     lib.port_j_thsynch.restype = D
     lib.port_a_th.argtypes = [D, D, D]
     lib.port_a_th.restype = D
+    for name in ("port_j_kappa", "port_a_kappa"):
+        getattr(lib, name).argtypes = [D, D, D, D, D]
+        getattr(lib, name).restype = D
+    lib.port_hyp2f1.argtypes = [D, D, D, D]
+    lib.port_hyp2f1.restype = D
     lib.port_fluid.argtypes = [S, P(D), P(D)]
     lib.port_fluid.restype = ctypes.c_int
     lib.port_trace_ray.argtypes = [S, ctypes.c_int, P(D), ctypes.c_int, ctypes.c_int, P(D)]
@@ -82,13 +87,13 @@ class Scene:
 
     def __init__(self, geom, prims, width, height, cam_size_x=40.0, cam_size_y=40.0,
                  inclination=60.0, stepsize=0.05, mbh=8.9505e39, m_unit=1e19, r_high=3.0,
-                 r_low=3.0, integrator=4, camera=0):
+                 r_low=3.0, integrator=4, camera=0, emission=0):
         self.prims = np.ascontiguousarray(prims, dtype=np.float64)
         assert self.prims.shape == (8, geom.n1, geom.n2)
         self.c = PortScene(geom.n1, geom.n2, geom.startx1, geom.startx2, geom.dx1, geom.dx2,
                            geom.a, geom.hslope, geom.R0, _dp(self.prims), width, height,
                            cam_size_x, cam_size_y, inclination, stepsize, mbh, m_unit,
-                           r_high, r_low, integrator, camera)
+                           r_high, r_low, integrator, camera, emission)
         self.lib = load()
 
     def render(self, freqs, pixels=None, nthreads=0, with_stats=False):

@@ -381,6 +381,85 @@ double port_j_thsynch(double B, double costh, double thetae, double nu, double n
     return j * K_E2C;
 }
 
+/* ---- Gauss hypergeometric function 2F1(a, b; c; x), in place of GSL's
+ * gsl_sf_hyperg_2F1 at the kappa absorptivity's call sites (j_nu.c:85-96;
+ * GSL is unpinned and absent here): the power series
+ * sum_n (a)_n (b)_n / ((c)_n n!) x^n for 0 <= x <= 1/2, Pfaff's
+ * transformation 2F1(a, b; c; x) = (1 - x)^-a 2F1(a, c - b; c; x / (x - 1))
+ * for -1 <= x < 0 (which maps x into [0, 1/2]); the reference calls it only
+ * on [-1, 1/2).  Checked against scipy's hyp2f1 by tests/test_oracle.py. ---- */
+#ifndef PORT_COUNT_FLOPS /* the operation count covers the thermal path only */
+double port_hyp2f1(double a, double b, double c, double x)
+{
+    if (x < 0)
+        return pow(1 - x, -a) * port_hyp2f1(a, c - b, c, x / (x - 1));
+    double term = 1.0, sum = 1.0;
+    for (int n = 0; n < 400; n++) {
+        term *= (a + n) * (b + n) / ((c + n) * (n + 1)) * x;
+        sum += term;
+        if (fabs(term) <= 1e-17 * fabs(sum))
+            break;
+    }
+    return sum;
+}
+
+/* ---- kappa-distribution emissivity, j_nu.c:28-54 (kappa = 3.5; cos of pitch in) ---- */
+double port_j_kappa(double nu, double ne, double thetae, double B, double costh)
+{
+    double kappa = 3.5;
+    double w = thetae;
+    double nuc = K_ECHARGE * B / (2. * K_PI * K_EMASS * K_CLIGHT);
+    double sth = sqrt(1 - costh * costh);
+    double factor = (ne * pow(K_ECHARGE, 2.) * nuc * sth) / K_CLIGHT;
+    double nus = nuc * sth * pow(w * kappa, 2);
+    if (nu == 1.0 || fabs(costh) == 1)
+        return 0;
+    double X = nu / nus;
+    double J_low = pow(X, 1. / 3.) * 4 * K_PI * tgamma(kappa - 4. / 3.) / (pow(3, 7. / 3.) * tgamma(kappa - 2.));
+    double J_high = pow(X, -(kappa - 2) / 2.) * pow(3, (kappa - 1) / 2.) * (kappa - 2.) * (kappa - 1.) / 4. *
+                    tgamma(kappa / 4. - 1. / 3.) * tgamma(kappa / 4. + 4. / 3.);
+    double x = 3 * pow(kappa, -3. / 2.);
+    double J_s = pow((pow(J_low, -x) + pow(J_high, -x)), -1. / x);
+    return J_s * factor;
+}
+
+/* ---- kappa-distribution absorptivity, j_nu.c:56-106 ---- */
+double port_a_kappa(double nu, double ne, double thetae, double B, double costh)
+{
+    double kappa = 3.5;
+    double w = thetae;
+    double nuc = K_ECHARGE * B / (2. * K_PI * K_EMASS * K_CLIGHT);
+    double sth = sqrt(1 - costh * costh);
+    double factor = ne * K_ECHARGE / (B * sth);
+    if (nu == 1.0 || fabs(costh) == 1.)
+        return 0;
+    double nus = nuc * sth * pow(w * kappa, 2);
+    double X = nu / nus;
+    double a = kappa - 1. / 3., b = kappa + 1., c = kappa + 2. / 3., z = -kappa * w;
+    double hyp2F1;
+    if (fabs(z) == 1.)
+        return 0;
+    if (fabs(z) > 1.)
+        hyp2F1 = pow(1. - z, -a) * tgamma(c) * tgamma(b - a) / (tgamma(b) * tgamma(c - a)) *
+                     port_hyp2f1(a, c - b, a - b + 1., 1. / (1. - z)) +
+                 pow(1. - z, -b) * tgamma(c) * tgamma(a - b) / (tgamma(a) * tgamma(c - b)) *
+                     port_hyp2f1(b, c - a, b - a + 1., 1. / (1. - z));
+    else
+        hyp2F1 = port_hyp2f1(a, b, c, z);
+    double A_low = pow(X, -5. / 3.) * pow(3, 1. / 6.) * (10. / 41.) * pow(2 * K_PI, 2) / pow(w * kappa, 16. / 3. - kappa) *
+                   (kappa - 2.) * (kappa - 1.) * kappa / (3. * kappa - 1.) * tgamma(5. / 3.) * hyp2F1;
+    double A_high = pow(X, -(3. + kappa) / 2.) * (pow(K_PI, 5. / 2.) / 3.) *
+                    ((kappa - 2.) * (kappa - 1.) * kappa / pow(w * kappa, 5.)) *
+                    (2 * tgamma(2. + kappa / 2.) / (2. + kappa) - 1.) * (pow(3. / kappa, 19. / 4.) + 3. / 5.);
+    double x = pow(-7. / 4. + 8. * kappa / 5., -43. / 50.);
+    double A_s = pow((pow(A_low, -x) + pow(A_high, -x)), -1. / x);
+    return factor * A_s;
+}
+#else
+double port_j_kappa(double nu, double ne, double thetae, double B, double costh) { return 0.0 * (nu + ne + thetae + B + costh); }
+double port_a_kappa(double nu, double ne, double thetae, double B, double costh) { return 0.0 * (nu + ne + thetae + B + costh); }
+#endif
+
 /* ---- Kirchhoff absorptivity with the Planck function, j_nu.c:188-200 ---- */
 double port_a_th(double j, double nu, double thetae)
 {
@@ -545,8 +624,14 @@ static int transfer(const ray_ctx *c, const double X[4], const double k[4], doub
         if (nup <= 0.0)
             nup = 1.0;
         double nup2 = nup * nup;
-        double j = port_j_thsynch(fs.B, pitch, fs.thetae, nup, fs.ne);
-        double an = port_a_th(j, nup, fs.thetae);
+        double j, an;
+        if (c->s->emission == 1) { /* the kappa fits in emission_coeff's place */
+            j = port_j_kappa(nup, fs.ne, fs.thetae, fs.B, pitch);
+            an = port_a_kappa(nup, fs.ne, fs.thetae, fs.B, pitch);
+        } else {
+            j = port_j_thsynch(fs.B, pitch, fs.thetae, nup, fs.ne);
+            an = port_a_th(j, nup, fs.thetae);
+        }
         double dlf = dl * c->Rg / (freqs[f]);
         double dtau = (nup * an * dlf);
         tau[f] += dtau;

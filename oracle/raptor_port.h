@@ -26,6 +26,7 @@ typedef struct port_scene {
     double mbh, m_unit, r_high, r_low;
     int integrator; /* 4 = RK4 (integrator.c:13-41), 2 = RK2 (integrator.c:44-70) */
     int camera;     /* 0 = LINEAR_IMPACT_CAM, 1 = LOG_IMPACT_CAM (parameters.h:54-55) */
+    int emission;   /* 0 = the thermal fits emission_coeff calls (j_nu.c:20-26), 1 = the kappa fits (j_nu.c:28-106) */
 } port_scene;
 
 typedef struct port_ray_stats {
@@ -55,6 +56,9 @@ void port_init_photon(const port_scene *s, double alpha, double beta, double pho
 double port_camera_x2(const port_scene *s);
 double port_j_thsynch(double B, double costh, double thetae, double nu, double ne);
 double port_a_th(double j, double nu, double thetae);
+double port_hyp2f1(double a, double b, double c, double x);
+double port_j_kappa(double nu, double ne, double thetae, double B, double costh);
+double port_a_kappa(double nu, double ne, double thetae, double B, double costh);
 int port_fluid(const port_scene *s, const double X[4], double out[12]);
 
 #ifdef __cplusplus

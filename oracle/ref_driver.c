@@ -147,3 +147,14 @@ int ref_scale_prim(int q, int i, int j, double factor)
     p[q][i][j][0] *= factor;
     return 0;
 }
+
+/* The reference's kappa-distribution fits (j_nu.c:28-106), which its
+ * emission_coeff does not call: out[0] = emission_coeff_kappa_FIT,
+ * out[1] = absorption_coeff_kappa_FIT at one plasma state (theta: the
+ * cosine of the pitch angle, as radiative_transfer.c:67 passes it; beta is
+ * unused by both). */
+void ref_kappa_coeffs(double nu, double ne, double thetae, double B, double theta, double *out)
+{
+    out[0] = emission_coeff_kappa_FIT(nu, ne, thetae, B, 0.0, theta);
+    out[1] = absorption_coeff_kappa_FIT(nu, ne, thetae, B, 0.0, theta);
+}

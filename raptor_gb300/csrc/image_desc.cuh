@@ -28,6 +28,20 @@ constexpr double kGGrav = 6.6742e-8;
 constexpr double kE2C = 7.695589048e-30;
 constexpr double kE2CH = 1.161410e-03;
 
+constexpr int kEmissionThermal = 0;  // RAPTOR_EMISSION_THERMAL
+constexpr int kEmissionKappa = 1;    // RAPTOR_EMISSION_KAPPA
+constexpr double kKappa = 3.5;       // j_nu.c:35, 62
+
+// The kappa-distribution fits' constants for one image (host, FP64; see
+// kappa.cuh and build_dev_image).
+struct KappaConst {
+    double ln_jlow, ln_jhigh;  // ln of the X-independent factors of J_low, J_high
+    double xj;                 // the emissivity's blend exponent 3 kappa^-3/2
+    double ln_alow, ln_ahigh;  // ln of the X- and Theta_e-independent factors of A_low, A_high
+    double xa;                 // the absorptivity's blend exponent (-7/4 + 8 kappa/5)^(-43/50)
+    double g1, g2;             // the connection formula's gamma-function ratios
+};
+
 struct DevImage {
     long long ray_begin;   // first global ray of this image
     long long out_offset;  // first double of this image in the output
@@ -69,6 +83,9 @@ struct DevImage {
     // output double, and the word a failed check is recorded in
     long long out_end;
     unsigned long long* check_word;
+    // emission model: kEmissionThermal, or kEmissionKappa with its constants
+    int emission;
+    KappaConst kap;
 };
 
 // Per-step record of one traced ray (the analogue of the reference's GEOD

@@ -86,6 +86,8 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "integrator %d is neither RK4 (4) nor RK2 (2)", d.integrator);
     if (d.camera != RAPTOR_CAM_LINEAR && d.camera != RAPTOR_CAM_LOG)
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "camera %d is neither linear (0) nor log-polar (1)", d.camera);
+    if (d.emission != RAPTOR_EMISSION_THERMAL && d.emission != RAPTOR_EMISSION_KAPPA)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "emission %d is neither thermal (0) nor kappa (1)", d.emission);
     if (!finite_all({d.cam_size_x, d.cam_size_y, d.inclination, d.mbh, d.m_unit, d.r_high, d.r_low, d.stepsize}) ||
         !(d.stepsize > 0) || !(d.mbh > 0) || !(d.m_unit > 0))
         return ctx_fail(ctx, RAPTOR_ERR_INVALID, "non-finite or non-positive image parameter");
@@ -179,6 +181,25 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
         im.inv_freq2[f] = 1.0 / (d.freq[f] * d.freq[f]);
         im.freq_f[f] = (float)im.freq[f];
         im.rg_over_nu_f[f] = (float)im.rg_over_nu[f];
+    }
+    // kappa-distribution fits (j_nu.c:28-106): the constant factors, in the
+    // reference's own expressions, as logarithms
+    im.emission = d.emission;
+    if (d.emission == RAPTOR_EMISSION_KAPPA) {
+        const double k = kKappa;
+        KappaConst& kc = im.kap;
+        kc.ln_jlow = log(4. * M_PI * std::tgamma(k - 4. / 3.) / (pow(3., 7. / 3.) * std::tgamma(k - 2.)));
+        kc.ln_jhigh = log(pow(3., (k - 1) / 2.) * (k - 2.) * (k - 1.) / 4. * std::tgamma(k / 4. - 1. / 3.) *
+                          std::tgamma(k / 4. + 4. / 3.));
+        kc.xj = 3 * pow(k, -3. / 2.);
+        kc.ln_alow = log(pow(3, 1. / 6.) * (10. / 41.) * pow(2 * M_PI, 2) * (k - 2.) * (k - 1.) * k / (3. * k - 1.) *
+                         std::tgamma(5. / 3.));
+        kc.ln_ahigh = log((pow(M_PI, 5. / 2.) / 3.) * ((k - 2.) * (k - 1.) * k) *
+                          (2 * std::tgamma(2. + k / 2.) / (2. + k) - 1.) * (pow(3. / k, 19. / 4.) + 3. / 5.));
+        kc.xa = pow(-7. / 4. + 8. * k / 5., -43. / 50.);
+        const double ka = k - 1. / 3., kb = k + 1., kcc = k + 2. / 3.;
+        kc.g1 = std::tgamma(kcc) * std::tgamma(kb - ka) / (std::tgamma(kb) * std::tgamma(kcc - ka));
+        kc.g2 = std::tgamma(kcc) * std::tgamma(ka - kb) / (std::tgamma(ka) * std::tgamma(kcc - kb));
     }
     im.ne_unit_f = (float)im.Ne_unit;
     im.b_unit_f = (float)im.B_unit;
@@ -623,6 +644,10 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, imgs, n_imgs, b);
     if (rc) return rc;
+    if (precision != RAPTOR_PREC_FP64)
+        for (int k = 0; k < n_imgs; ++k)
+            if (imgs[k].emission == RAPTOR_EMISSION_KAPPA)
+                return ctx_fail(ctx, RAPTOR_ERR_INVALID, "image %d: the kappa emission model renders in FP64 only", k);
     long long rb = ray_begin < 0 ? 0 : ray_begin;
     long long re = ray_count < 0 ? b.total_rays : std::min(b.total_rays, rb + ray_count);
     if (rb > b.total_rays) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "ray range starts past the batch");
@@ -689,6 +714,8 @@ extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, img, 1, b);
     if (rc) return rc;
+    if (precision != RAPTOR_PREC_FP64 && img->emission == RAPTOR_EMISSION_KAPPA)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "the kappa emission model traces in FP64 only");
     const size_t bytes = sizeof(double) * (size_t)max_records * kTraceWidth;
     rc = ensure_buffer(ctx, (void**)&ctx->d_trace, &ctx->trace_cap, bytes);
     if (rc) return rc;

@@ -17,6 +17,7 @@
 //    inside FP32's range; e2_c is applied once per ray in FP64.
 #pragma once
 #include "image_desc.cuh"
+#include "kappa.cuh"
 
 namespace raptor {
 
@@ -272,6 +273,24 @@ __device__ __forceinline__ bool rt_terms_fp64(const DevImage& im, const double y
     const double ikB = recip(kU * Bn);
     double pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) * fabs(ikB);
     if (fabs(pitch) > 1.0) pitch /= fabs(pitch);
+    if (im.emission == kEmissionKappa) {
+        // the kappa fits (kappa.cuh) in place of the thermal ones:
+        // dtau = nu_p a_nu dl_f and j_nu / nu_p^2, radiative_transfer.c:87-90
+        const KappaSample ks = kappa_sample(im.kap, fl.B, pitch, fl.thetae, fl.ne);
+        const double ikU = ikB * Bn;
+        const double ikU2 = ikU * ikU;
+#pragma unroll 1
+        for (int f = 0; f < NF; ++f) {
+            if (f >= im.nfreq) break;
+            double nup = -kU * im.freq[f];
+            if (nup <= 0.0) nup = 1.0;
+            double j, a;
+            kappa_coeffs(im.kap, ks, nup, j, a);
+            dtau[f] = nup * a * (adl * im.rg_over_nu[f]);
+            jn[f] = j * (ikU2 * im.inv_freq2[f]);  // 1/nu_p^2 where j != 0 (nu_p not the sentinel)
+        }
+        return true;
+    }
     const double sth = sqrt(1.0 - pitch * pitch);
     const double nuc = fl.B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
     const double nus = (2.0 / 9.0) * nuc * fl.thetae * fl.thetae * sth;

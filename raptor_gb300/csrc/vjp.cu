@@ -766,6 +766,8 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, img, 1, b);
     if (rc) return rc;
+    if (img->emission != RAPTOR_EMISSION_THERMAL)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: the adjoint covers the thermal emission model only");
     const DevImage& him = b.host[0];
     const GridSlot& gs = ctx->grids[img->grid];
     const long long ncell = (long long)gs.geom.n1 * gs.geom.n2;

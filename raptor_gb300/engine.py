@@ -30,6 +30,8 @@ RK4 = 4
 RK2 = 2
 CAM_LINEAR = 0
 CAM_LOG = 1
+EMISSION_THERMAL = 0
+EMISSION_KAPPA = 1
 TRACE_WIDTH = 16
 
 STATUS = {0: "OK", -1: "INVALID", -2: "CUDA", -3: "DEVICE", -4: "NOMEM", -5: "NODEVICE", -6: "NOALLOC_LIMIT",
@@ -71,7 +73,8 @@ class ImageDesc(ctypes.Structure):
                 ("cam_size_y", ctypes.c_double), ("inclination", ctypes.c_double), ("mbh", ctypes.c_double),
                 ("m_unit", ctypes.c_double), ("r_high", ctypes.c_double), ("r_low", ctypes.c_double),
                 ("stepsize", ctypes.c_double), ("integrator", ctypes.c_int), ("grid", ctypes.c_int),
-                ("n_freq", ctypes.c_int), ("freq", ctypes.c_double * RAPTOR_MAX_FREQS), ("camera", ctypes.c_int)]
+                ("n_freq", ctypes.c_int), ("freq", ctypes.c_double * RAPTOR_MAX_FREQS), ("camera", ctypes.c_int),
+                ("emission", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -138,14 +141,16 @@ def _dp(a: np.ndarray | None):
 
 def image_desc(width, height, freqs: Sequence[float], grid: int = 0, inclination=60.0, cam_size_x=40.0,
                cam_size_y=40.0, mbh=8.9505e39, m_unit=1e19, r_high=3.0, r_low=3.0, stepsize=0.05,
-               integrator=RK4, camera=0) -> ImageDesc:
-    """camera: CAM_LINEAR (0, the reference's default) or CAM_LOG (1)."""
+               integrator=RK4, camera=0, emission=EMISSION_THERMAL) -> ImageDesc:
+    """camera: CAM_LINEAR (0, the reference's default) or CAM_LOG (1);
+    emission: EMISSION_THERMAL (0, the reference's) or EMISSION_KAPPA (1,
+    the kappa = 3.5 fits, FP64 renders)."""
     freqs = list(np.atleast_1d(freqs).astype(float))
     if not 1 <= len(freqs) <= RAPTOR_MAX_FREQS:
         raise ValueError(f"1..{RAPTOR_MAX_FREQS} frequencies per image")
     fa = (ctypes.c_double * RAPTOR_MAX_FREQS)(*(freqs + [0.0] * (RAPTOR_MAX_FREQS - len(freqs))))
     return ImageDesc(width, height, cam_size_x, cam_size_y, inclination, mbh, m_unit, r_high, r_low,
-                     stepsize, integrator, grid, len(freqs), fa, camera)
+                     stepsize, integrator, grid, len(freqs), fa, camera, emission)
 
 
 class Engine:

@@ -83,7 +83,7 @@ def build(out_dir: str, n1: int = 64, n2: int = 64, rk: str = "RK4", lib_dir: st
            ["-I" + work, "-I" + os.path.join(ORACLE, "ref_stubs"), "-I" + os.path.join(ROOT, "include"),
             "-include", os.path.join(ORACLE, "ref_config.h"), f"-DREF_N1={n1}", f"-DREF_N2={n2}",
             f"-DREF_INT_METHOD={rk}"] +
-           [os.path.join(work, f) for f in SOURCES] + [os.path.join(ORACLE, "ref_stubs", "gsl_abort_stub.c")] +
+           [os.path.join(work, f) for f in SOURCES] + [os.path.join(ORACLE, "ref_stubs", "gsl_hyperg_stub.c")] +
            ["-o", exe, "-L" + lib_dir, "-lraptor_gpu", "-Wl,-rpath," + lib_dir, "-lm"])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

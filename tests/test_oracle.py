@@ -165,3 +165,84 @@ def test_port_matches_reference_nonzero_r0(name):
     sc, freq = _scene(d, g[f"{name}_params"])
     out, _ = sc.render([freq])
     assert_fp64_parity(out[:, 0], g[f"{name}_img"], name)
+
+
+# ---- kappa-distribution emission (j_nu.c:28-106) ----
+
+def _kappa_hyp_params():
+    k = 3.5
+    a, b, c = k - 1 / 3, k + 1, k + 2 / 3
+    return a, b, c
+
+
+def test_port_hyp2f1_against_scipy():
+    """The oracle's Gauss hypergeometric function (in place of GSL's, which
+    is absent) against scipy's hyp2f1 on every argument range the kappa
+    absorptivity reaches: 2F1(a, b; c; z) for z in [-1, 0), and the
+    connection formula's two functions at w = 1/(1 - z) in (0, 1/2)."""
+    special = pytest.importorskip("scipy.special")
+    from oracle import port
+    lib = port.load()
+    a, b, c = _kappa_hyp_params()
+    worst = 0.0
+    for z in -np.geomspace(1e-6, 1.0, 300):
+        worst = max(worst, abs(lib.port_hyp2f1(a, b, c, z) / special.hyp2f1(a, b, c, z) - 1))
+    for w in np.linspace(1e-6, 0.5, 300):
+        for p, q, r in ((a, c - b, a - b + 1), (b, c - a, b - a + 1)):
+            worst = max(worst, abs(lib.port_hyp2f1(p, q, r, w) / special.hyp2f1(p, q, r, w) - 1))
+    assert worst < 1e-13, worst
+
+
+def test_kappa_series_tables():
+    """csrc/kappa_tables.inc (written by csrc/gen_kappa_tables.py) holds the
+    exact power-series coefficients rounded to double, and 80 terms sum the
+    two series to scipy's hyp2f1 within 1e-14 on [0, 1/2]."""
+    import importlib.util
+    import re
+    special = pytest.importorskip("scipy.special")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("gkt", os.path.join(root, "raptor_gb300", "csrc",
+                                                                      "gen_kappa_tables.py"))
+    gkt = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gkt)
+    src = open(os.path.join(root, "raptor_gb300", "csrc", "kappa_tables.inc")).read()
+    for name, p, q, r, _ in gkt.series():
+        m = re.search(name + r"\[(\d+)\] = \{(.*?)\};", src, re.S)
+        assert m, name
+        vals = [float(t) for t in m.group(2).replace("\n", " ").split(",") if t.strip()]
+        assert len(vals) == int(m.group(1)) == gkt.N_TERMS
+        assert vals == [float(v) for v in gkt.coefficients(p, q, r)], name
+        for x in np.linspace(0.0, 0.5, 101):
+            s = 0.0
+            for v in reversed(vals):
+                s = s * x + v
+            assert abs(s / special.hyp2f1(float(p), float(q), float(r), x) - 1) < 1e-14, (name, x)
+
+
+def test_port_kappa_matches_reference_functions():
+    """The port's kappa emissivity and absorptivity against the reference's
+    own emission_coeff_kappa_FIT / absorption_coeff_kappa_FIT (built from its
+    sources with the oracle's 2F1 in GSL's place) on seeded plasma states."""
+    import ctypes
+    from oracle import port, ref
+    if not ref.available(64, 64):
+        pytest.skip("the reference's sources are not staged on this machine")
+    lib = ref.load(64, 64, "RK4")
+    lib.ref_kappa_coeffs.argtypes = [ctypes.c_double] * 5 + [ctypes.POINTER(ctypes.c_double)]
+    pl = port.load()
+    out = (ctypes.c_double * 2)()
+    rng = np.random.default_rng(35)
+    n_nonzero = 0
+    for _ in range(3000):
+        nu, ne = 10 ** rng.uniform(9, 13), 10 ** rng.uniform(2, 8)
+        th, B, cth = 10 ** rng.uniform(-2.5, 3), 10 ** rng.uniform(-2, 3), rng.uniform(-0.999, 0.999)
+        lib.ref_kappa_coeffs(nu, ne, th, B, cth, out)
+        got = (pl.port_j_kappa(nu, ne, th, B, cth), pl.port_a_kappa(nu, ne, th, B, cth))
+        for g, w in zip(got, out):
+            assert g == pytest.approx(w, rel=1e-13, abs=0.0)
+            n_nonzero += w != 0.0
+    # the special cases: the nu_p sentinel, a clamped pitch angle, |z| = 1
+    for args in ((1.0, 1e5, 10.0, 20.0, 0.3), (2e11, 1e5, 10.0, 20.0, 1.0), (2e11, 1e5, 1 / 3.5, 20.0, 0.3)):
+        lib.ref_kappa_coeffs(*args, out)
+        assert (pl.port_j_kappa(*args), pl.port_a_kappa(*args)) == (out[0], out[1])
+    assert n_nonzero > 5000

@@ -43,7 +43,7 @@ def test_kappa_image_matches_port(eng, torus64, torus256, n, w, h, freqs, incl, 
     # a different image from the thermal model's
     thermal, _ = eng.render(engine.image_desc(w, h, freqs, grid=gid, inclination=incl, camera=camera),
                             engine.PREC_FP64)
-    assert not np.allclose(thermal, img)
+    assert not np.allclose(thermal, img, rtol=1e-3, atol=0.0)
 
 
 def test_kappa_pooled_equals_in_place(torus64):

@@ -1,13 +1,19 @@
 // Double-float arithmetic ("DF") for the geodesic of the mixed-DF form.
 //
 // A DF value is the unevaluated sum hi + lo of two FP32 numbers with
-// |lo| about ulp(hi)/2 or less: a 48-bit significand (relative rounding
-// ~3.6e-15, against 1.1e-16 for FP64) with FP32's exponent range.  Sums are
-// renormalised (|lo| <= ulp(hi)/2); products are not (|lo| stays below
-// ~4 ulp(hi)), which every operation here accepts as input: that saves 3 of
-// a product's 7 instructions and made the mixed-DF render 1.4x faster with
-// the same trajectories.  Comparisons go through a renormalised difference,
-// so they hold for unnormalised operands.  GB300 runs FP64 at
+// |lo| a few ulp(hi) or less: a 48-bit significand (relative rounding
+// ~3.6e-15, against 1.1e-16 for FP64) with FP32's exponent range.  Neither
+// products nor sums are renormalised: a product's lo stays below ~4 ulp(hi),
+// a sum's is the exact error of its leading parts plus the operands' lo
+// parts, which every operation here accepts as input.  Leaving products
+// unnormalised saves 3 of a product's 7 instructions, sums 3 of 11.  A sum
+// whose leading parts cancel keeps a lo larger than ulp(hi); its rounding
+// then adds an error of the order of the one the cancellation already
+// carries.  Renormalised values (df_norm, add_norm) are kept where a value
+// accumulates over many steps (the photon state) or where its leading part
+// is read alone (sin and cos of a point, the cell coordinate); comparisons
+// and signs read hi + lo rounded to FP32, which has the sign of the exact
+// value.  GB300 runs FP64 at
 // 2 operations per clock per SM and FP32 at 128, so a DF operation built
 // from 6-11 FP32 instructions costs the SM far less than one FP64
 // instruction.  The algorithms are the classical error-free
@@ -53,15 +59,23 @@ __device__ __forceinline__ DF quick_two_sum(float a, float b) {
 // ------------------------------------------------------------ arithmetic
 __device__ __forceinline__ DF operator-(DF a) { return DF{-a.hi, -a.lo}; }
 
+// sums: the exact sum of the leading parts, the lo parts added to its error
 __device__ __forceinline__ DF operator+(DF a, DF b) {
     const DF s = two_sum(a.hi, b.hi);
-    return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+    return DF{s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
 }
 __device__ __forceinline__ DF add_f(DF a, float b) {
     const DF s = two_sum(a.hi, b);
-    return quick_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+    return DF{s.hi, __fadd_rn(s.lo, a.lo)};
 }
 __device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+
+// |lo| <= ulp(hi)/2 again
+__device__ __forceinline__ DF df_norm(DF a) { return quick_two_sum(a.hi, a.lo); }
+// a renormalised sum (the photon state's updates)
+__device__ __forceinline__ DF add_norm(DF a, DF b) { return df_norm(a + b); }
+// the value rounded to FP32
+__device__ __forceinline__ float df_value(DF a) { return __fadd_rn(a.hi, a.lo); }
 
 // products: the exact product of the leading parts plus the cross terms,
 // left unnormalised
@@ -86,12 +100,11 @@ __device__ __forceinline__ float rcp_refined(float b) {
     return __fmul_rn(r, __fmaf_rn(-b, r, 2.0f));
 }
 
-// a / b: q1 = a.hi / b, one DF correction (relative error ~2^-46).
+// a / b: q1 = a / b in FP32, one DF correction (relative error ~2^-46).
 __device__ __forceinline__ DF operator/(DF a, DF b) {
-    const float rb = rcp_refined(b.hi);
-    const float q1 = __fmul_rn(a.hi, rb);
-    const DF r = a - mul_f(b, q1);
-    const float q2 = __fmul_rn(r.hi, rb);
+    const float rb = rcp_refined(df_value(b));
+    const float q1 = __fmul_rn(df_value(a), rb);
+    const float q2 = __fmul_rn(df_value(a - mul_f(b, q1)), rb);
     return quick_two_sum(q1, q2);
 }
 
@@ -126,15 +139,15 @@ __device__ __forceinline__ DF fma(DF a, DF b, DF c) { return a * b + c; }
 __device__ __forceinline__ DF fma(DF a, DF b, double c) { return a * b + c; }
 
 // ----------------------------------------------------------- comparisons
-// by the sign of the renormalised difference
-__device__ __forceinline__ bool operator<(DF a, DF b) { return (a - b).hi < 0.0f; }
+// by the sign of the difference rounded to FP32
+__device__ __forceinline__ bool operator<(DF a, DF b) { return df_value(a - b) < 0.0f; }
 __device__ __forceinline__ bool operator>(DF a, DF b) { return b < a; }
 __device__ __forceinline__ bool operator<=(DF a, DF b) { return !(b < a); }
 __device__ __forceinline__ bool operator>=(DF a, DF b) { return !(a < b); }
-__device__ __forceinline__ bool operator==(DF a, DF b) { return (a - b).hi == 0.0f; }
+__device__ __forceinline__ bool operator==(DF a, DF b) { return df_value(a - b) == 0.0f; }
 __device__ __forceinline__ bool operator!=(DF a, DF b) { return !(a == b); }
 __device__ __forceinline__ bool operator==(DF a, double c) { return a == df_const(c); }
-__device__ __forceinline__ DF fabs(DF a) { return (a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f)) ? -a : a; }
+__device__ __forceinline__ DF fabs(DF a) { return df_value(a) < 0.0f ? -a : a; }
 __device__ __forceinline__ DF fmin(DF a, DF b) { return (b < a) ? b : a; }
 __device__ __forceinline__ DF fmax(DF a, DF b) { return (a < b) ? b : a; }
 
@@ -183,9 +196,29 @@ __device__ __forceinline__ void fast_sincospi(DF x, DF* s, DF* c) {
     const DF cm1 = add_f(DF{__fmul_rn(a2.hi, -0.5f), __fmul_rn(a2.lo, -0.5f)}, crest);
     const float4 T = __ldg(&kSinCosPiTableDF[n & 255]);
     const DF S{T.x, T.y}, C{T.z, T.w};
-    *s = S + (S * cm1 + C * sa);
-    *c = C + (C * cm1 - S * sa);
+    *s = add_norm(S, S * cm1 + C * sa);
+    *c = add_norm(C, C * cm1 - S * sa);
 }
+
+// The photon state after a step (ray_kernel.cuh), renormalised so that its
+// error does not grow over the ray's steps; by two-sum, which is exact for
+// any hi and lo (a momentum component through zero leaves |lo| > |hi|).
+__device__ __forceinline__ DF renorm(DF a) { return two_sum(a.hi, a.lo); }
+
+// trunc toward zero of hi + lo (the reference's (int) cast in Xtoij)
+__device__ __forceinline__ int df_trunc(DF x) {
+    const DF t = two_sum(x.hi, x.lo);
+    int i = (int)t.hi;
+    if ((float)i == t.hi) {
+        if (t.hi > 0.0f && t.lo < 0.0f) i -= 1;
+        else if (t.hi < 0.0f && t.lo > 0.0f) i += 1;
+    }
+    return i;
+}
+
+// A stage derivative times its RK weight, a power of two: two exact
+// multiplies.
+__device__ __forceinline__ DF stage_scale(DF f, float w) { return DF{__fmul_rn(f.hi, w), __fmul_rn(f.lo, w)}; }
 
 // RK stage weights (1/2, 1, 2) in FP32 for DF states: exact, and a DF times
 // an FP32 power of two is two multiplies.

@@ -31,6 +31,14 @@ __host__ __device__ inline DF scalar_cast<DF>(double x) {
     return df_const(x);
 }
 
+// The photon state after an RK step (ray_kernel.cuh): the value itself for
+// FP64; the DF overload (df64.cuh) renormalises it, the dual-number one
+// (dual.cuh) its value.
+template <class R>
+__device__ __forceinline__ R renorm(const R& x) {
+    return x;
+}
+
 // Geo (kerr_mks.cuh) with DF fields
 struct GeoDF {
     DF a, a2, hslope, R0;

@@ -58,6 +58,14 @@ struct Dual {
     }
 };
 
+// the state after an RK step: the value renormalised as its type does it
+template <int N, class T, class TD>
+__device__ __forceinline__ Dual<N, T, TD> renorm(const Dual<N, T, TD>& x) {
+    Dual<N, T, TD> r = x;
+    r.v = renorm(x.v);
+    return r;
+}
+
 // enabled for scalar types other than double (whose mixed operators are the
 // double ones below)
 template <class T>

@@ -190,8 +190,15 @@ __device__ __forceinline__ void rk4_step(const G& g, R y[8], MksPointT<R>& p, R 
     const R dt6 = dt * (1.0 / 6.0);
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-        if (rk_updates<TPhi>(i)) y[i] = y[i] + dt6 * acc[i];
+        if (rk_updates<TPhi>(i)) y[i] = renorm(y[i] + dt6 * acc[i]);
     mks_point(y[1], y[2], g, p);
+}
+
+// f times a stage weight (1 or 2); exact scaling for the double-float state
+// (df64.cuh).
+template <class R, class W>
+__device__ __forceinline__ R stage_scale(const R& f, W w) {
+    return f * w;
 }
 
 // The same RK4 step with all four stages and the end point's evaluation in
@@ -213,20 +220,21 @@ __device__ __forceinline__ void rk4_step_rolled(const G& g, R y[8], MksPointT<R>
         if (q > 0) mks_point(ys[1], ys[2], g, qp);
         if (q == 4) break;
         rhs(qp, g, ys, f);
-        const W wacc = (q == 1 || q == 2) ? W(2.0) : W(1.0);  // f2, f3 count twice
-        const R dnext = (q < 2) ? hdt : dt;                   // stage offsets dt/2, dt/2, dt
+        if (q < 3) {
+            const W wacc = (q == 0) ? W(1.0) : W(2.0);  // f2, f3 count twice
+            const R dnext = (q < 2) ? hdt : dt;         // stage offsets dt/2, dt/2, dt
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (!rk_updates<TPhi>(i)) continue;
-            acc[i] = (q == 0) ? f[i] : acc[i] + f[i] * wacc;
-            ys[i] = y[i] + dnext * f[i];
-        }
-        if (q == 3) {
+            for (int i = 0; i < 8; ++i) {
+                if (!rk_updates<TPhi>(i)) continue;
+                acc[i] = (q == 0) ? f[i] : acc[i] + stage_scale(f[i], wacc);
+                ys[i] = y[i] + dnext * f[i];
+            }
+        } else {
             const R dt6 = dt * (1.0 / 6.0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 if (!rk_updates<TPhi>(i)) continue;
-                y[i] = y[i] + dt6 * acc[i];
+                y[i] = renorm(y[i] + dt6 * (acc[i] + f[i]));
                 ys[i] = y[i];
             }
         }
@@ -246,7 +254,7 @@ __device__ __forceinline__ void rk2_step(const G& g, R y[8], MksPointT<R>& p, R 
     rhs(q, g, ys, f);
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-        if (rk_updates<TPhi>(i)) y[i] = y[i] + dt * f[i];
+        if (rk_updates<TPhi>(i)) y[i] = renorm(y[i] + dt * f[i]);
     mks_point(y[1], y[2], g, p);
 }
 

@@ -69,16 +69,6 @@ __device__ __forceinline__ MetricT<float> metric_f32(const MksPointT<DF>& p, con
     return g;
 }
 
-// trunc toward zero of hi + lo (the reference's (int) cast in Xtoij)
-__device__ __forceinline__ int df_trunc(DF t) {
-    int i = (int)t.hi;
-    if ((float)i == t.hi) {
-        if (t.hi > 0.0f && t.lo < 0.0f) i -= 1;
-        else if (t.hi < 0.0f && t.lo > 0.0f) i += 1;
-    }
-    return i;
-}
-
 // One transfer sample: Xtoij (grmhd.c:46-71) from the DF position, the
 // metric in FP32 from the point's leading parts, the rest as the mixed
 // form's FP32 sample.
@@ -93,10 +83,10 @@ __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], 
     float d1, d2;
     if (i < 0) { i = 0; d1 = 0.0f; }
     else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = 1.0f; }
-    else d1 = add_f(t1, (float)-i).hi;
+    else d1 = df_value(add_f(t1, (float)-i));
     if (j < 0) { j = 0; d2 = 0.0f; }
     else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = 1.0f; }
-    else d2 = add_f(t2, (float)-j).hi;
+    else d2 = df_value(add_f(t2, (float)-j));
     if (!chk(i >= 0 && i <= im.n1 - 2 && j >= 0 && j <= im.n2 - 2, im.check_word, kChkCell,
              (long long)i * im.n2 + j))
         i = j = 0;

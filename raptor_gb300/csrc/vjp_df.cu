@@ -87,16 +87,6 @@ __device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<DD1>& pd, const
     return g;
 }
 
-// trunc toward zero of hi + lo (the reference's (int) cast in Xtoij)
-__device__ __forceinline__ int df_trunc_i(DF t) {
-    int i = (int)t.hi;
-    if ((float)i == t.hi) {
-        if (t.hi > 0.0f && t.lo < 0.0f) i -= 1;
-        else if (t.hi < 0.0f && t.lo > 0.0f) i += 1;
-    }
-    return i;
-}
-
 // The frequency-independent part of one FP32 sample with three tangents.
 struct SampleCommonF {
     F3 kU, nus, jpre, xpre, adl;
@@ -216,14 +206,14 @@ struct FormDF {
         const MetricT<F3> g = metric_f3(p, im.geo_df);
         const DF t1 = (y[1].v - im.startx1_df) * im.idx1_df - 0.5;
         const DF t2 = (y[2].v - im.startx2_df) * im.idx2_df - 0.5;
-        int i = df_trunc_i(t1), j = df_trunc_i(t2);
+        int i = df_trunc(t1), j = df_trunc(t2);
         F3 d1(0.0f), d2(0.0f);
         if (i < 0) i = 0;
         else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F3(1.0f); }
-        else { d1 = F3(add_f(t1, (float)-i).hi); d1.d[kSIncl] = y[1].d[0] * im.idx1_df.hi; }
+        else { d1 = F3(df_value(add_f(t1, (float)-i))); d1.d[kSIncl] = y[1].d[0] * im.idx1_df.hi; }
         if (j < 0) j = 0;
         else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F3(1.0f); }
-        else { d2 = F3(add_f(t2, (float)-j).hi); d2.d[kSIncl] = y[2].d[0] * im.idx2_df.hi; }
+        else { d2 = F3(df_value(add_f(t2, (float)-j))); d2.d[kSIncl] = y[2].d[0] * im.idx2_df.hi; }
         if (!chk(i >= 0 && i <= im.n1 - 2 && j >= 0 && j <= im.n2 - 2, im.check_word, kChkCell,
                  (long long)i * im.n2 + j))
             i = j = 0;

@@ -218,8 +218,8 @@ __host__ __device__ inline Dual<N, T, TD> chain(const Dual<N, T, TD>& a, T f, T 
 // field-free region: b^2 = 0), so the tangent is taken as 0 there rather
 // than 0.5/0 * 0 = NaN.
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> sqrt(const Dual<N, T, TD>& a) {
-    const T s = sqrt(a.v);
-    return chain(a, s, s > scalar_cast<T>(0.0) ? scalar_cast<T>(0.5) / s : scalar_cast<T>(0.0));
+    const T s = fsqrt(a.v);
+    return chain(a, s, s > scalar_cast<T>(0.0) ? scalar_cast<T>(0.5) * recip(s) : scalar_cast<T>(0.0));
 }
 // 1/sqrt(x) of an FP64 dual, its tangent -r^3/2 without a division
 template <int N> __device__ inline Dual<N, double, double> rsqrt(const Dual<N, double, double>& a) {
@@ -230,7 +230,7 @@ template <int N, class T, class TD> __device__ inline Dual<N, T, TD> exp(const D
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> log(const Dual<N, T, TD>& a) { return chain(a, log(a.v), scalar_cast<T>(1.0) / a.v); }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> cbrt(const Dual<N, T, TD>& a) {
     const T c = cbrt(a.v);
-    return chain(a, c, c != scalar_cast<T>(0.0) ? scalar_cast<T>(1.0) / (scalar_cast<T>(3.0) * c * c) : scalar_cast<T>(0.0));
+    return chain(a, c, c != scalar_cast<T>(0.0) ? recip(scalar_cast<T>(3.0) * c * c) : scalar_cast<T>(0.0));
 }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> expm1(const Dual<N, T, TD>& a) { return chain(a, expm1(a.v), exp(a.v)); }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> fabs(const Dual<N, T, TD>& a) { return a.v < scalar_cast<T>(0.0) ? -a : a; }

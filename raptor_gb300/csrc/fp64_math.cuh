@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include "fp32_math.cuh"
+
 namespace raptor {
 
 #include "math_tables.inc"
@@ -40,15 +42,15 @@ __device__ __forceinline__ double fast_rcp(double x) {
     return (ex == 0u || ex == 0x7ff00000u) ? y : y2;
 }
 
-// 1/x in the templated geodesic and dual code: fast_rcp for FP64, FP32
-// division for FP32, the type's own division for the dual and double-float
-// types.
+// 1/x in the templated geodesic and dual code: fast_rcp for FP64, the
+// full-range approximate division of fp32_math.cuh for FP32, the type's own
+// division for the dual and double-float types.
 template <class R>
 __device__ __forceinline__ R recip(const R& x) {
     return 1.0 / x;
 }
 __device__ __forceinline__ double recip(double x) { return fast_rcp(x); }
-__device__ __forceinline__ float recip(float x) { return 1.0f / x; }
+__device__ __forceinline__ float recip(float x) { return fdiv(1.0f, x); }
 
 // e^x for |x| < 512 (exp(x) outside).  x = (128 m + j) ln2/128 + r with
 // |r| <= ln2/256: e^x = 2^m 2^(j/128) e^r, e^r - 1 by a degree-5 polynomial

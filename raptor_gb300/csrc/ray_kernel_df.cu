@@ -51,7 +51,7 @@ __device__ __forceinline__ MetricT<float> metric_f32(const MksPointT<DF>& p, con
     const float hfac = p.thp.hi;
     const float rho2 = p.Sg.hi;
     const float z = 2.0f * r * irho2;
-    const float ir = (R0 == 0.0f) ? p.irp.hi : 1.0f / r;
+    const float ir = (R0 == 0.0f) ? p.irp.hi : fdiv(1.0f, r);
     MetricT<float> g;
     g.d00 = -1.0f + z;
     g.d01 = z * rfac;

@@ -16,6 +16,7 @@
 //    the absorptivity as j_hat (e^x - 1) / nu^2 so every intermediate stays
 //    inside FP32's range; e2_c is applied once per ray in FP64.
 #pragma once
+#include "fp32_math.cuh"
 #include "image_desc.cuh"
 #include "kappa.cuh"
 
@@ -132,7 +133,7 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     fl.ne = rho * Ne_unit;
     // g_ij V^i V^j, i,j = 1..3, with g_12 = g_23 = 0
     const T VdotV = (g.d11 * V1 + T(2) * g.d13 * V3) * V1 + g.d22 * V2 * V2 + g.d33 * V3 * V3;
-    const T Vfac = sqrt(T(-1) / g.u00 * (T(1) + fabs(VdotV)));
+    const T Vfac = fsqrt(fdiv(T(-1), g.u00) * (T(1) + fabs(VdotV)));
     T* U = fl.ucon;
     U[0] = -Vfac * g.u00;
     U[1] = V1 - Vfac * g.u01;
@@ -142,7 +143,7 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     lowerT(g, U, Ucov);
     const T UdotBp = Ucov[1] * Bp1 + Ucov[2] * Bp2 + Ucov[3] * Bp3;
     T* Bc = fl.bcon;
-    const T iU0 = T(1) / U[0];
+    const T iU0 = fdiv(T(1), U[0]);
     Bc[0] = UdotBp;
     Bc[1] = (Bp1 + U[1] * UdotBp) * iU0;
     Bc[2] = (Bp2 + U[2] * UdotBp) * iU0;
@@ -151,18 +152,18 @@ __device__ __forceinline__ bool fluid_from_prims(const T v[8], const MetricT<T>&
     lowerT(g, Bc, Bcov);
     const T Bsq = Bc[0] * Bcov[0] + Bc[1] * Bcov[1] + Bc[2] * Bcov[2] + Bc[3] * Bcov[3];
     fl.bsq = Bsq;
-    fl.B = sqrt(Bsq) * B_unit + tiny;
+    fl.B = fsqrt(Bsq) * B_unit + tiny;
     // R-beta electron temperature, raptor_harm_model.c:262-276
-    const T beta = uu * (T(4) / T(3) - T(1)) / (T(0.5) * (Bsq + tiny));
+    const T beta = fdiv(uu * (T(4) / T(3) - T(1)), T(0.5) * (Bsq + tiny));
     const T b2 = beta * beta;
-    const T i1b2 = T(1) / (T(1) + b2);
+    const T i1b2 = fdiv(T(1), T(1) + b2);
     const T trat = r_high * b2 * i1b2 + r_low * i1b2;
     // (trat + 1)/(trat + 2) and 1/(1 + trat) from one division
     const T tp1 = trat + T(1), tp2 = trat + T(2);
-    const T itt = T(1) / (tp1 * tp2);
+    const T itt = fdiv(T(1), tp1 * tp2);
     const T two_temp_gam = T(0.5) * ((T(1) + T(2) / T(3) * (tp1 * tp1 * itt)) + T(4) / T(3));
     const T Thetae_unit = (two_temp_gam - T(1)) * (T)(kPMass / kEMass) * (tp2 * itt);
-    const T irho = T(1) / rho;
+    const T irho = fdiv(T(1), rho);
     fl.irho = irho;
     T th = (uu * irho) * Thetae_unit;
     if (th < T(0)) th = tiny;
@@ -381,16 +382,16 @@ __device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const Me
     const float* U = fl.ucon;
     const float* Bc = fl.bcon;
     const float kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    float pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) /
-                  (fabsf(kU) * (fl.B * im.inv_b_unit_f));
-    if (fabsf(pitch) > 1.0f) pitch /= fabsf(pitch);
-    const float sth = sqrtf(1.0f - pitch * pitch);
+    float pitch = fdiv(kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3],
+                       fabsf(kU) * (fl.B * im.inv_b_unit_f));
+    if (fabsf(pitch) > 1.0f) pitch = copysignf(1.0f, pitch);  // pitch / |pitch|
+    const float sth = fsqrt(1.0f - pitch * pitch);
     const float nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
     const float nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
     const bool emits = (fabsf(sth) >= 1.e-10f) && (fl.thetae > 1e-4f);
     // j / e2_c = n_e sqrt(2) pi nu_s / (3 K2) F(X) with K2 = 2 Theta^2, nu_s = (2/9) nu_c Theta^2 sin
     const float jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
-    const float xpre = (float)(kPlanck / (kEMass * kC * kC)) / fl.thetae;  // h nu / (k T) per Hz
+    const float xpre = fdiv((float)(kPlanck / (kEMass * kC * kC)), fl.thetae);  // h nu / (k T) per Hz
     const float ktau = (float)(kE2CH * kC * kC * 0.5);
     // one copy of the frequency body (mixed-DF, 5 frequencies: 12 % faster)
 #pragma unroll 1
@@ -400,11 +401,11 @@ __device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const Me
         if (nup <= 0.0f) nup = 1.0f;
         if (!(emits && nup != 1.0f)) continue;
         const float dlf = dlf_of(f);
-        const float X = nup / nus;
+        const float X = fdiv(nup, nus);
         const float cb = cbrtf(X);
-        const float sq = sqrtf(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
+        const float sq = fsqrt(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
         const float jh = jpre * (sq * sq) * expf(-cb);
-        const float q = (jh / nup) / nup;
+        const float q = fdiv(fdiv(jh, nup), nup);
         const float dtau = q * expm1f(xpre * nup) * ktau * dlf;
         neumaier_add(tau[f], tauc[f], dtau);
         const float t = tau[f] + tauc[f];

@@ -37,20 +37,20 @@ struct SampleScalarsT {
 template <class T>
 __device__ __forceinline__ void thetae_log_derivs(T rho, T uu, T bsq, T Rh, T Rl, T (&out)[4]) {
     const T tiny = (T)1.e-20;
-    const T beta = uu * (T(4) / T(3) - T(1)) / (T(0.5) * (bsq + tiny));
+    const T beta = fdiv(uu * (T(4) / T(3) - T(1)), T(0.5) * (bsq + tiny));
     const T b2 = beta * beta;
-    const T i1b2 = T(1) / (T(1) + b2);
+    const T i1b2 = fdiv(T(1), T(1) + b2);
     const T t = Rh * b2 * i1b2 + Rl * i1b2;
-    const T gam = T(0.5) * ((T(1) + T(2) / T(3) * (t + T(1)) / (t + T(2))) + T(4) / T(3));
-    if ((uu / rho) * (gam - T(1)) < T(0)) {
+    const T gam = T(0.5) * ((T(1) + fdiv(T(2) / T(3) * (t + T(1)), t + T(2))) + T(4) / T(3));
+    if (fdiv(uu, rho) * (gam - T(1)) < T(0)) {
         out[0] = out[1] = out[2] = out[3] = T(0);
         return;
     }
     // d ln((gam - 1) / (1 + t)) / dt and dt / d ln beta
-    const T dlnTU = (T(1) / T(3)) / ((t + T(2)) * (t + T(2))) / (gam - T(1)) - T(1) / (T(1) + t);
+    const T dlnTU = fdiv(fdiv(T(1) / T(3), (t + T(2)) * (t + T(2))), gam - T(1)) - fdiv(T(1), T(1) + t);
     const T dt_dlnb = T(2) * b2 * (Rh - Rl) * i1b2 * i1b2;
-    out[0] = -T(1) / rho;
-    out[1] = (T(1) + dlnTU * dt_dlnb) / uu;
+    out[0] = -fdiv(T(1), rho);
+    out[1] = fdiv(T(1) + dlnTU * dt_dlnb, uu);
     out[2] = dlnTU * b2 * i1b2;
     out[3] = dlnTU * i1b2;
 }

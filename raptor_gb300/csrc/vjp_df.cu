@@ -119,7 +119,7 @@ __device__ bool sample_common_f(const DevImage& im, const MetricT<F3>& g, int ba
     const F3 B_unit(im.b_unit_f);
     Fluid<F3> fl;
     if (!fluid_from_prims(v, g, F3(im.ne_unit_f), B_unit, F3(im.r_high_f), F3(im.r_low_f), fl)) return false;
-    out.ss.irho = 1.0f / v[0].v;
+    out.ss.irho = fdiv(1.0f, v[0].v);
     thetae_log_derivs(v[0].v, v[1].v, fl.bsq.v, im.r_high_f, im.r_low_f, out.ss.dlnth);
     // |b| in code units for the pitch angle, which M_unit does not move:
     // formed before B takes its ln B direction

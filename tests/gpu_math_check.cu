@@ -54,6 +54,26 @@ __global__ void eval_rcp(const double* x, int n, double* out) {
     out[2 * i + 1] = 1.0 / x[i];
 }
 
+// fdiv / fsqrt (fp32_math.cuh) against IEEE FP32 division and sqrtf
+__global__ void eval_f32(const float* a, const float* b, int n, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[4 * i + 0] = raptor::fdiv(a[i], b[i]);
+    out[4 * i + 1] = a[i] / b[i];
+    out[4 * i + 2] = raptor::fsqrt(fabsf(a[i]));
+    out[4 * i + 3] = sqrtf(fabsf(a[i]));
+}
+
+static double ulpsf(float a, float b) {
+    if (a == b) return 0;
+    if (!std::isfinite(a) || !std::isfinite(b)) return 1e30;
+    int ia, ib;
+    memcpy(&ia, &a, 4);
+    memcpy(&ib, &b, 4);
+    if ((ia < 0) != (ib < 0)) return 1e30;
+    return fabs((double)ia - (double)ib);
+}
+
 static double ulps(double a, double b) {
     if (a == b) return 0;
     if (!std::isfinite(a) || !std::isfinite(b)) return 1e30;
@@ -114,8 +134,47 @@ int main() {
         if (!(o[2 * k] == o[2 * k + 1]) || std::signbit(o[2 * k]) != std::signbit(o[2 * k + 1])) rcp_u = 1e30;
     if (!(o[8] != o[8])) rcp_u = 1e30;  // NaN stays NaN
     for (int i = 5; i < n; ++i) rcp_u = fmax(rcp_u, ulps(o[2 * i], o[2 * i + 1]));
+    // FP32 quotients and square roots over magnitudes 2^-149 .. 2^127 of both
+    // signs (subnormals included), then IEEE's special cases
+    std::vector<float> fa(n), fb(n);
+    for (int i = 0; i < n; ++i) {
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        const float u = (float)((s >> 40) * (1.0 / 16777216.0));
+        fa[i] = ((s >> 3) & 1 ? -1.0f : 1.0f) * ldexpf(1.0f + u, (int)((s >> 8) % 277) - 149);
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        const float v = (float)((s >> 40) * (1.0 / 16777216.0));
+        fb[i] = ((s >> 3) & 1 ? -1.0f : 1.0f) * ldexpf(1.0f + v, (int)((s >> 8) % 277) - 149);
+    }
+    const float sa[] = {0.0f, 1.0f, 0.0f, INFINITY, 3.0f, -0.0f, NAN};
+    const float sb[] = {0.0f, 0.0f, 2.0f, 2.0f, INFINITY, 1.0f, 1.0f};
+    for (int k = 0; k < 7; ++k) { fa[k] = sa[k]; fb[k] = sb[k]; }
+    float *dfa, *dfb, *dfo;
+    cudaMalloc(&dfa, n * sizeof(float));
+    cudaMalloc(&dfb, n * sizeof(float));
+    cudaMalloc(&dfo, 4 * (size_t)n * sizeof(float));
+    cudaMemcpy(dfa, fa.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(dfb, fb.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    eval_f32<<<(n + 255) / 256, 256>>>(dfa, dfb, n, dfo);
+    std::vector<float> fo(4 * (size_t)n);
+    cudaMemcpy(fo.data(), dfo, fo.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    double div_u = 0, div_u_sub = 0, sqrt_u = 0;
+    int special_bad = 0;
+    for (int k = 0; k < 7; ++k) {
+        const float q = fo[4 * k], qi = fo[4 * k + 1], r = fo[4 * k + 2], ri = fo[4 * k + 3];
+        const bool qs = (q == qi && std::signbit(q) == std::signbit(qi)) || (q != q && qi != qi);
+        const bool rs = (r == ri && std::signbit(r) == std::signbit(ri)) || (r != r && ri != ri);
+        special_bad += !qs + !rs;
+    }
+    for (int i = 7; i < n; ++i) {
+        const float qi = fo[4 * i + 1];
+        const double u = ulpsf(fo[4 * i], qi);
+        if (fabsf(qi) >= 1.17549435e-38f && fabsf(qi) < 3.0e38f) div_u = fmax(div_u, u);
+        else if (fabsf(qi) < 1.17549435e-38f) div_u_sub = fmax(div_u_sub, u);
+        sqrt_u = fmax(sqrt_u, ulpsf(fo[4 * i + 2], fo[4 * i + 3]));
+    }
     printf("exp_ulp %g sin_ulp %g cos_ulp %g sin_abs %g cos_abs %g df_exp_rel %g df_sin_abs %g df_cos_abs %g "
-           "df_div_rel %g rcp_ulp %g err %s\n",
-           me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, rcp_u, cudaGetErrorString(cudaGetLastError()));
+           "df_div_rel %g rcp_ulp %g fdiv_ulp %g fdiv_sub_ulp %g fsqrt_ulp %g f32_special_bad %d err %s\n",
+           me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, rcp_u, div_u, div_u_sub, sqrt_u, special_bad,
+           cudaGetErrorString(cudaGetLastError()));
     return 0;
 }

@@ -5,7 +5,11 @@ double-float versions (csrc/df64.cuh) against the same FP64 functions:
 exp, sin and cos within 2e-14 (a few units of the 48-bit significand), the
 division (one correction step, ~2^-45) within 5e-14.  The FP64 reciprocal
 (csrc/fp64_math.cuh fast_rcp: the hardware approximation and two
-Newton-Raphson steps) within 1 ulp of the IEEE quotient."""
+Newton-Raphson steps) within 1 ulp of the IEEE quotient.  The FP32
+samples' division and square root (csrc/fp32_math.cuh: PTX div.full.f32 and
+sqrt.approx.f32) within 2 ulp and 1 ulp of IEEE division and sqrtf, from
+subnormal to near-overflow magnitudes, with IEEE's zeros, infinities and
+NaNs."""
 import os
 import subprocess
 
@@ -30,3 +34,6 @@ def test_fast_math_against_cuda(tmp_path):
     assert float(vals["df_sin_abs"]) <= 2e-14 and float(vals["df_cos_abs"]) <= 2e-14
     assert float(vals["df_div_rel"]) <= 5e-14
     assert float(vals["rcp_ulp"]) <= 1
+    assert float(vals["fdiv_ulp"]) <= 2 and float(vals["fdiv_sub_ulp"]) <= 2
+    assert float(vals["fsqrt_ulp"]) <= 1
+    assert vals["f32_special_bad"] == "0"

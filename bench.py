@@ -48,8 +48,8 @@ TRAFFIC_FP64_1024 = 17052160
 # ncu smsp__sass_thread_inst_executed_op_{ffma,fadd,fmul}_pred_on.sum of one
 # mixed-DF ray-kernel launch (ray_kernel_df<1>) on the 1024x1024 workload:
 # the FP32 thread-instructions the double-float geodesic and the FP32 sample
-# execute (1.082e12 FADD + 5.198e11 FFMA + 2.344e11 FMUL)
-FP32_INST_DF_1024 = 1836218217738
+# execute (8.176e11 FADD + 4.945e11 FFMA + 2.335e11 FMUL)
+FP32_INST_DF_1024 = 1545619712704
 
 
 def df_roofline(kernel_ms, peak_tinst):

@@ -6,7 +6,7 @@
 // Same loop as ray_kernel (ray_kernel.cuh, integrator.c:149-289): the
 // persistent grid, the ray queue with warp-aggregated refills, termination,
 // theta-turn limit and transfer gating.  FP64 is used only per ray: the
-// camera set-up (init_photon), the output write and the k.k drift.
+// camera set-up (init_photon) and the output write.
 #include <cuda_runtime.h>
 
 #include "df64.cuh"
@@ -166,8 +166,23 @@ __device__ __forceinline__ int advance_ray_df(const DevImage& im, RayStateDF<NF>
     return 0;
 }
 
+// |k.k| / k0^2 at the final state (null_drift of ray_kernel.cuh) in DF
+// arithmetic from the point the last RK step left: the terms carry ~1e-14 of
+// k0^2, far below the drift itself (~1e-4).  In FP64 this per-ray work ran
+// at the FP64 pipe's rate on the one or two lanes that finish together.
+__device__ __forceinline__ double null_drift_df(const MksPointT<DF>& p, const GeoDF& g, const DF y[8]) {
+    MetricDDT<DF> d;
+    MetricUUT<DF> u;
+    mks_metric(p, g, d, u);
+    const DF k0 = y[4], k1 = y[5], k2 = y[6], k3 = y[7];
+    const DF kk = d.g00 * k0 * k0 + d.g11 * k1 * k1 + d.g22 * k2 * k2 + d.g33 * k3 * k3 +
+                  2.0 * (d.g01 * k0 * k1 + d.g03 * k0 * k3 + d.g13 * k1 * k3);
+    const double k0d = df_to_double(k0);
+    return fabs(df_to_double(kk)) / (k0d * k0d);
+}
+
 // The ray has ended: write I nu^3 (core.c:121-137) and the ray's statistics,
-// with the k.k drift in FP64 at the final state.
+// with the k.k drift at the final state.
 template <int NF>
 __device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayStateDF<NF>& s, double* __restrict__ out,
                                               RayCounters& c) {
@@ -187,12 +202,7 @@ __device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayState
     if ((double)s.steps >= kMaxSteps) ++c.cap;
     if (!finite) ++c.nan;  // a non-finite photon state or intensity
     c.max_steps = max(c.max_steps, (unsigned long long)s.steps);
-    double yd[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) yd[i] = df_to_double(s.y[i]);
-    MksPoint pd;
-    mks_point(yd[1], yd[2], im.geo, pd);
-    const double kk = null_drift(pd, im.geo, yd);
+    const double kk = null_drift_df(s.p, im.geo_df, s.y);
     if (kk == kk) c.kk_max = fmax(c.kk_max, kk);
 }
 

@@ -40,18 +40,45 @@ __device__ __forceinline__ void mks_point(DF x1, DF x2, const GeoDF& g, MksPoint
     mks_point_rolled(x1, x2, g, p);
 }
 
+// A sample's inputs from the DF state: |d lambda|, the cell coordinates x1,
+// x2 in DF, k^mu and the point's leading parts, all the sample reads.
+struct SampleInDF {
+    float adl;
+    DF x1, x2;
+    float k[4];
+    float r, s, iS, thp, Sg, irp, ithp, isn;
+};
+
+__device__ __forceinline__ SampleInDF sample_in_df(const DF y[8], const MksPointT<DF>& p, float adl) {
+    SampleInDF in;
+    in.adl = adl;
+    in.x1 = y[1];
+    in.x2 = y[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) in.k[i] = y[4 + i].hi;
+    in.r = p.r.hi;
+    in.s = p.s.hi;
+    in.iS = p.iS.hi;
+    in.thp = p.thp.hi;
+    in.Sg = p.Sg.hi;
+    in.irp = p.irp.hi;
+    in.ithp = p.ithp.hi;
+    in.isn = p.isn.hi;
+    return in;
+}
+
 // The sample's metric (metric.c:94-137, 207-231 as mks_metric) in FP32 from
 // the point's leading parts: it only feeds the FP32 fluid and tetrad
 // projection.
-__device__ __forceinline__ MetricT<float> metric_f32(const MksPointT<DF>& p, const GeoDF& gd) {
+__device__ __forceinline__ MetricT<float> metric_f32(const SampleInDF& in, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
-    const float r = p.r.hi, s = p.s.hi, irho2 = p.iS.hi;
+    const float r = in.r, s = in.s, irho2 = in.iS;
     const float s2 = s * s;
     const float rfac = r - R0;
-    const float hfac = p.thp.hi;
-    const float rho2 = p.Sg.hi;
+    const float hfac = in.thp;
+    const float rho2 = in.Sg;
     const float z = 2.0f * r * irho2;
-    const float ir = (R0 == 0.0f) ? p.irp.hi : fdiv(1.0f, r);
+    const float ir = (R0 == 0.0f) ? in.irp : fdiv(1.0f, r);
     MetricT<float> g;
     g.d00 = -1.0f + z;
     g.d01 = z * rfac;
@@ -64,21 +91,19 @@ __device__ __forceinline__ MetricT<float> metric_f32(const MksPointT<DF>& p, con
     g.u01 = 2.0f * irho2;
     g.u11 = irho2 * (r * (r - 2.0f) + a2) * (ir * ir);
     g.u13 = a * irho2 * ir;
-    g.u22 = irho2 * (p.ithp.hi * p.ithp.hi);
-    g.u33 = irho2 * (p.isn.hi * p.isn.hi);
+    g.u22 = irho2 * (in.ithp * in.ithp);
+    g.u33 = irho2 * (in.isn * in.isn);
     return g;
 }
 
-// One transfer sample: Xtoij (grmhd.c:46-71) from the DF position, the
-// metric in FP32 from the point's leading parts, the rest as the mixed
-// form's FP32 sample.
-template <int NF>
-__device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], const MksPointT<DF>& p, float adl,
-                                             float (&tau)[NF], float (&tauc)[NF], float (&I)[NF],
-                                             float (&Ic)[NF]) {
-    const MetricT<float> g = metric_f32(p, im.geo_df);
-    const DF t1 = (y[1] - im.startx1_df) * im.idx1_df - 0.5;
-    const DF t2 = (y[2] - im.startx2_df) * im.idx2_df - 0.5;
+// The frequency-independent part of one transfer sample: Xtoij
+// (grmhd.c:46-71) from the DF position, the metric in FP32 from the
+// point's leading parts, the rest as the mixed form's FP32 sample.  false
+// at the sigma cut.
+__device__ __forceinline__ bool sample_common_df(const DevImage& im, const SampleInDF& in, SampleF32& sc) {
+    const MetricT<float> g = metric_f32(in, im.geo_df);
+    const DF t1 = (in.x1 - im.startx1_df) * im.idx1_df - 0.5;
+    const DF t2 = (in.x2 - im.startx2_df) * im.idx2_df - 0.5;
     int i = df_trunc(t1), j = df_trunc(t2);
     float d1, d2;
     if (i < 0) { i = 0; d1 = 0.0f; }
@@ -92,9 +117,24 @@ __device__ __forceinline__ bool rt_sample_df(const DevImage& im, const DF y[8], 
         i = j = 0;
     float v[8];
     interp_prims_at(im.cells32, im.n2, i * im.n2 + j, d1, d2, v);
-    const float k[4] = {y[4].hi, y[5].hi, y[6].hi, y[7].hi};
-    return rt_sample_fp32_core<NF>(im, g, v, k, [&](int f) { return adl * im.rg_over_nu_f[f]; }, tau, tauc, I,
-                                   Ic);
+    return sample_common_fp32(im, g, v, in.k, sc);
+}
+
+// One transfer sample in place (the in-place kernel and traces).
+template <int NF>
+__device__ __forceinline__ bool rt_sample_df(const DevImage& im, const SampleInDF& in, float (&tau)[NF],
+                                             float (&tauc)[NF], float (&I)[NF], float (&Ic)[NF]) {
+    SampleF32 sc;
+    if (!sample_common_df(im, in, sc)) return false;
+    // one copy of the frequency body (mixed-DF, 5 frequencies: 12 % faster)
+#pragma unroll 1
+    for (int f = 0; f < NF; ++f) {
+        if (f >= im.nfreq) break;
+        const float dlf = in.adl * im.rg_over_nu_f[f];
+        float dtau, q;
+        if (sample_freq_fp32(im, sc, f, dlf, dtau, q)) sample_apply_fp32(dtau, q, dlf, tau[f], tauc[f], I[f], Ic[f]);
+    }
+    return true;
 }
 
 // Per-step record of the traced ray (the layout of trace_record in
@@ -215,11 +255,12 @@ __device__ __forceinline__ void finish_ray_df(const DevImage& im, const RayState
 #endif
 
 // Each lane samples its own ray in place.  A sample pool as in the FP64
-// form (ray_kernel_pool) gave the same images but ran 9 % slower here
-// (1024x1024: 122 against 112 ms): the FP32 sample is a quarter of this
-// kernel's time, and the ring's code (and a sample split into its
-// order-free and ordered halves) adds to an instruction stream that already
-// stalls on fetch.
+// form (ray_kernel_pool: tickets of the sample's inputs in a per-warp
+// shared-memory ring, evaluated 32 at a time, applied in step order) gave
+// bit-identical images but ran slower here: 1024x1024, 83 against 68 ms (one
+// frequency) and 109 against 81 ms (five).  The FP32 sample is a fifth of
+// this kernel's time, and the ring's bookkeeping and ticket traffic cost
+// more issue slots than the sample's half-empty warps waste.
 // TRACE: the per-step trace kernel (t and phi integrated, records written)
 template <int NF, bool TRACE>
 __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
@@ -261,7 +302,8 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_RAY_DF_MIN_BLOCKS)
                 const bool done = event == -1 || event == 3;
                 if (event == 1) {
                     ++c.rt_calls;
-                    const bool sampled = rt_sample_df<NF>(*im, s.y, s.p, -dl.hi, s.tf, s.tc, s.If, s.Ic);
+                    const bool sampled =
+                        rt_sample_df<NF>(*im, sample_in_df(s.y, s.p, -dl.hi), s.tf, s.tc, s.If, s.Ic);
                     c.rt_samples += sampled ? 1 : 0;
                     event = sampled ? 2 : 1;
                 }

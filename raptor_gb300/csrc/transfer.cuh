@@ -369,48 +369,82 @@ __device__ __forceinline__ void neumaier_add(float& s, float& c, float x) {
     s = t;
 }
 
-// The FP32 sample from the metric, the interpolated primitives and the
-// photon wave vector in FP32.  dlf_of(f) gives |d lambda| R_g / nu_f.
-template <int NF, class DlfOf>
-__device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const MetricT<float>& g, const float v[8],
-                                                    const float k[4], DlfOf dlf_of, float (&tau)[NF],
-                                                    float (&tauc)[NF], float (&I)[NF], float (&Ic)[NF]) {
+// The FP32 sample in three parts: the frequency-independent terms
+// (sample_common_fp32: fluid, k.u, pitch angle, emissivity prefactors), one
+// frequency's order-free terms (sample_freq_fp32: d tau and j / nu_p^2) and
+// their ordered application to tau and I (sample_apply_fp32).  The in-place
+// samples run them in one loop (rt_sample_fp32_core); the mixed-DF form's
+// sample pool evaluates the first two for 32 rays at once and applies the
+// third in each ray's step order - the same operations either way.
+struct SampleF32 {
+    float kU, nus, jpre, xpre;
+    bool emits;
+};
+
+// false at the sigma cut (no sample)
+__device__ __forceinline__ bool sample_common_fp32(const DevImage& im, const MetricT<float>& g, const float v[8],
+                                                   const float k[4], SampleF32& sc) {
     Fluid<float> fl;
     if (!fluid_from_prims(v, g, im.ne_unit_f, im.b_unit_f, im.r_high_f, im.r_low_f, fl)) return false;
     float kd[4];
     lowerT(g, k, kd);
     const float* U = fl.ucon;
     const float* Bc = fl.bcon;
-    const float kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
+    sc.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
     float pitch = fdiv(kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3],
-                       fabsf(kU) * (fl.B * im.inv_b_unit_f));
+                       fabsf(sc.kU) * (fl.B * im.inv_b_unit_f));
     if (fabsf(pitch) > 1.0f) pitch = copysignf(1.0f, pitch);  // pitch / |pitch|
     const float sth = fsqrt(1.0f - pitch * pitch);
     const float nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
-    const float nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
-    const bool emits = (fabsf(sth) >= 1.e-10f) && (fl.thetae > 1e-4f);
+    sc.nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
+    sc.emits = (fabsf(sth) >= 1.e-10f) && (fl.thetae > 1e-4f);
     // j / e2_c = n_e sqrt(2) pi nu_s / (3 K2) F(X) with K2 = 2 Theta^2, nu_s = (2/9) nu_c Theta^2 sin
-    const float jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
-    const float xpre = fdiv((float)(kPlanck / (kEMass * kC * kC)), fl.thetae);  // h nu / (k T) per Hz
-    const float ktau = (float)(kE2CH * kC * kC * 0.5);
+    sc.jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
+    sc.xpre = fdiv((float)(kPlanck / (kEMass * kC * kC)), fl.thetae);  // h nu / (k T) per Hz
+    return true;
+}
+
+// Frequency f: d tau and q = j / nu_p^2 (in units of e2_c), false where it
+// does not emit (tau and I stay as they are).  dlf = |d lambda| R_g / nu_f.
+__device__ __forceinline__ bool sample_freq_fp32(const DevImage& im, const SampleF32& sc, int f, float dlf,
+                                                 float& dtau, float& q) {
+    float nup = -sc.kU * im.freq_f[f];
+    if (nup <= 0.0f) nup = 1.0f;
+    if (!(sc.emits && nup != 1.0f)) return false;
+    const float X = fdiv(nup, sc.nus);
+    const float cb = cbrtf(X);
+    const float sq = fsqrt(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
+    const float jh = sc.jpre * (sq * sq) * expf(-cb);
+    q = fdiv(fdiv(jh, nup), nup);
+    dtau = q * expm1f(sc.xpre * nup) * (float)(kE2CH * kC * kC * 0.5) * dlf;
+    return true;
+}
+
+// tau += d tau, then I += q e^-tau dlf unless tau is past the ln 1000 gate
+// (radiative_transfer.c:87-98), both compensated
+__device__ __forceinline__ void sample_apply_fp32(float dtau, float q, float dlf, float& tau, float& tauc, float& I,
+                                                  float& Ic) {
+    neumaier_add(tau, tauc, dtau);
+    const float t = tau + tauc;
+    const float dI = q * expf(-t) * dlf;
+    if (t < 6.9077553f && !(t < 0.0f)) neumaier_add(I, Ic, dI);
+}
+
+// The in-place FP32 sample from the metric, the interpolated primitives and
+// the photon wave vector in FP32.  dlf_of(f) gives |d lambda| R_g / nu_f.
+template <int NF, class DlfOf>
+__device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const MetricT<float>& g, const float v[8],
+                                                    const float k[4], DlfOf dlf_of, float (&tau)[NF],
+                                                    float (&tauc)[NF], float (&I)[NF], float (&Ic)[NF]) {
+    SampleF32 sc;
+    if (!sample_common_fp32(im, g, v, k, sc)) return false;
     // one copy of the frequency body (mixed-DF, 5 frequencies: 12 % faster)
 #pragma unroll 1
     for (int f = 0; f < NF; ++f) {
         if (f >= im.nfreq) break;
-        float nup = -kU * im.freq_f[f];
-        if (nup <= 0.0f) nup = 1.0f;
-        if (!(emits && nup != 1.0f)) continue;
         const float dlf = dlf_of(f);
-        const float X = fdiv(nup, nus);
-        const float cb = cbrtf(X);
-        const float sq = fsqrt(cb) * (cb + 1.8877486f);  // X^1/2 + 2^(11/12) X^1/6
-        const float jh = jpre * (sq * sq) * expf(-cb);
-        const float q = fdiv(fdiv(jh, nup), nup);
-        const float dtau = q * expm1f(xpre * nup) * ktau * dlf;
-        neumaier_add(tau[f], tauc[f], dtau);
-        const float t = tau[f] + tauc[f];
-        const float dI = q * expf(-t) * dlf;
-        if (t < 6.9077553f && !(t < 0.0f)) neumaier_add(I[f], Ic[f], dI);
+        float dtau, q;
+        if (sample_freq_fp32(im, sc, f, dlf, dtau, q)) sample_apply_fp32(dtau, q, dlf, tau[f], tauc[f], I[f], Ic[f]);
     }
     return true;
 }

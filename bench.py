@@ -231,7 +231,7 @@ def workload_config(n_gpus=1):
             "parallelism": f"replicas{n_gpus}"}
 
 
-def run_vjp_config4(reps=3):
+def run_vjp_adjoint256(reps=3):
     """Adjoint configuration: 256x256 image of the 256x256 torus, loss = L2
     distance to a target at M_unit x 1.3, R = 4, i = 62 deg.  Reports, for
     the FP64, mixed and mixed-DF forms, the forward and VJP (forward pass +
@@ -265,7 +265,7 @@ def run_vjp_config4(reps=3):
     return out
 
 
-def run_batch_config3(dev):
+def run_batch_64(dev):
     """Batched configuration: 64 images (32x128^2, 24x256^2, 6x512^2,
     2x1024^2) over two 256x256 dumps, seeded angles/frequencies/M_unit: one
     graph-replayed persistent launch with the autotuned shape, against 64
@@ -590,8 +590,8 @@ def run_engine(args, rank, world, local):
     vjp = batch = incl17 = diff = None
     if not args.no_e2e:
         incl17 = run_inclination(eng, blib, dev, gid, 17.0, forms, args.steps)
-        vjp = run_vjp_config4()
-        batch = run_batch_config3(dev)
+        vjp = run_vjp_adjoint256()
+        batch = run_batch_64(dev)
         if not args.no_differentiable:
             diff = run_differentiable(dev, n_cells=2, reps=1, incl_hs=(1e-7,))
 
@@ -678,7 +678,7 @@ def main():
         print(json.dumps(run_differentiable(dist_env()[2])), flush=True)
         return
     if args.workload == "adjoint":
-        print(json.dumps(run_vjp_config4(reps=args.steps)), flush=True)
+        print(json.dumps(run_vjp_adjoint256(reps=args.steps)), flush=True)
         return
     if args.workload == "profile":
         global W, H, GRID_N

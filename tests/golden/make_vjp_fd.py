@@ -1,14 +1,13 @@
 """Finite-difference gradients of an image loss from the reference build
 (oracle/_ref, IEEE semantics), for checking raptor_gpu_vjp.
 
-    python tests/golden/make_vjp_fd.py [--threads 8] [--config 4|5]
+    python tests/golden/make_vjp_fd.py [--threads 8] [--workload adjoint256|5freq512]
 
-Configuration 4 (the adjoint configuration): 256x256 image, 230 GHz,
-i = 60 deg, a = 0.9375 torus at 256x256, M_unit = 1e19, R_high = R_low = 3,
-RK4 eps 0.05; 32 cells.  Configuration 5, reduced in rays (the large
-differentiable batch keeps its five frequencies 86/140/230/345/690 GHz and
-its 512x512 torus, on a 128x128 image): 8 cells, written to
-tests/golden/vjp_fd_c5_512.npz.
+adjoint256 (the adjoint workload): 256x256 image, 230 GHz, i = 60 deg,
+a = 0.9375 torus at 256x256, M_unit = 1e19, R_high = R_low = 3, RK4 eps
+0.05; 32 cells.  5freq512, the large differentiable batch reduced in rays
+(its five frequencies 86/140/230/345/690 GHz and its 512x512 torus, on a
+128x128 image): 8 cells, written to tests/golden/vjp_fd_5freq_512.npz.
 Loss L = 1/2 sum (O - O_target)^2 over the nu^3-scaled image O, the target
 rendered at M_unit x 1.3, R_high = R_low = 4, i = 62 deg.  Central differences
 with relative step h = 1e-4 on M_unit, R_high, R_low, the inclination, and on
@@ -41,20 +40,20 @@ from tests.golden.make_golden import quiet  # noqa: E402
 BASE = dict(m_unit=1e19, r_high=3.0, r_low=3.0, incl=60.0)
 TARGET = dict(m_unit=1.3e19, r_high=4.0, r_low=4.0, incl=62.0)
 REL_H = 1e-4
-# configuration: grid size, image size, frequencies, cells, output file
-CONFIGS = {
-    4: dict(n=256, w=256, freqs=(230e9,), n_cells=32, out="vjp_fd_256.npz"),
-    5: dict(n=512, w=128, freqs=(86e9, 140e9, 230e9, 345e9, 690e9), n_cells=8, out="vjp_fd_c5_512.npz"),
+# workload: grid size, image size, frequencies, cells, output file
+WORKLOADS = {
+    "adjoint256": dict(n=256, w=256, freqs=(230e9,), n_cells=32, out="vjp_fd_256.npz"),
+    "5freq512": dict(n=512, w=128, freqs=(86e9, 140e9, 230e9, 345e9, 690e9), n_cells=8, out="vjp_fd_5freq_512.npz"),
 }
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--config", type=int, choices=sorted(CONFIGS), default=4)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="adjoint256")
     ap.add_argument("--parts", default="scalars,cells,incl_small")
     a = ap.parse_args()
-    cfg = CONFIGS[a.config]
+    cfg = WORKLOADS[a.workload]
     N, W, FREQS, N_CELLS = cfg["n"], cfg["w"], cfg["freqs"], cfg["n_cells"]
     H = W
     parts = set(a.parts.split(","))

@@ -288,7 +288,7 @@ def test_invalid_arguments_are_rejected(eng, torus64):
 
 @pytest.mark.parametrize("incl", [60.0, 17.0])
 def test_1024_on_512_against_reference(eng, incl):
-    """Full-size images (BASELINE configuration 2): the reference rendered the
+    """Full-size images (the 1024x1024 headline workload): the reference rendered the
     1024x1024 image of the 512x512 torus here with 8 threads; the fixture keeps
     its flux and a strided 17,190-pixel subsample."""
     from raptor_gb300 import engine, synth

@@ -92,7 +92,7 @@ def test_vjp_against_engine_finite_differences(torus64):
 
 @pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "mixed", "mixed_df"])
 def test_vjp_against_reference_finite_differences(torus256, prec):
-    """The reference rerun at perturbed parameters (configuration 4), for
+    """The reference rerun at perturbed parameters (the 256x256 adjoint workload), for
     each form's VJP: its forward render and its adjoint pass (FP64; mixed:
     FP64 geodesic with FP32 tangents and the FP32 dual sample; mixed-DF:
     double-float geodesic, FP32 tangents and sample), all at the 1e-3 bar."""

@@ -3,12 +3,12 @@
 
 * Reduced in rays (128x128 image), each form's VJP against central
   differences of the reference's own build rerun at perturbed parameters
-  (tests/golden/vjp_fd_c5_512.npz, made by tests/golden/make_vjp_fd.py
-  --config 5): the four scalars and rho and u of 8 seeded cells, at the 1e-3
+  (tests/golden/vjp_fd_5freq_512.npz, made by tests/golden/make_vjp_fd.py
+  --workload 5freq512): the four scalars and rho and u of 8 seeded cells, at the 1e-3
   bar of tests/test_gpu_vjp.py.
 * At full size (2048x2048), the mixed form's forward render and VJP: every
   ray retired, finite gradients, the Theta_e-field identity, and peak device
-  memory within the configuration's 60 GB budget (the adjoint keeps no
+  memory within the workload's 60 GB budget (the adjoint keeps no
   checkpoints).
 """
 import numpy as np
@@ -29,9 +29,9 @@ def torus512():
 
 
 @pytest.mark.parametrize("prec", [1, 0, 2], ids=["mixed", "fp64", "mixed_df"])
-def test_reduced_config5_against_reference_finite_differences(torus512, prec):
+def test_reduced_5freq_512_against_reference_finite_differences(torus512, prec):
     from raptor_gb300 import engine
-    z = load_golden("vjp_fd_c5_512.npz")
+    z = load_golden("vjp_fd_5freq_512.npz")
     w, h, n = (int(x) for x in z["image"])
     assert n == 512 and list(z["freqs"]) == FREQS
     eng = engine.Engine()
@@ -59,7 +59,7 @@ def test_reduced_config5_against_reference_finite_differences(torus512, prec):
     assert not bad, "\n".join(bad)
 
 
-def test_full_size_config5_memory_and_identity(torus512):
+def test_full_size_2048_5freq_memory_and_identity(torus512):
     from raptor_gb300 import engine
     eng = engine.Engine()
     try:

@@ -14,12 +14,23 @@ w = 1 / (1 - z) in (0, 1/2) (its first, 2F1(a, c - b; a - b + 1; w), is
 (1 - w)^-a because c - b = a - b + 1).  With x, w <= 1/2 both power series
 sum_n (p)_n (q)_n / ((r)_n n!) x^n are within 1e-18 of their limits after
 80 terms.  The coefficients are exact rationals here (Python fractions),
-then rounded."""
+then rounded.  The FP32 samples of the mixed forms take the first 40 terms
+rounded to FP32 (kKappaPfaffF, kKappaConnF): after 40 terms the series are
+within 1e-9 of their limits, below FP32's rounding."""
 import os
+import struct
 from fractions import Fraction
 
 KAPPA = Fraction(7, 2)
 N_TERMS = 80
+N_TERMS_F32 = 40
+
+
+def to_f32(v):
+    """v rounded to FP32 (through its double), as a C float literal."""
+    f = struct.unpack("f", struct.pack("f", float(v)))[0]
+    t = f"{f:.9g}"
+    return (t if ("." in t or "e" in t) else t + ".0") + "f"
 
 
 def coefficients(p, q, r, n_terms=N_TERMS):
@@ -47,6 +58,12 @@ def main():
         lines.append(f"// {what}: coefficient n of the power series, p = {p}, q = {q}, r = {r}")
         lines.append(f"__device__ const double {name}[{N_TERMS}] = {{")
         lines += [f"    {float(v)!r}," for v in coefficients(p, q, r)]
+        lines.append("};")
+        lines.append("")
+    for name, p, q, r, what in series():
+        lines.append(f"// the same, first {N_TERMS_F32} coefficients rounded to FP32")
+        lines.append(f"__device__ const float {name}F[{N_TERMS_F32}] = {{")
+        lines += [f"    {to_f32(v)}," for v in coefficients(p, q, r, N_TERMS_F32)]
         lines.append("};")
         lines.append("")
     with open(os.path.join(here, "kappa_tables.inc"), "w") as f:

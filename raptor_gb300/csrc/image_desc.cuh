@@ -41,6 +41,10 @@ struct KappaConst {
     double xa;                 // the absorptivity's blend exponent (-7/4 + 8 kappa/5)^(-43/50)
     double g1, g2;             // the connection formula's gamma-function ratios
 };
+// the same in FP32, for the FP32 samples of the mixed forms
+struct KappaConstF {
+    float ln_jlow, ln_jhigh, xj, ln_alow, ln_ahigh, xa, g1, g2;
+};
 
 struct DevImage {
     long long ray_begin;   // first global ray of this image
@@ -86,6 +90,7 @@ struct DevImage {
     // emission model: kEmissionThermal, or kEmissionKappa with its constants
     int emission;
     KappaConst kap;
+    KappaConstF kapf;
 };
 
 // Per-step record of one traced ray (the analogue of the reference's GEOD

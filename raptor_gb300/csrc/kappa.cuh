@@ -20,6 +20,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "fp32_math.cuh"
 #include "fp64_math.cuh"
 #include "image_desc.cuh"
 
@@ -97,6 +98,77 @@ __device__ __forceinline__ void kappa_coeffs(const KappaConst& k, const KappaSam
     j = s.fj * kappa_blend(k.ln_jlow + lnX * (1.0 / 3.0), k.ln_jhigh - (kKappa - 2.0) / 2.0 * lnX, k.xj);
     if (s.absorbs)
         a = s.fa * kappa_blend(s.ln_alow_s - (5.0 / 3.0) * lnX, s.ln_ahigh_s - (3.0 + kKappa) / 2.0 * lnX, k.xa);
+}
+
+// ----------------------------------------------------------------- FP32
+// The same fits for the FP32 transfer samples of the mixed and mixed-DF
+// forms, from the FP32 copies of the constants (DevImage.kapf).  The
+// emissivity is carried without its e2_c = e^2/c factor, as the FP32
+// thermal emissivity is (transfer.cuh), and the blends
+// (e^(-x u) + e^(-x v))^(-1/x) are formed around the larger exponent, so
+// that e^(-x u) cannot overflow FP32's range (it would near x u = -88).
+
+// sum_n C[n] x^n by Horner's rule (40 terms, 0 <= x <= 1/2).
+__device__ __forceinline__ float kappa_series_f(const float* __restrict__ C, float x) {
+    float s = __ldg(&C[39]);
+#pragma unroll 8
+    for (int n = 38; n >= 0; --n) s = fmaf(s, x, __ldg(&C[n]));
+    return s;
+}
+
+// kappa_hyp2f1 in FP32
+__device__ __forceinline__ float kappa_hyp2f1_f(const KappaConstF& k, float thetae) {
+    const float a = (float)(kKappa - 1.0 / 3.0), b = (float)(kKappa + 1.0);
+    const float z = -(float)kKappa * thetae;
+    if (fabsf(z) == 1.0f) return 0.0f;
+    const float omz = 1.0f - z;
+    if (fabsf(z) > 1.0f) return k.g1 * powf(-z, -a) + k.g2 * powf(omz, -b) * kappa_series_f(kKappaConnF, fdiv(1.0f, omz));
+    return powf(omz, -a) * kappa_series_f(kKappaPfaffF, fdiv(z, z - 1.0f));
+}
+
+struct KappaSampleF {
+    float fj;            // n_e nu_c sin: the emissivity's prefactor over e2_c
+    float fa;            // n_e e / (B sin)
+    float inus;          // 1 / nu_s
+    float ln_alow_s, ln_ahigh_s;
+    bool emits, absorbs;
+};
+
+__device__ __forceinline__ KappaSampleF kappa_sample_f(const KappaConstF& k, float B, float cosp, float thetae,
+                                                       float ne) {
+    KappaSampleF s;
+    const float nuc = B * (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC));
+    const float sth = fsqrt(1.0f - cosp * cosp);
+    s.fj = ne * nuc * sth;
+    const float wk = thetae * (float)kKappa;
+    s.inus = fdiv(1.0f, nuc * sth * (wk * wk));
+    s.fa = ne * (float)kECharge * fdiv(1.0f, B * sth);
+    s.emits = fabsf(cosp) != 1.0f;
+    const float h = kappa_hyp2f1_f(k, thetae);
+    s.absorbs = h != 0.0f;
+    const float lnwk = logf(wk);
+    s.ln_alow_s = k.ln_alow - (float)(16.0 / 3.0 - kKappa) * lnwk + logf(h);
+    s.ln_ahigh_s = k.ln_ahigh - 5.0f * lnwk;
+    return s;
+}
+
+// (e^(-x u) + e^(-x v))^(-1/x) = e^(-(m + ln(1 + e^-|x (u - v)|)) / x), m = max(-x u, -x v)
+__device__ __forceinline__ float kappa_blend_f(float u, float v, float x) {
+    const float m = fmaxf(-x * u, -x * v);
+    return expf(-fdiv(m + log1pf(expf(-fabsf(x * (u - v)))), x));
+}
+
+// j_nu / e2_c and a_nu at plasma-frame frequency nup
+__device__ __forceinline__ void kappa_coeffs_f(const KappaConstF& k, const KappaSampleF& s, float nup, float& j,
+                                               float& a) {
+    j = 0.0f;
+    a = 0.0f;
+    if (nup == 1.0f || !s.emits) return;
+    const float lnX = logf(nup * s.inus);
+    j = s.fj * kappa_blend_f(k.ln_jlow + lnX * (1.0f / 3.0f), k.ln_jhigh - (float)((kKappa - 2.0) / 2.0) * lnX, k.xj);
+    if (s.absorbs)
+        a = s.fa * kappa_blend_f(s.ln_alow_s - (5.0f / 3.0f) * lnX,
+                                 s.ln_ahigh_s - (float)((3.0 + kKappa) / 2.0) * lnX, k.xa);
 }
 
 }  // namespace raptor

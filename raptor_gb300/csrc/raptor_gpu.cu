@@ -200,6 +200,8 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
         const double ka = k - 1. / 3., kb = k + 1., kcc = k + 2. / 3.;
         kc.g1 = std::tgamma(kcc) * std::tgamma(kb - ka) / (std::tgamma(kb) * std::tgamma(kcc - ka));
         kc.g2 = std::tgamma(kcc) * std::tgamma(ka - kb) / (std::tgamma(ka) * std::tgamma(kcc - kb));
+        im.kapf = KappaConstF{(float)kc.ln_jlow, (float)kc.ln_jhigh, (float)kc.xj,  (float)kc.ln_alow,
+                              (float)kc.ln_ahigh, (float)kc.xa,     (float)kc.g1, (float)kc.g2};
     }
     im.ne_unit_f = (float)im.Ne_unit;
     im.b_unit_f = (float)im.B_unit;
@@ -644,10 +646,6 @@ static int render_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, imgs, n_imgs, b);
     if (rc) return rc;
-    if (precision != RAPTOR_PREC_FP64)
-        for (int k = 0; k < n_imgs; ++k)
-            if (imgs[k].emission == RAPTOR_EMISSION_KAPPA)
-                return ctx_fail(ctx, RAPTOR_ERR_INVALID, "image %d: the kappa emission model renders in FP64 only", k);
     long long rb = ray_begin < 0 ? 0 : ray_begin;
     long long re = ray_count < 0 ? b.total_rays : std::min(b.total_rays, rb + ray_count);
     if (rb > b.total_rays) return ctx_fail(ctx, RAPTOR_ERR_INVALID, "ray range starts past the batch");
@@ -714,8 +712,6 @@ extern "C" int raptor_gpu_trace_ray(raptor_gpu_ctx* ctx, const raptor_image_desc
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, img, 1, b);
     if (rc) return rc;
-    if (precision != RAPTOR_PREC_FP64 && img->emission == RAPTOR_EMISSION_KAPPA)
-        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "the kappa emission model traces in FP64 only");
     const size_t bytes = sizeof(double) * (size_t)max_records * kTraceWidth;
     rc = ensure_buffer(ctx, (void**)&ctx->d_trace, &ctx->trace_cap, bytes);
     if (rc) return rc;

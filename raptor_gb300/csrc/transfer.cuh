@@ -379,6 +379,8 @@ __device__ __forceinline__ void neumaier_add(float& s, float& c, float x) {
 struct SampleF32 {
     float kU, nus, jpre, xpre;
     bool emits;
+    bool kappa;       // the kappa fits (kappa.cuh) in place of the thermal ones
+    KappaSampleF ks;  // their per-sample part
 };
 
 // false at the sigma cut (no sample)
@@ -394,6 +396,11 @@ __device__ __forceinline__ bool sample_common_fp32(const DevImage& im, const Met
     float pitch = fdiv(kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3],
                        fabsf(sc.kU) * (fl.B * im.inv_b_unit_f));
     if (fabsf(pitch) > 1.0f) pitch = copysignf(1.0f, pitch);  // pitch / |pitch|
+    sc.kappa = im.emission == kEmissionKappa;
+    if (sc.kappa) {
+        sc.ks = kappa_sample_f(im.kapf, fl.B, pitch, fl.thetae, fl.ne);
+        return true;
+    }
     const float sth = fsqrt(1.0f - pitch * pitch);
     const float nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
     sc.nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
@@ -410,6 +417,15 @@ __device__ __forceinline__ bool sample_freq_fp32(const DevImage& im, const Sampl
                                                  float& dtau, float& q) {
     float nup = -sc.kU * im.freq_f[f];
     if (nup <= 0.0f) nup = 1.0f;
+    if (sc.kappa) {
+        // dtau = nu_p a_nu dl_f and j_nu / nu_p^2, radiative_transfer.c:87-90
+        float j, a;
+        kappa_coeffs_f(im.kapf, sc.ks, nup, j, a);
+        if (j == 0.0f && a == 0.0f) return false;  // as the FP64 sample: tau and I unchanged
+        q = fdiv(fdiv(j, nup), nup);
+        dtau = nup * a * dlf;
+        return true;
+    }
     if (!(sc.emits && nup != 1.0f)) return false;
     const float X = fdiv(nup, sc.nus);
     const float cb = cbrtf(X);

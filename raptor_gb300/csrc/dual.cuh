@@ -28,6 +28,7 @@ using ::fma;
 using ::fmax;
 using ::fmin;
 using ::log;
+using ::pow;
 using ::rsqrt;
 using ::sincos;
 using ::sincospi;
@@ -225,6 +226,11 @@ template <int N, class T, class TD> __device__ inline Dual<N, T, TD> sqrt(const 
 template <int N> __device__ inline Dual<N, double, double> rsqrt(const Dual<N, double, double>& a) {
     const double r = rsqrt(a.v);
     return chain(a, r, -0.5 * r * r * r);
+}
+// a^b for a constant exponent b
+template <int N, class T, class TD> __device__ inline Dual<N, T, TD> pow(const Dual<N, T, TD>& a, double b) {
+    const T p = pow(a.v, scalar_cast<T>(b));
+    return chain(a, p, scalar_cast<T>(b) * p * recip(a.v));
 }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> exp(const Dual<N, T, TD>& a) { const T e = exp(a.v); return chain(a, e, e); }
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> log(const Dual<N, T, TD>& a) { return chain(a, log(a.v), scalar_cast<T>(1.0) / a.v); }

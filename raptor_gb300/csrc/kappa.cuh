@@ -28,9 +28,14 @@ namespace raptor {
 
 #include "kappa_tables.inc"
 
+// The FP64 functions are templates: T = double in the FP64 sample
+// (transfer.cuh, rt_terms_fp64), T = an FP64 dual number in the FP64
+// adjoint's sample (vjp.cu), whose values then follow the same operations.
+
 // sum_n C[n] x^n by Horner's rule (80 terms, 0 <= x <= 1/2).
-__device__ __forceinline__ double kappa_series(const double* __restrict__ C, double x) {
-    double s = __ldg(&C[79]);
+template <class T>
+__device__ __forceinline__ T kappa_series(const double* __restrict__ C, const T& x) {
+    T s = T(__ldg(&C[79]));
 #pragma unroll 8
     for (int n = 78; n >= 0; --n) s = fma(s, x, __ldg(&C[n]));
     return s;
@@ -38,63 +43,69 @@ __device__ __forceinline__ double kappa_series(const double* __restrict__ C, dou
 
 // 2F1(kappa - 1/3, kappa + 1; kappa + 2/3; -kappa Theta_e), the reference's
 // hyp2F1 (j_nu.c:78-96); 0 where it returns 0 (|z| = 1).
-__device__ __forceinline__ double kappa_hyp2f1(const KappaConst& k, double thetae) {
+template <class T>
+__device__ __forceinline__ T kappa_hyp2f1(const KappaConst& k, const T& thetae) {
     const double a = kKappa - 1.0 / 3.0, b = kKappa + 1.0;
-    const double z = -kKappa * thetae;
-    if (fabs(z) == 1.0) return 0.0;
+    const T z = -kKappa * thetae;
+    if (fabs(z) == 1.0) return T(0.0);
     if (fabs(z) > 1.0) {
         // (1-z)^-a G1 2F1(a, c-b; a-b+1; w) + (1-z)^-b G2 2F1(b, c-a; b-a+1; w),
         // w = 1/(1-z); the first 2F1 is (1-w)^-a, so its term is G1 (-z)^-a
-        const double omz = 1.0 - z;
-        const double w = recip(omz);
+        const T omz = 1.0 - z;
+        const T w = recip(omz);
         return k.g1 * pow(-z, -a) + k.g2 * pow(omz, -b) * kappa_series(kKappaConn, w);
     }
     // Pfaff: (1-z)^-a 2F1(a, c-b; c; z/(z-1))
-    const double omz = 1.0 - z;
+    const T omz = 1.0 - z;
     return pow(omz, -a) * kappa_series(kKappaPfaff, z * recip(z - 1.0));
 }
 
 // The per-sample part of the kappa coefficients at frequency-independent
 // plasma quantities: B (G), cosine of the pitch angle, Theta_e, n_e.
-struct KappaSample {
-    double fj, fa;        // the fits' prefactors: n_e e^2 nu_c sin / c and n_e e / (B sin)
-    double inus;          // 1 / nu_s, nu_s = nu_c sin (Theta_e kappa)^2
-    double ln_alow_s;     // ln of A_low's Theta_e-dependent factor, hyp2F1 included
-    double ln_ahigh_s;    // ln of A_high's
+template <class T>
+struct KappaSampleT {
+    T fj, fa;             // the fits' prefactors: n_e e^2 nu_c sin / c and n_e e / (B sin)
+    T inus;               // 1 / nu_s, nu_s = nu_c sin (Theta_e kappa)^2
+    T ln_alow_s;          // ln of A_low's Theta_e-dependent factor, hyp2F1 included
+    T ln_ahigh_s;         // ln of A_high's
     bool emits;           // not at a clamped pitch angle (|cos| = 1)
     bool absorbs;         // and hyp2F1 defined (|z| != 1)
 };
+using KappaSample = KappaSampleT<double>;
 
-__device__ __forceinline__ KappaSample kappa_sample(const KappaConst& k, double B, double cosp, double thetae,
-                                                   double ne) {
-    KappaSample s;
-    const double nuc = B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
-    const double sth = sqrt(1.0 - cosp * cosp);
+template <class T>
+__device__ __forceinline__ KappaSampleT<T> kappa_sample(const KappaConst& k, const T& B, const T& cosp,
+                                                        const T& thetae, const T& ne) {
+    KappaSampleT<T> s;
+    const T nuc = B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
+    const T sth = sqrt(1.0 - cosp * cosp);
     s.fj = (ne * (kECharge * kECharge) * nuc * sth) * (1.0 / kC);
-    const double wk = thetae * kKappa;
+    const T wk = thetae * kKappa;
     s.inus = recip(nuc * sth * (wk * wk));
     s.fa = ne * kECharge * recip(B * sth);
     s.emits = fabs(cosp) != 1.0;
-    const double h = kappa_hyp2f1(k, thetae);
+    const T h = kappa_hyp2f1(k, thetae);
     s.absorbs = h != 0.0;
-    const double lnwk = log(wk);
+    const T lnwk = log(wk);
     s.ln_alow_s = k.ln_alow - (16.0 / 3.0 - kKappa) * lnwk + log(h);
     s.ln_ahigh_s = k.ln_ahigh - 5.0 * lnwk;
     return s;
 }
 
 // (e^(-x u) + e^(-x v))^(-1/x) for u, v the logs of the two fits.
-__device__ __forceinline__ double kappa_blend(double u, double v, double x) {
+template <class T>
+__device__ __forceinline__ T kappa_blend(const T& u, const T& v, double x) {
     return exp(-log(fast_exp(-x * u) + fast_exp(-x * v)) / x);
 }
 
 // j_nu and a_nu at plasma-frame frequency nup (j_nu.c:28-106).
-__device__ __forceinline__ void kappa_coeffs(const KappaConst& k, const KappaSample& s, double nup, double& j,
-                                             double& a) {
-    j = 0.0;
-    a = 0.0;
+template <class T>
+__device__ __forceinline__ void kappa_coeffs(const KappaConst& k, const KappaSampleT<T>& s, const T& nup, T& j,
+                                             T& a) {
+    j = T(0.0);
+    a = T(0.0);
     if (nup == 1.0 || !s.emits) return;
-    const double lnX = log(nup * s.inus);
+    const T lnX = log(nup * s.inus);
     j = s.fj * kappa_blend(k.ln_jlow + lnX * (1.0 / 3.0), k.ln_jhigh - (kKappa - 2.0) / 2.0 * lnX, k.xj);
     if (s.absorbs)
         a = s.fa * kappa_blend(s.ln_alow_s - (5.0 / 3.0) * lnX, s.ln_ahigh_s - (3.0 + kKappa) / 2.0 * lnX, k.xa);

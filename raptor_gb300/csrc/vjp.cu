@@ -87,6 +87,10 @@ struct SampleCommon {
     double ikU;   // 1 / (k.u)
     SampleScalars ss;
     bool emits;
+    // the kappa fits (kappa.cuh) in place of the thermal ones: B in pre, Theta_e
+    // in hkt, and n_e and the pitch angle's cosine, the inputs of kappa_sample
+    bool kappa;
+    D1 kne, kcos;
 };
 
 __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, const D1 k1[4], const MksPointT<D1>& p,
@@ -142,6 +146,19 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
     const D1 ikB = 1.0 / (out.kU * Bcode);
     D1 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) * fabs(ikB);
     if (fabs(pitch.v) > 1.0) pitch = D1(pitch.v > 0 ? 1.0 : -1.0);
+    const D1 ikU = ikB * Bcode;
+    out.ikU = ikU.v;
+    out.ikU2 = ikU * ikU;
+    out.adl = adl1;
+    out.kappa = im.emission == kEmissionKappa;
+    if (out.kappa) {
+        out.pre = B;
+        out.hkt = thetae;
+        out.kne = fl.ne;
+        out.kcos = pitch;
+        out.emits = true;
+        return true;
+    }
     const D1 s2 = 1.0 - pitch * pitch;
     const D1 sth = s2.v > 0.0 ? sqrt(s2) : D1(0.0);
     const D3 nuc = B * (kECharge / (2.0 * CUDART_PI * kEMass * kC));
@@ -153,11 +170,25 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
     out.hkt = (kPlanck / (kEMass * kC * kC)) / thetae;
     out.inus = 1.0 / nus;
     out.nus = nus.v;
-    const D1 ikU = ikB * Bcode;
-    out.ikU = ikU.v;
-    out.ikU2 = ikU * ikU;
-    out.adl = adl1;
     return true;
+}
+
+// A kappa image's terms at one frequency: rt_terms_fp64's kappa branch
+// (kappa_sample, kappa_coeffs; dtau = nu_p a_nu dl_f, S = j_nu / nu_p^2
+// dl_f) on the same values, with tangents.  Out of line, and the per-sample
+// part recomputed per frequency: inlined, its dual state pushed the adjoint
+// kernels' live registers into local-memory spills on the thermal path too.
+// Returns sample_freq's kind: 1 if the frequency changes tau or I, else 0.
+__device__ __noinline__ int kappa_terms(const DevImage& im, const D3& B, const D1& cosp, const D3& thetae,
+                                        const D1& ne, const D1& nup, const D1& dlf, const D1& inup2, D3& S,
+                                        D3& dtau) {
+    const KappaSampleT<D3> ks = kappa_sample(im.kap, B, lift(cosp), thetae, lift(ne));
+    D3 j, a;
+    kappa_coeffs(im.kap, ks, lift(nup), j, a);
+    if (j.v == 0.0 && a.v == 0.0) return 0;  // rt_apply_fp64 leaves tau and I as they are
+    dtau = mul31(mul31(a, nup), dlf);
+    S = mul31(mul31(j, inup2), dlf);
+    return 1;
 }
 
 // The terms S and delta of the tau / I recurrence at frequency fi, in the
@@ -168,6 +199,9 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
 __device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommon& sc, int fi, D3& S, D3& dtau) {
     D1 nup = -sc.kU * im.freq[fi];
     if (nup.v <= 0.0) nup = D1(1.0);
+    if (sc.kappa)
+        return kappa_terms(im, sc.pre, sc.kcos, sc.hkt, sc.kne, nup, sc.adl * im.rg_over_nu[fi],
+                           sc.ikU2 * im.inv_freq2[fi], S, dtau);
     if (sc.emits && nup.v != 1.0) {
         const D1 dlf = sc.adl * im.rg_over_nu[fi];
         const D3 X = mul31(sc.inus, nup);
@@ -766,8 +800,8 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, img, 1, b);
     if (rc) return rc;
-    if (img->emission != RAPTOR_EMISSION_THERMAL)
-        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: the adjoint covers the thermal emission model only");
+    if (img->emission != RAPTOR_EMISSION_THERMAL && precision != RAPTOR_PREC_FP64)
+        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: the kappa emission model's adjoint runs in the FP64 form only");
     const DevImage& him = b.host[0];
     const GridSlot& gs = ctx->grids[img->grid];
     const long long ncell = (long long)gs.geom.n1 * gs.geom.n2;

@@ -4,7 +4,8 @@ FP64 form and compared with the oracle port, whose kappa functions equal
 the reference's own (tests/test_oracle.py), at the FP64 parity bar of
 tests/parity.py; rendered by the mixed and mixed-DF forms (the FP32 fits of
 kappa.cuh) and compared with the FP64 form at the mixed forms' flux bar.
-The adjoints refuse kappa images with RAPTOR_ERR_INVALID."""
+The kappa adjoint runs in the FP64 form; the mixed forms' adjoints refuse
+kappa images with RAPTOR_ERR_INVALID."""
 import numpy as np
 import pytest
 
@@ -102,12 +103,17 @@ def test_kappa_mixed_forms_match_fp64(eng, torus64, torus256, prec, n, w, h, fre
     assert not np.allclose(thermal, img, rtol=1e-3, atol=0.0)
 
 
-def test_kappa_refused_by_the_adjoints(eng, torus64):
+def test_kappa_adjoint_fp64_only(eng, torus64):
+    """The kappa model's adjoint runs in the FP64 form (its gradients are
+    checked in tests/test_gpu_vjp.py); the mixed forms' FP32 dual samples
+    refuse kappa images."""
     from raptor_gb300 import engine
     gid = eng.upload_grid(torus64.geom, torus64.prims)
     desc = engine.image_desc(8, 8, [230e9], grid=gid, emission=engine.EMISSION_KAPPA)
     img, _ = eng.render(desc, engine.PREC_FP64)
-    for prec in (engine.PREC_FP64, engine.PREC_MIXED, engine.PREC_MIXED_DF):
+    out, g = eng.vjp(desc, img, engine.PREC_FP64)
+    np.testing.assert_array_equal(out, img)
+    for prec in (engine.PREC_MIXED, engine.PREC_MIXED_DF):
         with pytest.raises(engine.EngineError) as e:
             eng.vjp(desc, img, prec)
         assert e.value.code == -1

@@ -44,11 +44,15 @@ class Mismatches(list):
         self.check(name, got, want, max(abs(want), 1e-3 * largest), tol)
 
 
-def test_vjp_against_engine_finite_differences(torus64):
+@pytest.mark.parametrize("emission", [0, 1], ids=["thermal", "kappa"])
+def test_vjp_against_engine_finite_differences(torus64, emission):
+    """The FP64 VJP against central differences of the engine's FP64 render
+    (the thermal fits, and the kappa fits, whose FP64 renders are pinned to
+    the reference's kappa functions in tests/test_gpu_kappa.py)."""
     from raptor_gb300 import engine
     eng = engine.Engine()
     gid = eng.upload_grid(torus64.geom, torus64.prims)
-    kw = dict(grid=gid, inclination=60.0, m_unit=1e19, r_high=3.0, r_low=3.0)
+    kw = dict(grid=gid, inclination=60.0, m_unit=1e19, r_high=3.0, r_low=3.0, emission=emission)
     mk = lambda **o: engine.image_desc(32, 32, [230e9], **dict(kw, **o))  # noqa: E731
     target, _ = eng.render(mk(inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0), engine.PREC_FP64)
     img, _ = eng.render(mk(), engine.PREC_FP64)
@@ -62,7 +66,16 @@ def test_vjp_against_engine_finite_differences(torus64):
             lp = _loss(eng, engine, mk(**{key: kw[key] + h}), target)
             lm = _loss(eng, engine, mk(**{key: kw[key] - h}), target)
             d.append((lp - lm) / (2 * h))
-        bad.check(key, g[attr], (4 * d[1] - d[0]) / 3)
+        fd = (4 * d[1] - d[0]) / 3
+        if key == "inclination" and emission == engine.EMISSION_KAPPA:
+            # the loss is only piecewise smooth in the inclination (module
+            # docstring); on the kappa image the Richardson value at h = 1e-4
+            # sits 1.6e-3 from the VJP, the plain differences at 1e-6 and 1e-7
+            # within 1e-7 of it
+            h = 1e-7 * kw[key]
+            fd = (_loss(eng, engine, mk(**{key: kw[key] + h}), target) -
+                  _loss(eng, engine, mk(**{key: kw[key] - h}), target)) / (2 * h)
+        bad.check(key, g[attr], fd)
     # per-cell fields: cells in the torus body
     rng = np.random.default_rng(5)
     cand = np.argwhere(torus64.prims[0] > 0.3)

@@ -63,8 +63,8 @@ extern "C" {
 /* emission models: the fits that emission_coeff (j_nu.c:20-26) returns */
 #define RAPTOR_EMISSION_THERMAL 0 /* thermal synchrotron, j_nu.c:130-153, 188-200 (the reference's) */
 #define RAPTOR_EMISSION_KAPPA 1   /* kappa distribution, kappa = 3.5, j_nu.c:28-106 (defined in the
-                                     reference but not called by it); renders and traces in every
-                                     form, adjoint in the FP64 form */
+                                     reference but not called by it); renders, traces and
+                                     adjoints in every form */
 
 /* camera maps (parameters.h:54-55) */
 #define RAPTOR_CAM_LINEAR 0 /* LINEAR_IMPACT_CAM: uniform grid of impact parameters (integrator.c:186-190) */

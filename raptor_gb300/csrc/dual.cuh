@@ -28,6 +28,7 @@ using ::fma;
 using ::fmax;
 using ::fmin;
 using ::log;
+using ::log1p;
 using ::pow;
 using ::rsqrt;
 using ::sincos;
@@ -226,6 +227,9 @@ template <int N, class T, class TD> __device__ inline Dual<N, T, TD> sqrt(const 
 template <int N> __device__ inline Dual<N, double, double> rsqrt(const Dual<N, double, double>& a) {
     const double r = rsqrt(a.v);
     return chain(a, r, -0.5 * r * r * r);
+}
+template <int N, class T, class TD> __device__ inline Dual<N, T, TD> log1p(const Dual<N, T, TD>& a) {
+    return chain(a, log1p(a.v), recip(scalar_cast<T>(1.0) + a.v));
 }
 // a^b for a constant exponent b
 template <int N, class T, class TD> __device__ inline Dual<N, T, TD> pow(const Dual<N, T, TD>& a, double b) {

@@ -119,63 +119,75 @@ __device__ __forceinline__ void kappa_coeffs(const KappaConst& k, const KappaSam
 // (e^(-x u) + e^(-x v))^(-1/x) are formed around the larger exponent, so
 // that e^(-x u) cannot overflow FP32's range (it would near x u = -88).
 
+// Templates as the FP64 functions are: T = float in the FP32 samples
+// (transfer.cuh), T = an FP32 dual number in the mixed forms' adjoints
+// (vjp_df.cu).
+
 // sum_n C[n] x^n by Horner's rule (40 terms, 0 <= x <= 1/2).
-__device__ __forceinline__ float kappa_series_f(const float* __restrict__ C, float x) {
-    float s = __ldg(&C[39]);
+template <class T>
+__device__ __forceinline__ T kappa_series_f(const float* __restrict__ C, const T& x) {
+    T s = T(__ldg(&C[39]));
 #pragma unroll 8
-    for (int n = 38; n >= 0; --n) s = fmaf(s, x, __ldg(&C[n]));
+    for (int n = 38; n >= 0; --n) s = fma(s, x, __ldg(&C[n]));
     return s;
 }
 
 // kappa_hyp2f1 in FP32
-__device__ __forceinline__ float kappa_hyp2f1_f(const KappaConstF& k, float thetae) {
+template <class T>
+__device__ __forceinline__ T kappa_hyp2f1_f(const KappaConstF& k, const T& thetae) {
     const float a = (float)(kKappa - 1.0 / 3.0), b = (float)(kKappa + 1.0);
-    const float z = -(float)kKappa * thetae;
-    if (fabsf(z) == 1.0f) return 0.0f;
-    const float omz = 1.0f - z;
-    if (fabsf(z) > 1.0f) return k.g1 * powf(-z, -a) + k.g2 * powf(omz, -b) * kappa_series_f(kKappaConnF, fdiv(1.0f, omz));
-    return powf(omz, -a) * kappa_series_f(kKappaPfaffF, fdiv(z, z - 1.0f));
+    const T z = -(float)kKappa * thetae;
+    if (fabs(z) == 1.0f) return T(0.0f);
+    const T omz = 1.0f - z;
+    if (fabs(z) > 1.0f)
+        return k.g1 * pow(-z, -a) + k.g2 * pow(omz, -b) * kappa_series_f(kKappaConnF, fdiv(T(1.0f), omz));
+    return pow(omz, -a) * kappa_series_f(kKappaPfaffF, fdiv(z, z - 1.0f));
 }
 
-struct KappaSampleF {
-    float fj;            // n_e nu_c sin: the emissivity's prefactor over e2_c
-    float fa;            // n_e e / (B sin)
-    float inus;          // 1 / nu_s
-    float ln_alow_s, ln_ahigh_s;
+template <class T>
+struct KappaSampleFT {
+    T fj;            // n_e nu_c sin: the emissivity's prefactor over e2_c
+    T fa;            // n_e e / (B sin)
+    T inus;          // 1 / nu_s
+    T ln_alow_s, ln_ahigh_s;
     bool emits, absorbs;
 };
+using KappaSampleF = KappaSampleFT<float>;
 
-__device__ __forceinline__ KappaSampleF kappa_sample_f(const KappaConstF& k, float B, float cosp, float thetae,
-                                                       float ne) {
-    KappaSampleF s;
-    const float nuc = B * (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC));
-    const float sth = fsqrt(1.0f - cosp * cosp);
+template <class T>
+__device__ __forceinline__ KappaSampleFT<T> kappa_sample_f(const KappaConstF& k, const T& B, const T& cosp,
+                                                           const T& thetae, const T& ne) {
+    KappaSampleFT<T> s;
+    const T nuc = B * (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC));
+    const T sth = fsqrt(1.0f - cosp * cosp);
     s.fj = ne * nuc * sth;
-    const float wk = thetae * (float)kKappa;
-    s.inus = fdiv(1.0f, nuc * sth * (wk * wk));
-    s.fa = ne * (float)kECharge * fdiv(1.0f, B * sth);
-    s.emits = fabsf(cosp) != 1.0f;
-    const float h = kappa_hyp2f1_f(k, thetae);
+    const T wk = thetae * (float)kKappa;
+    s.inus = fdiv(T(1.0f), nuc * sth * (wk * wk));
+    s.fa = ne * (float)kECharge * fdiv(T(1.0f), B * sth);
+    s.emits = fabs(cosp) != 1.0f;
+    const T h = kappa_hyp2f1_f(k, thetae);
     s.absorbs = h != 0.0f;
-    const float lnwk = logf(wk);
-    s.ln_alow_s = k.ln_alow - (float)(16.0 / 3.0 - kKappa) * lnwk + logf(h);
+    const T lnwk = log(wk);
+    s.ln_alow_s = k.ln_alow - (float)(16.0 / 3.0 - kKappa) * lnwk + log(h);
     s.ln_ahigh_s = k.ln_ahigh - 5.0f * lnwk;
     return s;
 }
 
 // (e^(-x u) + e^(-x v))^(-1/x) = e^(-(m + ln(1 + e^-|x (u - v)|)) / x), m = max(-x u, -x v)
-__device__ __forceinline__ float kappa_blend_f(float u, float v, float x) {
-    const float m = fmaxf(-x * u, -x * v);
-    return expf(-fdiv(m + log1pf(expf(-fabsf(x * (u - v)))), x));
+template <class T>
+__device__ __forceinline__ T kappa_blend_f(const T& u, const T& v, float x) {
+    const T m = fmax(-x * u, -x * v);
+    return exp(-fdiv(m + log1p(exp(-fabs(x * (u - v)))), T(x)));
 }
 
 // j_nu / e2_c and a_nu at plasma-frame frequency nup
-__device__ __forceinline__ void kappa_coeffs_f(const KappaConstF& k, const KappaSampleF& s, float nup, float& j,
-                                               float& a) {
-    j = 0.0f;
-    a = 0.0f;
+template <class T>
+__device__ __forceinline__ void kappa_coeffs_f(const KappaConstF& k, const KappaSampleFT<T>& s, const T& nup, T& j,
+                                               T& a) {
+    j = T(0.0f);
+    a = T(0.0f);
     if (nup == 1.0f || !s.emits) return;
-    const float lnX = logf(nup * s.inus);
+    const T lnX = log(nup * s.inus);
     j = s.fj * kappa_blend_f(k.ln_jlow + lnX * (1.0f / 3.0f), k.ln_jhigh - (float)((kKappa - 2.0) / 2.0) * lnX, k.xj);
     if (s.absorbs)
         a = s.fa * kappa_blend_f(s.ln_alow_s - (5.0f / 3.0f) * lnX,

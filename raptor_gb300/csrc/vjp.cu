@@ -87,12 +87,14 @@ struct SampleCommon {
     double ikU;   // 1 / (k.u)
     SampleScalars ss;
     bool emits;
-    // the kappa fits (kappa.cuh) in place of the thermal ones: B in pre, Theta_e
-    // in hkt, and n_e and the pitch angle's cosine, the inputs of kappa_sample
-    bool kappa;
+    // kappa images (K): B in pre, Theta_e in hkt, and n_e and the pitch
+    // angle's cosine, the inputs of kappa_sample
     D1 kne, kcos;
 };
 
+// K: the image takes the kappa fits (the adjoint kernels are instantiated
+// apart for them, so that the thermal kernels carry none of their code).
+template <bool K>
 __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, const D1 k1[4], const MksPointT<D1>& p,
                               const D1& adl1, CellCoef& cc, SampleCommon& out) {
     MetricDDT<D1> gd1;
@@ -150,8 +152,7 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
     out.ikU = ikU.v;
     out.ikU2 = ikU * ikU;
     out.adl = adl1;
-    out.kappa = im.emission == kEmissionKappa;
-    if (out.kappa) {
+    if constexpr (K) {
         out.pre = B;
         out.hkt = thetae;
         out.kne = fl.ne;
@@ -175,9 +176,8 @@ __device__ bool sample_common(const DevImage& im, const D1& x1, const D1& x2, co
 
 // A kappa image's terms at one frequency: rt_terms_fp64's kappa branch
 // (kappa_sample, kappa_coeffs; dtau = nu_p a_nu dl_f, S = j_nu / nu_p^2
-// dl_f) on the same values, with tangents.  Out of line, and the per-sample
-// part recomputed per frequency: inlined, its dual state pushed the adjoint
-// kernels' live registers into local-memory spills on the thermal path too.
+// dl_f) on the same values, with tangents; out of line, the per-sample part
+// recomputed per frequency.
 // Returns sample_freq's kind: 1 if the frequency changes tau or I, else 0.
 __device__ __noinline__ int kappa_terms(const DevImage& im, const D3& B, const D1& cosp, const D3& thetae,
                                         const D1& ne, const D1& nup, const D1& dlf, const D1& inup2, D3& S,
@@ -196,10 +196,11 @@ __device__ __noinline__ int kappa_terms(const DevImage& im, const D3& B, const D
 // formed, a nu = j (e2_ch c^2 / (2 e2_c)) (e^{h nu / k T} - 1) / nu^2.
 // Returns 1 if the frequency emits, 2 where the primal's tau turns NaN (B_nu
 // underflowed to 0), else 0.
+template <bool K>
 __device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommon& sc, int fi, D3& S, D3& dtau) {
     D1 nup = -sc.kU * im.freq[fi];
     if (nup.v <= 0.0) nup = D1(1.0);
-    if (sc.kappa)
+    if constexpr (K)
         return kappa_terms(im, sc.pre, sc.kcos, sc.hkt, sc.kne, nup, sc.adl * im.rg_over_nu[fi],
                            sc.ikU2 * im.inv_freq2[fi], S, dtau);
     if (sc.emits && nup.v != 1.0) {
@@ -336,7 +337,7 @@ CamT<D1> camera_tangent(const DevImage& im, double inclination, double a, double
 // duals' register footprint, keeping a ray's state across lane refills (as
 // the mixed-DF adjoint does) spilled more and ran slower (5-frequency
 // 2048x2048: 14.5 s against 11.7 s).
-template <int NF>
+template <int NF, bool K>
 __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 SampleCommon sc;
                 CellCoef cc;
                 const D1 k1[4] = {y[4], y[5], y[6], y[7]};
-                if (sample_common(im, y[1], y[2], k1, p, fabs(dl), cc, sc)) {
+                if (sample_common<K>(im, y[1], y[2], k1, p, fabs(dl), cc, sc)) {
                     ++n_samples;
                     double Gr = 0.0, Gt = 0.0;
                     // one copy of the frequency body: with NF > 1 the per-frequency
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                     for (int f = 0; f < NF; ++f) {
                         if (f >= im.nfreq) break;
                         D3 S, dt;
-                        const int kind = sample_freq(im, sc, f, S, dt);
+                        const int kind = sample_freq<K>(im, sc, f, S, dt);
                         consume_term(kind, S, dt, sc.ss, w[f], Itot[f], tau[f], Ipart[f], dtg[f], dIw, Gr, Gt,
                                      n_emit, n_gate);
                     }
@@ -480,7 +481,7 @@ struct Layout {
 };
 }  // namespace vpool
 
-template <int NF>
+template <int NF, bool K>
 __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel_pool(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                     const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
@@ -630,14 +631,14 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                 SampleCommon sc;
                 CellCoef cc;
                 double* const o = res + te;
-                if (sample_common(im, x1, x2, k1, mp, a, cc, sc)) {
+                if (sample_common<K>(im, x1, x2, k1, mp, a, cc, sc)) {
                     ++n_samples;
 #pragma unroll 1
                     for (int f = 0; f < NF; ++f) {
                         int kd = 0;
                         if (f < im.nfreq) {
                             D3 S, dt;
-                            kd = sample_freq(im, sc, f, S, dt);
+                            kd = sample_freq<K>(im, sc, f, S, dt);
                             if (kd == 1) {
                                 double* of = o + (7 + 8 * f) * C;
                                 of[0] = S.v;
@@ -736,33 +737,43 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     }
 }
 
-template <int NF>
+template <int NF, bool K>
 void launch_vjp_pool(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                      const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
                      int refill, double* scratch, RayRange rr) {
-    vjp_kernel_pool<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch, rr);
+    vjp_kernel_pool<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch, rr);
 }
 
-template <int NF>
+template <int NF, bool K>
 void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                 const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
                 int, double*, RayRange rr) {
-    vjp_kernel<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, rr);
+    vjp_kernel<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, rr);
 }
 
 // pool: the sample-pool kernel; *scratch_rows gets the scratch rows (of
-// kPoolCap doubles) it needs per warp
-VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows) {
+// kPoolCap doubles) it needs per warp.  kappa: the kappa fits'
+// instantiation (any frequency count).
+VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows, bool kappa) {
     *scratch_rows = 0;
+    if (kappa) {
+        if (pool) {
+            *fn = (const void*)vjp_kernel_pool<8, true>;
+            *scratch_rows = vpool::Layout<8>::kScratchRows;
+            return launch_vjp_pool<8, true>;
+        }
+        *fn = (const void*)vjp_kernel<8, true>;
+        return launch_vjp<8, true>;
+    }
 #define PICK(NF)                                                                         \
     if (nf <= NF) {                                                                      \
         if (pool) {                                                                      \
-            *fn = (const void*)vjp_kernel_pool<NF>;                                      \
+            *fn = (const void*)vjp_kernel_pool<NF, false>;                               \
             *scratch_rows = vpool::Layout<NF>::kScratchRows;                             \
-            return launch_vjp_pool<NF>;                                                  \
+            return launch_vjp_pool<NF, false>;                                           \
         }                                                                                \
-        *fn = (const void*)vjp_kernel<NF>;                                               \
-        return launch_vjp<NF>;                                                           \
+        *fn = (const void*)vjp_kernel<NF, false>;                                        \
+        return launch_vjp<NF, false>;                                                    \
     }
     PICK(1)
     PICK(2)
@@ -770,12 +781,12 @@ VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows)
     PICK(5)
 #undef PICK
     if (pool) {
-        *fn = (const void*)vjp_kernel_pool<8>;
+        *fn = (const void*)vjp_kernel_pool<8, false>;
         *scratch_rows = vpool::Layout<8>::kScratchRows;
-        return launch_vjp_pool<8>;
+        return launch_vjp_pool<8, false>;
     }
-    *fn = (const void*)vjp_kernel<8>;
-    return launch_vjp<8>;
+    *fn = (const void*)vjp_kernel<8, false>;
+    return launch_vjp<8, false>;
 }
 
 }  // namespace
@@ -800,8 +811,6 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
     Batch& b = ctx->batch;
     int rc = prepare_batch(ctx, img, 1, b);
     if (rc) return rc;
-    if (img->emission != RAPTOR_EMISSION_THERMAL && precision != RAPTOR_PREC_FP64)
-        return ctx_fail(ctx, RAPTOR_ERR_INVALID, "vjp: the kappa emission model's adjoint runs in the FP64 form only");
     const DevImage& him = b.host[0];
     const GridSlot& gs = ctx->grids[img->grid];
     const long long ncell = (long long)gs.geom.n1 * gs.geom.n2;
@@ -837,10 +846,11 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
     int occ = 1;
     const void* kp = nullptr;
     int scratch_rows = 0;
-    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp)
+    const bool kappa = img->emission == RAPTOR_EMISSION_KAPPA;
+    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp, kappa)
                             : precision == RAPTOR_PREC_MIXED
-                                ? pick_vjp_mixed(b.max_nf, &kp)
-                                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows);
+                                ? pick_vjp_mixed(b.max_nf, &kp, kappa)
+                                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows, kappa);
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
     const int grid = ctx->num_sms * std::max(occ, 1);
     // the pooled adjoint's per-warp result slices (several frequencies)

@@ -122,7 +122,7 @@ using VjpLaunchFn = void (*)(int grid, cudaStream_t st, const DevImage* im, cons
                              double* g_u, double* g_th, int refill, double* scratch, RayRange rr);
 // the mixed-DF and the mixed adjoints for nf frequencies (vjp_df.cu); *fn
 // gets the kernel
-VjpLaunchFn pick_vjp_df(int nf, const void** fn);
-VjpLaunchFn pick_vjp_mixed(int nf, const void** fn);
+VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa);
+VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa);
 
 }  // namespace raptor

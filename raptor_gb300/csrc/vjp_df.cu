@@ -94,12 +94,18 @@ struct SampleCommonF {
     bool emits;
     int base;        // first of the four cells
     float d1, d2;    // bilinear offsets
+    // kappa images (K): B in nus, Theta_e in xpre, n_e in jpre, and the pitch
+    // angle's cosine, the inputs of kappa_sample_f
+    F3 kcos;
 };
 
 // The FP32 sample (rt_sample_fp32_core's fluid, tetrad projection and
 // emission prefactors) from its FP32 metric, the first of its four cells and
 // the bilinear offsets, the wave vector and |d lambda|, each with its
 // inclination tangent.
+// K: the image takes the kappa fits (the adjoint kernels are instantiated
+// apart for them, so that the thermal kernels carry none of their code).
+template <bool K>
 __device__ bool sample_common_f(const DevImage& im, const MetricT<F3>& g, int base, const F3& d1, const F3& d2,
                                 const F3 (&k)[4], const F3& adl, SampleCommonF& out) {
     out.base = base;
@@ -134,21 +140,47 @@ __device__ bool sample_common_f(const DevImage& im, const MetricT<F3>& g, int ba
     out.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
     F3 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * Bcode);
     if (fabsf(pitch.v) > 1.0f) pitch = F3(pitch.v > 0.0f ? 1.0f : -1.0f);
+    out.adl = adl;
+    if constexpr (K) {
+        out.nus = fl.B;
+        out.xpre = fl.thetae;
+        out.jpre = fl.ne;
+        out.kcos = pitch;
+        out.emits = true;
+        return true;
+    }
     const F3 sth = sqrt(1.0f - pitch * pitch);
     const F3 nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
     out.nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
     out.emits = (fabsf(sth.v) >= 1.e-10f) && (fl.thetae.v > 1e-4f);
     out.jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
     out.xpre = (float)(kPlanck / (kEMass * kC * kC)) / fl.thetae;
-    out.adl = adl;
+    return true;
+}
+
+// A kappa image's terms at one frequency: the FP32 sample's kappa branch
+// (transfer.cuh, sample_freq_fp32) on the same values, with tangents; out of
+// line, the per-sample part recomputed per frequency.
+__device__ __noinline__ bool kappa_terms_f(const DevImage& im, const F3& B, const F3& cosp, const F3& thetae,
+                                           const F3& ne, const F3& nup, const F3& dlf, F3& S, F3& dtau) {
+    const KappaSampleFT<F3> ks = kappa_sample_f(im.kapf, B, cosp, thetae, ne);
+    F3 j, a;
+    kappa_coeffs_f(im.kapf, ks, nup, j, a);
+    if (j.v == 0.0f && a.v == 0.0f) return false;
+    const F3 q = fdiv(fdiv(j, nup), nup);
+    dtau = nup * a * dlf;
+    S = q * dlf;
     return true;
 }
 
 // S and delta at frequency fi (rt_sample_fp32_core's arithmetic, emissivity
 // without e2_c); false if the frequency does not emit.
+template <bool K>
 __device__ __forceinline__ bool sample_freq_f(const DevImage& im, const SampleCommonF& sc, int fi, F3& S, F3& dtau) {
     F3 nup = -sc.kU * im.freq_f[fi];
     if (nup.v <= 0.0f) nup = F3(1.0f);
+    if constexpr (K)
+        return kappa_terms_f(im, sc.nus, sc.kcos, sc.xpre, sc.jpre, nup, sc.adl * im.rg_over_nu_f[fi], S, dtau);
     if (!(sc.emits && nup.v != 1.0f)) return false;
     const F3 dlf = sc.adl * im.rg_over_nu_f[fi];
     const F3 X = nup / sc.nus;
@@ -201,6 +233,7 @@ struct FormDF {
     }
     // rt_sample_df's inputs: Xtoij (grmhd.c:46-71) from the DF position,
     // the offsets carrying the inclination tangent unless clamped
+    template <bool K>
     __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
                                   SampleCommonF& out) {
         const MetricT<F3> g = metric_f3(p, im.geo_df);
@@ -218,7 +251,7 @@ struct FormDF {
                  (long long)i * im.n2 + j))
             i = j = 0;
         const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
-        return sample_common_f(im, g, i * im.n2 + j, d1, d2, k, liftf(to_f1(adl)), out);
+        return sample_common_f<K>(im, g, i * im.n2 + j, d1, d2, k, liftf(to_f1(adl)), out);
     }
 };
 
@@ -248,6 +281,7 @@ struct FormMixed {
     }
     // rt_sample_fp32's inputs: the metric in FP64 (with its tangent) rounded
     // to FP32, Xtoij in FP64 (cell_coef), the wave vector rounded to FP32
+    template <bool K>
     __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
                                   SampleCommonF& out) {
         MetricDDT<S> gd;
@@ -267,7 +301,7 @@ struct FormMixed {
         if ((int)t1 == i) d1.d[kSIncl] = (float)y[1].d[0] * (float)im.idx1;  // not clamped
         if ((int)t2 == j) d2.d[kSIncl] = (float)y[2].d[0] * (float)im.idx2;
         const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
-        return sample_common_f(im, g, cc.base, d1, d2, k, liftf(to_f1(adl)), out);
+        return sample_common_f<K>(im, g, cc.base, d1, d2, k, liftf(to_f1(adl)), out);
     }
 };
 
@@ -291,7 +325,7 @@ __device__ __forceinline__ double pow2_double(int e) {
 
 // The adjoint pass: lanes take rays from the queue and refill every
 // refill_interval steps, as the forward kernels do.
-template <int NF, class F>
+template <int NF, class F, bool K>
 __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>& cam, const double* __restrict__ fwd,
                                              const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                                              double* __restrict__ gscal, double* __restrict__ g_rho,
@@ -383,7 +417,7 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                 } else if (F::in_grid(im, s.y)) {
                     ++n_calls;
                     SampleCommonF sc;
-                    if (F::sample(im, s.y, s.p, fabs(dl), sc)) {
+                    if (F::template sample<K>(im, s.y, s.p, fabs(dl), sc)) {
                         ++n_samples;
                         float Gr = 0.0f, Gt = 0.0f;
                         // one copy of the frequency body (the per-frequency
@@ -392,7 +426,7 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                         for (int f = 0; f < NF; ++f) {
                             if (f >= im.nfreq) break;
                             F3 S3, dt;
-                            if (!sample_freq_f(im, sc, f, S3, dt)) continue;
+                            if (!sample_freq_f<K>(im, sc, f, S3, dt)) continue;
                             ++n_emit;
                             s.tau[f] += dt.v;
 #pragma unroll
@@ -485,51 +519,54 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
 #endif
 using MixedTangent = std::conditional<RAPTOR_VJP_MIXED_TANGENT_FP32 != 0, float, double>::type;
 
-template <int NF>
+template <int NF, bool K>
 __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
     vjp_kernel_df(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                   const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                   double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
                   double* __restrict__ g_th, int refill_interval, RayRange rr) {
-    vjp_f32_body<NF, FormDF>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval, rr);
+    vjp_f32_body<NF, FormDF, K>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval, rr);
 }
 
-template <int NF>
+template <int NF, bool K>
 __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_MIXED_MIN_BLOCKS)
     vjp_kernel_mixed(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                      const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                      double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
                      double* __restrict__ g_th, int refill_interval, RayRange rr) {
-    vjp_f32_body<NF, FormMixed<MixedTangent>>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th,
+    vjp_f32_body<NF, FormMixed<MixedTangent>, K>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th,
                                               refill_interval, rr);
 }
 
-template <int NF>
+template <int NF, bool K>
 void launch_vjp_df(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                    const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
                    int refill, double*, RayRange rr) {
-    vjp_kernel_df<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
+    vjp_kernel_df<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
 }
 
-template <int NF>
+template <int NF, bool K>
 void launch_vjp_mixed(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                       const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
                       int refill, double*, RayRange rr) {
-    vjp_kernel_mixed<NF><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
+    vjp_kernel_mixed<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
 }
 
 }  // namespace
 
-VjpLaunchFn pick_vjp_df(int nf, const void** fn) {
-    if (nf <= 1) { *fn = (const void*)vjp_kernel_df<1>; return launch_vjp_df<1>; }
-    *fn = (const void*)vjp_kernel_df<kMaxFreqs>;
-    return launch_vjp_df<kMaxFreqs>;
+// kappa: the kappa fits' instantiation (any frequency count)
+VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa) {
+    if (kappa) { *fn = (const void*)vjp_kernel_df<kMaxFreqs, true>; return launch_vjp_df<kMaxFreqs, true>; }
+    if (nf <= 1) { *fn = (const void*)vjp_kernel_df<1, false>; return launch_vjp_df<1, false>; }
+    *fn = (const void*)vjp_kernel_df<kMaxFreqs, false>;
+    return launch_vjp_df<kMaxFreqs, false>;
 }
 
-VjpLaunchFn pick_vjp_mixed(int nf, const void** fn) {
-    if (nf <= 1) { *fn = (const void*)vjp_kernel_mixed<1>; return launch_vjp_mixed<1>; }
-    *fn = (const void*)vjp_kernel_mixed<kMaxFreqs>;
-    return launch_vjp_mixed<kMaxFreqs>;
+VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa) {
+    if (kappa) { *fn = (const void*)vjp_kernel_mixed<kMaxFreqs, true>; return launch_vjp_mixed<kMaxFreqs, true>; }
+    if (nf <= 1) { *fn = (const void*)vjp_kernel_mixed<1, false>; return launch_vjp_mixed<1, false>; }
+    *fn = (const void*)vjp_kernel_mixed<kMaxFreqs, false>;
+    return launch_vjp_mixed<kMaxFreqs, false>;
 }
 
 }  // namespace raptor

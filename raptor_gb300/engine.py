@@ -144,7 +144,7 @@ def image_desc(width, height, freqs: Sequence[float], grid: int = 0, inclination
                integrator=RK4, camera=0, emission=EMISSION_THERMAL) -> ImageDesc:
     """camera: CAM_LINEAR (0, the reference's default) or CAM_LOG (1);
     emission: EMISSION_THERMAL (0, the reference's) or EMISSION_KAPPA (1,
-    the kappa = 3.5 fits: renders and traces in every form, adjoint in FP64)."""
+    the kappa = 3.5 fits, in every form and the adjoints)."""
     freqs = list(np.atleast_1d(freqs).astype(float))
     if not 1 <= len(freqs) <= RAPTOR_MAX_FREQS:
         raise ValueError(f"1..{RAPTOR_MAX_FREQS} frequencies per image")

@@ -67,33 +67,10 @@ __device__ __forceinline__ SampleInDF sample_in_df(const DF y[8], const MksPoint
     return in;
 }
 
-// The sample's metric (metric.c:94-137, 207-231 as mks_metric) in FP32 from
-// the point's leading parts: it only feeds the FP32 fluid and tetrad
-// projection.
+// The sample's metric in FP32 from the point's leading parts (transfer.cuh)
 __device__ __forceinline__ MetricT<float> metric_f32(const SampleInDF& in, const GeoDF& gd) {
-    const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
-    const float r = in.r, s = in.s, irho2 = in.iS;
-    const float s2 = s * s;
-    const float rfac = r - R0;
-    const float hfac = in.thp;
-    const float rho2 = in.Sg;
-    const float z = 2.0f * r * irho2;
-    const float ir = (R0 == 0.0f) ? in.irp : fdiv(1.0f, r);
-    MetricT<float> g;
-    g.d00 = -1.0f + z;
-    g.d01 = z * rfac;
-    g.d03 = -a * z * s2;
-    g.d11 = (1.0f + z) * rfac * rfac;
-    g.d13 = -a * s2 * (1.0f + z) * rfac;
-    g.d22 = rho2 * hfac * hfac;
-    g.d33 = s2 * (rho2 + a2 * s2 * (1.0f + z));
-    g.u00 = -1.0f - z;
-    g.u01 = 2.0f * irho2;
-    g.u11 = irho2 * (r * (r - 2.0f) + a2) * (ir * ir);
-    g.u13 = a * irho2 * ir;
-    g.u22 = irho2 * (in.ithp * in.ithp);
-    g.u33 = irho2 * (in.isn * in.isn);
-    return g;
+    return metric_f32(PointF32{in.r, in.s, in.iS, in.thp, in.Sg, in.irp, in.ithp, in.isn}, gd.a.hi, gd.a2.hi,
+                      gd.R0.hi);
 }
 
 // The frequency-independent part of one transfer sample: Xtoij

@@ -465,15 +465,50 @@ __device__ __forceinline__ bool rt_sample_fp32_core(const DevImage& im, const Me
     return true;
 }
 
-// Mixed form: metric and cell coefficients from the FP64 geodesic state.
+// The FP32 samples' metric (metric.c:94-137, 207-231 as mks_metric) in FP32
+// from the point's quantities rounded to FP32 (r, sin theta, 1/Sigma,
+// theta', Sigma, 1/r', 1/theta', 1/sin theta) and the spin and R0: it feeds
+// only the FP32 fluid and tetrad projection.
+struct PointF32 {
+    float r, s, iS, thp, Sg, irp, ithp, isn;
+};
+
+__device__ __forceinline__ MetricT<float> metric_f32(const PointF32& q, float a, float a2, float R0) {
+    const float r = q.r, s = q.s, irho2 = q.iS;
+    const float s2 = s * s;
+    const float rfac = r - R0;
+    const float hfac = q.thp;
+    const float rho2 = q.Sg;
+    const float z = 2.0f * r * irho2;
+    const float ir = (R0 == 0.0f) ? q.irp : fdiv(1.0f, r);
+    MetricT<float> g;
+    g.d00 = -1.0f + z;
+    g.d01 = z * rfac;
+    g.d03 = -a * z * s2;
+    g.d11 = (1.0f + z) * rfac * rfac;
+    g.d13 = -a * s2 * (1.0f + z) * rfac;
+    g.d22 = rho2 * hfac * hfac;
+    g.d33 = s2 * (rho2 + a2 * s2 * (1.0f + z));
+    g.u00 = -1.0f - z;
+    g.u01 = 2.0f * irho2;
+    g.u11 = irho2 * (r * (r - 2.0f) + a2) * (ir * ir);
+    g.u13 = a * irho2 * ir;
+    g.u22 = irho2 * (q.ithp * q.ithp);
+    g.u33 = irho2 * (q.isn * q.isn);
+    return g;
+}
+
+// Mixed form: the cell coefficients from the FP64 geodesic state, the
+// metric in FP32 from the FP64 point rounded (computing it in FP64 and
+// rounding it took some 30 FP64-pipe instructions per sample, run with the
+// warp's non-sampling lanes idle).
 template <int NF>
 __device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double y[8], const MksPoint& p,
                                                double adl, float (&tau)[NF], float (&tauc)[NF],
                                                float (&I)[NF], float (&Ic)[NF]) {
-    MetricDD gd;
-    MetricUU gu;
-    mks_metric(p, im.geo, gd, gu);
-    const MetricT<float> g = metric_cast<float>(gd, gu);
+    const PointF32 q{(float)p.r, (float)p.s, (float)p.iS, (float)p.thp,
+                     (float)p.Sg, (float)p.irp, (float)p.ithp, (float)p.isn};
+    const MetricT<float> g = metric_f32(q, im.geo_df.a.hi, im.geo_df.a2.hi, im.geo_df.R0.hi);
     const CellCoef cc = cell_coef(im, y[1], y[2]);
     float v[8];
     interp_prims(im.cells32, im.n2, cc, v);

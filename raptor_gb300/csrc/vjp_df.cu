@@ -57,9 +57,11 @@ __device__ __forceinline__ F3 liftf(const F1& a) {
 }
 
 // The sample's metric (metric.c:94-137, 207-231) in FP32 with its
-// inclination tangent, from the DF point's leading parts (as metric_f32 in
-// ray_kernel_df.cu).
-__device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<DD1>& pd, const GeoDF& gd) {
+// inclination tangent, from the point's values rounded to FP32 (the DF
+// point's leading parts, or the FP64 point), as the forward samples'
+// metric_f32 (transfer.cuh).
+template <class P>
+__device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<P>& pd, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
     const F1 r = to_f1(pd.r), s = to_f1(pd.s), irho2 = to_f1(pd.iS);
     const F1 irp = to_f1(pd.irp), ithp = to_f1(pd.ithp), isn = to_f1(pd.isn);
@@ -279,20 +281,13 @@ struct FormMixed {
     __device__ static bool in_grid(const DevImage& im, const S y[8]) {
         return y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2;
     }
-    // rt_sample_fp32's inputs: the metric in FP64 (with its tangent) rounded
-    // to FP32, Xtoij in FP64 (cell_coef), the wave vector rounded to FP32
+    // rt_sample_fp32's inputs: the metric in FP32 from the FP64 point
+    // rounded (with its tangent), Xtoij in FP64 (cell_coef), the wave vector
+    // rounded to FP32
     template <bool K>
     __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
                                   SampleCommonF& out) {
-        MetricDDT<S> gd;
-        MetricUUT<S> gu;
-        mks_metric(p, im.geo, gd, gu);
-        MetricT<F3> g;
-        g.d00 = liftf(to_f1(gd.g00)); g.d01 = liftf(to_f1(gd.g01)); g.d03 = liftf(to_f1(gd.g03));
-        g.d11 = liftf(to_f1(gd.g11)); g.d13 = liftf(to_f1(gd.g13)); g.d22 = liftf(to_f1(gd.g22));
-        g.d33 = liftf(to_f1(gd.g33));
-        g.u00 = liftf(to_f1(gu.g00)); g.u01 = liftf(to_f1(gu.g01)); g.u11 = liftf(to_f1(gu.g11));
-        g.u13 = liftf(to_f1(gu.g13)); g.u22 = liftf(to_f1(gu.g22)); g.u33 = liftf(to_f1(gu.g33));
+        const MetricT<F3> g = metric_f3(p, im.geo_df);
         const CellCoef cc = cell_coef(im, y[1].v, y[2].v);
         const int i = cc.base / im.n2, j = cc.base - i * im.n2;
         F3 d1((float)cc.d1), d2((float)cc.d2);

@@ -91,6 +91,11 @@ struct DevImage {
     int emission;
     KappaConst kap;
     KappaConstF kapf;
+    // the point quantities at the camera position xcam, where every ray of
+    // the image starts: written by camera_point_kernel (ray_kernel.cuh) on
+    // the device after each upload, read by the FP64 and mixed kernels'
+    // start_ray
+    MksPoint cam_point;
 };
 
 // Per-step record of one traced ray (the analogue of the reference's GEOD

@@ -173,6 +173,9 @@ extern "C" int raptor_gpu_render_noalloc(int device, const double* d_cells, cons
         cudaMemcpyAsync(d_desc, h_desc, sizeof(DevImage) * n_imgs, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(d_map, h_map, sizeof(int) * 2 * nspec, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return RAPTOR_ERR_CUDA;
+    // the camera's point quantities, which the ray kernel reads from each image
+    camera_point_kernel<<<(n_imgs + 127) / 128, 128, 0, st>>>(d_desc, n_imgs);
+    if (cudaGetLastError() != cudaSuccess) return RAPTOR_ERR_CUDA;
 
     // the FP64 form's default kernel and launch shape, as raptor_gpu_render
     // picks them without tuning

@@ -503,6 +503,8 @@ int prepare_batch(raptor_gpu_ctx* ctx, const raptor_image_desc* imgs, int n_imgs
         map[b.spec_len + s] = b.spec_f[s];
     }
     CK(cudaMemcpyAsync(ctx->d_imgs, ctx->h_imgs, sizeof(DevImage) * n_imgs, cudaMemcpyHostToDevice, ctx->stream));
+    camera_point_kernel<<<(n_imgs + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_imgs, n_imgs);
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(ctx->d_spec_map, map.data(), sizeof(int) * 2 * b.spec_len, cudaMemcpyHostToDevice,
                        ctx->stream));
     b.h2d_bytes = sizeof(DevImage) * n_imgs + sizeof(int) * 2 * b.spec_len;

@@ -356,7 +356,7 @@ __device__ __forceinline__ const DevImage* start_ray(const DevImage* __restrict_
     s.rid = rid;
     const int px = s.pix % im->width, py = s.pix / im->width;
     init_photon(*im, camera_of(*im), px, py, s.y, s.beta);
-    mks_point(s.y[1], s.y[2], im->geo, s.p);
+    s.p = im->cam_point;  // mks_point at (xcam[1], xcam[2]), once per image
     s.steps = 0;
     s.turns = 0;
     s.stop = 0;
@@ -727,6 +727,19 @@ __global__ void __launch_bounds__(kRayMaxBlock, RAPTOR_POOL_MIN_BLOCKS)
 // Spectrum: core.c:146-150 sums intensityfield over pixels per frequency.
 // One block per (image, frequency) in a fixed-order tree, so the result is
 // deterministic.  spec_img[s], spec_f[s] map spectrum slot s to its source.
+// The camera's point quantities (mks_point at xcam[1], xcam[2], the same for
+// every ray of an image), once per image after the images are uploaded and
+// before any ray kernel reads them: per ray, the FP64 pipe evaluated them on
+// the one or two lanes that a refill starts, at the cost of a full warp.
+static __global__ void camera_point_kernel(DevImage* __restrict__ imgs, int n_imgs) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n_imgs) {
+        MksPoint p;
+        mks_point(imgs[k].xcam[1], imgs[k].xcam[2], imgs[k].geo, p);
+        imgs[k].cam_point = p;
+    }
+}
+
 static __global__ void spectrum_kernel(const DevImage* __restrict__ imgs, const int* __restrict__ spec_img,
                                 const int* __restrict__ spec_f, const double* __restrict__ out,
                                 double* __restrict__ spectrum) {

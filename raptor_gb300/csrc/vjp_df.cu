@@ -61,7 +61,7 @@ __device__ __forceinline__ F3 liftf(const F1& a) {
 // point's leading parts, or the FP64 point), as the forward samples'
 // metric_f32 (transfer.cuh).
 template <class P>
-__device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<P>& pd, const GeoDF& gd) {
+__device__ __forceinline__ MetricT<F1> metric_f1(const MksPointT<P>& pd, const GeoDF& gd) {
     const float a = gd.a.hi, a2 = gd.a2.hi, R0 = gd.R0.hi;
     const F1 r = to_f1(pd.r), s = to_f1(pd.s), irho2 = to_f1(pd.iS);
     const F1 irp = to_f1(pd.irp), ithp = to_f1(pd.ithp), isn = to_f1(pd.isn);
@@ -72,21 +72,31 @@ __device__ __forceinline__ MetricT<F3> metric_f3(const MksPointT<P>& pd, const G
     const F1 z = 2.0f * (r * irho2);
     const F1 ir = (R0 == 0.0f) ? irp : F1(1.0f) / r;
     const F1 opz = 1.0f + z;
-    MetricT<F3> g;
-    g.d00 = liftf(-1.0f + z);
-    g.d01 = liftf(z * rfac);
-    g.d03 = liftf((-a) * (z * s2));
-    g.d11 = liftf(opz * rfac * rfac);
-    g.d13 = liftf((-a) * (s2 * opz * rfac));
-    g.d22 = liftf(rho2 * hfac * hfac);
-    g.d33 = liftf(s2 * (rho2 + a2 * (s2 * opz)));
-    g.u00 = liftf(-1.0f - z);
-    g.u01 = liftf(2.0f * irho2);
-    g.u11 = liftf(irho2 * (r * (r - 2.0f) + a2) * (ir * ir));
-    g.u13 = liftf(a * (irho2 * ir));
-    g.u22 = liftf(irho2 * (ithp * ithp));
-    g.u33 = liftf(irho2 * (isn * isn));
+    MetricT<F1> g;
+    g.d00 = -1.0f + z;
+    g.d01 = z * rfac;
+    g.d03 = (-a) * (z * s2);
+    g.d11 = opz * rfac * rfac;
+    g.d13 = (-a) * (s2 * opz * rfac);
+    g.d22 = rho2 * hfac * hfac;
+    g.d33 = s2 * (rho2 + a2 * (s2 * opz));
+    g.u00 = -1.0f - z;
+    g.u01 = 2.0f * irho2;
+    g.u11 = irho2 * (r * (r - 2.0f) + a2) * (ir * ir);
+    g.u13 = a * (irho2 * ir);
+    g.u22 = irho2 * (ithp * ithp);
+    g.u33 = irho2 * (isn * isn);
     return g;
+}
+
+// a F3 times an F1 (the second's ln Theta_e and ln B tangents are zero)
+__device__ __forceinline__ F3 mul31f(const F3& a, const F1& b) {
+    F3 r;
+    r.v = a.v * b.v;
+    r.d[kSIncl] = a.d[kSIncl] * b.v + a.v * b.d[0];
+    r.d[kSLnTh] = a.d[kSLnTh] * b.v;
+    r.d[kSLnB] = a.d[kSLnB] * b.v;
+    return r;
 }
 
 // The frequency-independent part of one FP32 sample with three tangents.
@@ -104,59 +114,64 @@ struct SampleCommonF {
 // The FP32 sample (rt_sample_fp32_core's fluid, tetrad projection and
 // emission prefactors) from its FP32 metric, the first of its four cells and
 // the bilinear offsets, the wave vector and |d lambda|, each with its
-// inclination tangent.
+// inclination tangent.  Everything up to the fluid's Theta_e and B depends
+// on the inclination alone and is carried as single-direction duals (F1);
+// Theta_e and B take their ln Theta_e and ln B directions, and only what
+// depends on them is F3.
 // K: the image takes the kappa fits (the adjoint kernels are instantiated
 // apart for them, so that the thermal kernels carry none of their code).
 template <bool K>
-__device__ bool sample_common_f(const DevImage& im, const MetricT<F3>& g, int base, const F3& d1, const F3& d2,
-                                const F3 (&k)[4], const F3& adl, SampleCommonF& out) {
+__device__ bool sample_common_f(const DevImage& im, const MetricT<F1>& g, int base, const F1& d1, const F1& d2,
+                                const F1 (&k)[4], const F1& adl, SampleCommonF& out) {
     out.base = base;
     out.d1 = d1.v;
     out.d2 = d2.v;
-    const F3 c0 = (1.0f - d1) * (1.0f - d2), c1 = (1.0f - d1) * d2, c2 = d1 * (1.0f - d2), c3 = d1 * d2;
+    const F1 c0 = (1.0f - d1) * (1.0f - d2), c1 = (1.0f - d1) * d2, c2 = d1 * (1.0f - d2), c3 = d1 * d2;
     float a[8], b[8], e[8], f[8];
     const float* cp = im.cells32 + (size_t)base * 8;
     load_cell(cp, a);
     load_cell(cp + 8, b);
     load_cell(cp + (size_t)im.n2 * 8, e);
     load_cell(cp + (size_t)im.n2 * 8 + 8, f);
-    F3 v[8];
+    F1 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = c0 * a[q] + c1 * b[q] + c2 * e[q] + c3 * f[q];
 
-    const F3 B_unit(im.b_unit_f);
-    Fluid<F3> fl;
-    if (!fluid_from_prims(v, g, F3(im.ne_unit_f), B_unit, F3(im.r_high_f), F3(im.r_low_f), fl)) return false;
+    const F1 B_unit(im.b_unit_f);
+    Fluid<F1> fl;
+    if (!fluid_from_prims(v, g, F1(im.ne_unit_f), B_unit, F1(im.r_high_f), F1(im.r_low_f), fl)) return false;
     out.ss.irho = fdiv(1.0f, v[0].v);
     thetae_log_derivs(v[0].v, v[1].v, fl.bsq.v, im.r_high_f, im.r_low_f, out.ss.dlnth);
     // |b| in code units for the pitch angle, which M_unit does not move:
     // formed before B takes its ln B direction
-    const F3 Bcode = fl.B / B_unit;
-    fl.thetae.d[kSLnTh] = fl.thetae.v;
-    fl.B.d[kSLnB] = fl.B.v - 1.e-20f;  // B = sqrt(Bsq) B_unit + tiny: the part that scales
+    const F1 Bcode = fl.B / B_unit;
+    F3 thetae = liftf(fl.thetae), B = liftf(fl.B);
+    thetae.d[kSLnTh] = fl.thetae.v;
+    B.d[kSLnB] = fl.B.v - 1.e-20f;  // B = sqrt(Bsq) B_unit + tiny: the part that scales
 
-    F3 kd[4];
+    F1 kd[4];
     lowerT(g, k, kd);
-    const F3* U = fl.ucon;
-    const F3* Bc = fl.bcon;
-    out.kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
-    F3 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(out.kU) * Bcode);
-    if (fabsf(pitch.v) > 1.0f) pitch = F3(pitch.v > 0.0f ? 1.0f : -1.0f);
-    out.adl = adl;
+    const F1* U = fl.ucon;
+    const F1* Bc = fl.bcon;
+    const F1 kU = kd[0] * U[0] + kd[1] * U[1] + kd[2] * U[2] + kd[3] * U[3];
+    out.kU = liftf(kU);
+    F1 pitch = (kd[0] * Bc[0] + kd[1] * Bc[1] + kd[2] * Bc[2] + kd[3] * Bc[3]) / (fabs(kU) * Bcode);
+    if (fabsf(pitch.v) > 1.0f) pitch = F1(pitch.v > 0.0f ? 1.0f : -1.0f);
+    out.adl = liftf(adl);
     if constexpr (K) {
-        out.nus = fl.B;
-        out.xpre = fl.thetae;
-        out.jpre = fl.ne;
-        out.kcos = pitch;
+        out.nus = B;
+        out.xpre = thetae;
+        out.jpre = liftf(fl.ne);
+        out.kcos = liftf(pitch);
         out.emits = true;
         return true;
     }
-    const F3 sth = sqrt(1.0f - pitch * pitch);
-    const F3 nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * fl.B;
-    out.nus = (2.0f / 9.0f) * nuc * fl.thetae * fl.thetae * sth;
+    const F1 sth = sqrt(1.0f - pitch * pitch);
+    const F3 nuc = (float)(kECharge / (2.0 * CUDART_PI * kEMass * kC)) * B;
+    out.nus = mul31f((2.0f / 9.0f) * nuc * thetae * thetae, sth);
     out.emits = (fabsf(sth.v) >= 1.e-10f) && (fl.thetae.v > 1e-4f);
-    out.jpre = fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0) * nuc * sth;
-    out.xpre = (float)(kPlanck / (kEMass * kC * kC)) / fl.thetae;
+    out.jpre = mul31f(mul31f(nuc, fl.ne * (float)(1.4142135623730951 * CUDART_PI / 27.0)), sth);
+    out.xpre = (float)(kPlanck / (kEMass * kC * kC)) / thetae;
     return true;
 }
 
@@ -238,22 +253,22 @@ struct FormDF {
     template <bool K>
     __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
                                   SampleCommonF& out) {
-        const MetricT<F3> g = metric_f3(p, im.geo_df);
+        const MetricT<F1> g = metric_f1(p, im.geo_df);
         const DF t1 = (y[1].v - im.startx1_df) * im.idx1_df - 0.5;
         const DF t2 = (y[2].v - im.startx2_df) * im.idx2_df - 0.5;
         int i = df_trunc(t1), j = df_trunc(t2);
-        F3 d1(0.0f), d2(0.0f);
+        F1 d1(0.0f), d2(0.0f);
         if (i < 0) i = 0;
-        else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F3(1.0f); }
-        else { d1 = F3(df_value(add_f(t1, (float)-i))); d1.d[kSIncl] = y[1].d[0] * im.idx1_df.hi; }
+        else if (i > im.n1 - 2) { i = im.n1 - 2; d1 = F1(1.0f); }
+        else { d1 = F1(df_value(add_f(t1, (float)-i))); d1.d[0] = y[1].d[0] * im.idx1_df.hi; }
         if (j < 0) j = 0;
-        else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F3(1.0f); }
-        else { d2 = F3(df_value(add_f(t2, (float)-j))); d2.d[kSIncl] = y[2].d[0] * im.idx2_df.hi; }
+        else if (j > im.n2 - 2) { j = im.n2 - 2; d2 = F1(1.0f); }
+        else { d2 = F1(df_value(add_f(t2, (float)-j))); d2.d[0] = y[2].d[0] * im.idx2_df.hi; }
         if (!chk(i >= 0 && i <= im.n1 - 2 && j >= 0 && j <= im.n2 - 2, im.check_word, kChkCell,
                  (long long)i * im.n2 + j))
             i = j = 0;
-        const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
-        return sample_common_f<K>(im, g, i * im.n2 + j, d1, d2, k, liftf(to_f1(adl)), out);
+        const F1 k[4] = {to_f1(y[4]), to_f1(y[5]), to_f1(y[6]), to_f1(y[7])};
+        return sample_common_f<K>(im, g, i * im.n2 + j, d1, d2, k, to_f1(adl), out);
     }
 };
 
@@ -287,16 +302,16 @@ struct FormMixed {
     template <bool K>
     __device__ static bool sample(const DevImage& im, const S y[8], const MksPointT<S>& p, const S& adl,
                                   SampleCommonF& out) {
-        const MetricT<F3> g = metric_f3(p, im.geo_df);
+        const MetricT<F1> g = metric_f1(p, im.geo_df);
         const CellCoef cc = cell_coef(im, y[1].v, y[2].v);
         const int i = cc.base / im.n2, j = cc.base - i * im.n2;
-        F3 d1((float)cc.d1), d2((float)cc.d2);
+        F1 d1((float)cc.d1), d2((float)cc.d2);
         const double t1 = (y[1].v - im.startx1) * im.idx1 - 0.5;
         const double t2 = (y[2].v - im.startx2) * im.idx2 - 0.5;
-        if ((int)t1 == i) d1.d[kSIncl] = (float)y[1].d[0] * (float)im.idx1;  // not clamped
-        if ((int)t2 == j) d2.d[kSIncl] = (float)y[2].d[0] * (float)im.idx2;
-        const F3 k[4] = {liftf(to_f1(y[4])), liftf(to_f1(y[5])), liftf(to_f1(y[6])), liftf(to_f1(y[7]))};
-        return sample_common_f<K>(im, g, cc.base, d1, d2, k, liftf(to_f1(adl)), out);
+        if ((int)t1 == i) d1.d[0] = (float)y[1].d[0] * (float)im.idx1;  // not clamped
+        if ((int)t2 == j) d2.d[0] = (float)y[2].d[0] * (float)im.idx2;
+        const F1 k[4] = {to_f1(y[4]), to_f1(y[5]), to_f1(y[6]), to_f1(y[7])};
+        return sample_common_f<K>(im, g, cc.base, d1, d2, k, to_f1(adl), out);
     }
 };
 

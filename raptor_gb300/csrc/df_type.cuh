@@ -42,7 +42,7 @@ __device__ __forceinline__ R renorm(const R& x) {
 // Geo (kerr_mks.cuh) with DF fields
 struct GeoDF {
     DF a, a2, hslope, R0;
-    DF one_m_h, th_coef, half_1mh;
+    DF one_m_h, th_coef;
 };
 
 // Type of the RK stage weights for a state type: FP64 constants for double

@@ -31,7 +31,6 @@ struct Geo {
     double a, a2, hslope, R0;
     double one_m_h;   // 1 - hslope
     double th_coef;   // (1 - hslope) / (2 pi): theta / pi = x2 + th_coef sin(2 pi x2)
-    double half_1mh;  // (1 - hslope)/2
 };
 
 // Quantities at one MKS position X = (x0, x1, x2, x3).

@@ -117,7 +117,6 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
     im.geo.hslope = g.hslope;
     im.geo.R0 = g.R0;
     im.geo.one_m_h = 1.0 - g.hslope;
-    im.geo.half_1mh = 0.5 * (1.0 - g.hslope);
     im.geo.th_coef = (1.0 - g.hslope) / (2.0 * M_PI);
 
     // camera grid (integrator.c:188-191)
@@ -209,9 +208,8 @@ int build_dev_image(raptor_gpu_ctx* ctx, const raptor_image_desc& d, DevImage& i
     im.r_high_f = (float)im.r_high;
     im.r_low_f = (float)im.r_low;
     // DF copies for the mixed-DF geodesic
-    im.geo_df = GeoDF{df_const(im.geo.a),       df_const(im.geo.a2),      df_const(im.geo.hslope),
-                      df_const(im.geo.R0),      df_const(im.geo.one_m_h), df_const(im.geo.th_coef),
-                      df_const(im.geo.half_1mh)};
+    im.geo_df = GeoDF{df_const(im.geo.a),  df_const(im.geo.a2),      df_const(im.geo.hslope),
+                      df_const(im.geo.R0), df_const(im.geo.one_m_h), df_const(im.geo.th_coef)};
     im.inv_stepsize_df = df_const(im.inv_stepsize);
     im.cutoff_inner_df = df_const(im.cutoff_inner);
     im.startx1_df = df_const(im.startx1);

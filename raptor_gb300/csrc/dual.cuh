@@ -44,6 +44,11 @@ template <>
 struct TanCast<float, DF> {
     __host__ __device__ static float of(const DF& x) { return x.hi; }
 };
+// off the FP64 pipe (fp32_math.cuh f32_of)
+template <>
+struct TanCast<float, double> {
+    __device__ static float of(const double& x) { return f32_of(x); }
+};
 template <class TD, class T>
 __host__ __device__ inline TD tan_cast(const T& x) {
     return TanCast<TD, T>::of(x);

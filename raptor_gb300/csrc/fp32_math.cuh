@@ -30,6 +30,26 @@ __device__ __forceinline__ float fsqrt(float x) {
     return r;
 }
 
+// double -> float on the integer pipes, for the FP32 tangents of FP64 values
+// (the mixed adjoint's dual products convert both factors' values).  The
+// hardware conversion issues to the FP64 pipe, one warp instruction per 16
+// SM cycles on this part: there the conversions were 8.7e9 of the mixed
+// adjoint's 23e9 FP64-pipe thread instructions.  This one rebiases the
+// exponent and rounds the significand to nearest, ties away from zero.  It
+// equals the IEEE conversion for magnitudes from 2^-126 up, except at exact
+// ties (one ulp apart there); it gives a signed zero below 2^-126, where
+// the IEEE conversion gives subnormals, and a signed infinity for NaN.
+__device__ __forceinline__ float f32_of(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    // exponent and 23 significand bits, the exponent's low 9 bits at 31:23;
+    // rebiased 1023 -> 127 (-0x380 = +0x80 in 9 bits), rounded on the 24th
+    unsigned f = __funnelshift_l(lo, hi, 3) + 0x40000000u + ((lo >> 28) & 1u);
+    // outside [2^-126, 2^128): zero below, infinity above (NaN included)
+    const unsigned e2 = hi << 1;
+    if (e2 - 0x70200000u >= 0x1fc00000u) f = e2 < 0x70200000u ? 0u : 0x7f800000u;
+    return __uint_as_float(f | (hi & 0x80000000u));
+}
+
 template <class T>
 __device__ __forceinline__ T fdiv(const T& a, const T& b) {
     return a / b;

@@ -64,6 +64,14 @@ __global__ void eval_f32(const float* a, const float* b, int n, float* out) {
     out[4 * i + 3] = sqrtf(fabsf(a[i]));
 }
 
+// f32_of (fp32_math.cuh) against the IEEE double -> float conversion
+__global__ void eval_f2f(const double* x, int n, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[2 * i] = raptor::f32_of(x[i]);
+    out[2 * i + 1] = (float)x[i];
+}
+
 static double ulpsf(float a, float b) {
     if (a == b) return 0;
     if (!std::isfinite(a) || !std::isfinite(b)) return 1e30;
@@ -172,9 +180,49 @@ int main() {
         else if (fabsf(qi) < 1.17549435e-38f) div_u_sub = fmax(div_u_sub, u);
         sqrt_u = fmax(sqrt_u, ulpsf(fo[4 * i + 2], fo[4 * i + 3]));
     }
+    // double -> float over magnitudes 2^-140 .. 2^140 of both signs, exact
+    // ties of the FP32 rounding, then zeros, infinities and NaN
+    for (int i = 0; i < n; ++i) {
+        s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+        const double u = (s >> 11) * (1.0 / 9007199254740992.0);
+        rx[i] = ((s >> 3) & 1 ? -1.0 : 1.0) * ldexp(1.0 + u, (int)((s >> 40) % 281) - 140);
+        if (i % 64 == 1) {  // a tie: 24 significant bits and a half
+            long long b;
+            memcpy(&b, &rx[i], 8);
+            b = (b & ~0x1fffffffll) | 0x10000000ll;
+            memcpy(&rx[i], &b, 8);
+        }
+    }
+    const double dspecial[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, 3.4028235677973366e38, 1e-40, -1e-39};
+    for (int k = 0; k < 8; ++k) rx[k] = dspecial[k];
+    cudaMemcpy(dx, rx.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    eval_f2f<<<(n + 255) / 256, 256>>>(dx, n, dfo);
+    cudaMemcpy(fo.data(), dfo, 2 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    double f2f_u = 0;
+    int f2f_bad = 0, f2f_ties = 0;
+    for (int i = 0; i < n; ++i) {
+        const float c = fo[2 * i], ci = fo[2 * i + 1];
+        const double ax = fabs(rx[i]);
+        if (rx[i] != rx[i]) {
+            f2f_bad += !std::isinf(c);  // NaN -> infinity
+        } else if (ax < 1.1754943508222875e-38) {
+            f2f_bad += !(c == 0.0f && std::signbit(c) == std::signbit(rx[i]));  // signed zero
+        } else if (std::isinf(ci)) {
+            f2f_bad += !(c == ci);
+        } else {
+            long long b;
+            memcpy(&b, &rx[i], 8);
+            const bool tie = (b & 0x1fffffffll) == 0x10000000ll;
+            const double u = ulpsf(c, ci);
+            f2f_ties += tie && u > 0;
+            if (!tie) f2f_bad += u > 0;  // equal but at ties
+            f2f_u = fmax(f2f_u, u);
+        }
+    }
     printf("exp_ulp %g sin_ulp %g cos_ulp %g sin_abs %g cos_abs %g df_exp_rel %g df_sin_abs %g df_cos_abs %g "
-           "df_div_rel %g rcp_ulp %g fdiv_ulp %g fdiv_sub_ulp %g fsqrt_ulp %g f32_special_bad %d err %s\n",
+           "df_div_rel %g rcp_ulp %g fdiv_ulp %g fdiv_sub_ulp %g fsqrt_ulp %g f32_special_bad %d "
+           "f2f_ulp %g f2f_bad %d f2f_tie_diffs %d err %s\n",
            me, ms, mc, abs_s, abs_c, df_e, df_s, df_c, df_q, rcp_u, div_u, div_u_sub, sqrt_u, special_bad,
-           cudaGetErrorString(cudaGetLastError()));
+           f2f_u, f2f_bad, f2f_ties, cudaGetErrorString(cudaGetLastError()));
     return 0;
 }

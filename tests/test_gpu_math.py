@@ -9,7 +9,10 @@ Newton-Raphson steps) within 1 ulp of the IEEE quotient.  The FP32
 samples' division and square root (csrc/fp32_math.cuh: PTX div.full.f32 and
 sqrt.approx.f32) within 2 ulp and 1 ulp of IEEE division and sqrtf, from
 subnormal to near-overflow magnitudes, with IEEE's zeros, infinities and
-NaNs."""
+NaNs.  The integer-pipe double -> float conversion of the mixed adjoint's
+tangents (csrc/fp32_math.cuh f32_of) equal to the IEEE conversion from
+2^-126 up but at exact ties (1 ulp there), signed zeros below, infinity for
+NaN."""
 import os
 import subprocess
 
@@ -37,3 +40,4 @@ def test_fast_math_against_cuda(tmp_path):
     assert float(vals["fdiv_ulp"]) <= 2 and float(vals["fdiv_sub_ulp"]) <= 2
     assert float(vals["fsqrt_ulp"]) <= 1
     assert vals["f32_special_bad"] == "0"
+    assert float(vals["f2f_ulp"]) <= 1 and vals["f2f_bad"] == "0"

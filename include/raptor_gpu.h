@@ -249,8 +249,8 @@ int raptor_gpu_vjp_range(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
  * one fixed device array in the library that every GPU loading the library
  * keeps until exit.  The first call on each device (and the first after that
  * device's context was re-created, e.g. by cudaDeviceReset) looks up the
- * array's device address with cudaGetSymbolAddress: make that first call
- * before any stream capture begins.  All calls share the array, which keeps
+ * array's device address with cudaGetSymbolAddress.  Being synchronous, no
+ * call may be made while a stream is being captured.  All calls share the array, which keeps
  * the last call's contents (each call clears its counters first): calls whose
  * GPU work overlaps race on it and must be serialised by the caller.  A batch
  * larger than RAPTOR_NOALLOC_MAX_IMAGES is rejected with

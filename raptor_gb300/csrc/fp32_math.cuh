@@ -50,6 +50,17 @@ __device__ __forceinline__ float f32_of(double x) {
     return __uint_as_float(f | (hi & 0x80000000u));
 }
 
+// a double in the working type T: f32_of for FP32, else the type's own
+// conversion
+template <class T>
+__device__ __forceinline__ T narrow(double x) {
+    return (T)x;
+}
+template <>
+__device__ __forceinline__ float narrow<float>(double x) {
+    return f32_of(x);
+}
+
 template <class T>
 __device__ __forceinline__ T fdiv(const T& a, const T& b) {
     return a / b;

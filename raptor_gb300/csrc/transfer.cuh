@@ -87,7 +87,7 @@ __device__ __forceinline__ void interp_prims_at(const T* __restrict__ cells, int
 template <class T>
 __device__ __forceinline__ void interp_prims(const T* __restrict__ cells, int n2, const CellCoef& cc,
                                              T v[8]) {
-    interp_prims_at(cells, n2, cc.base, (T)cc.d1, (T)cc.d2, v);
+    interp_prims_at(cells, n2, cc.base, narrow<T>(cc.d1), narrow<T>(cc.d2), v);
 }
 
 template <class T>
@@ -501,19 +501,20 @@ __device__ __forceinline__ MetricT<float> metric_f32(const PointF32& q, float a,
 // Mixed form: the cell coefficients from the FP64 geodesic state, the
 // metric in FP32 from the FP64 point rounded (computing it in FP64 and
 // rounding it took some 30 FP64-pipe instructions per sample, run with the
-// warp's non-sampling lanes idle).
+// warp's non-sampling lanes idle; the roundings are f32_of's, on the
+// integer pipes, for the same reason).
 template <int NF>
 __device__ __forceinline__ bool rt_sample_fp32(const DevImage& im, const double y[8], const MksPoint& p,
                                                double adl, float (&tau)[NF], float (&tauc)[NF],
                                                float (&I)[NF], float (&Ic)[NF]) {
-    const PointF32 q{(float)p.r, (float)p.s, (float)p.iS, (float)p.thp,
-                     (float)p.Sg, (float)p.irp, (float)p.ithp, (float)p.isn};
+    const PointF32 q{f32_of(p.r),  f32_of(p.s),   f32_of(p.iS),   f32_of(p.thp),
+                     f32_of(p.Sg), f32_of(p.irp), f32_of(p.ithp), f32_of(p.isn)};
     const MetricT<float> g = metric_f32(q, im.geo_df.a.hi, im.geo_df.a2.hi, im.geo_df.R0.hi);
     const CellCoef cc = cell_coef(im, y[1], y[2]);
     float v[8];
     interp_prims(im.cells32, im.n2, cc, v);
-    const float k[4] = {(float)y[4], (float)y[5], (float)y[6], (float)y[7]};
-    return rt_sample_fp32_core<NF>(im, g, v, k, [&](int f) { return (float)(adl * im.rg_over_nu[f]); }, tau,
+    const float k[4] = {f32_of(y[4]), f32_of(y[5]), f32_of(y[6]), f32_of(y[7])};
+    return rt_sample_fp32_core<NF>(im, g, v, k, [&](int f) { return f32_of(adl * im.rg_over_nu[f]); }, tau,
                                    tauc, I, Ic);
 }
 

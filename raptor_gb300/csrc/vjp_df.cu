@@ -46,8 +46,8 @@ __device__ __forceinline__ F1 to_f1(const DD1& x) {
 }
 template <class TD>
 __device__ __forceinline__ F1 to_f1(const Dual<1, double, TD>& x) {
-    F1 r((float)x.v);
-    r.d[0] = (float)x.d[0];
+    F1 r(f32_of(x.v));
+    r.d[0] = tan_cast<float>(x.d[0]);
     return r;
 }
 __device__ __forceinline__ F3 liftf(const F1& a) {
@@ -305,11 +305,11 @@ struct FormMixed {
         const MetricT<F1> g = metric_f1(p, im.geo_df);
         const CellCoef cc = cell_coef(im, y[1].v, y[2].v);
         const int i = cc.base / im.n2, j = cc.base - i * im.n2;
-        F1 d1((float)cc.d1), d2((float)cc.d2);
+        F1 d1(f32_of(cc.d1)), d2(f32_of(cc.d2));
         const double t1 = (y[1].v - im.startx1) * im.idx1 - 0.5;
         const double t2 = (y[2].v - im.startx2) * im.idx2 - 0.5;
-        if ((int)t1 == i) d1.d[0] = (float)y[1].d[0] * (float)im.idx1;  // not clamped
-        if ((int)t2 == j) d2.d[0] = (float)y[2].d[0] * (float)im.idx2;
+        if ((int)t1 == i) d1.d[0] = y[1].d[0] * im.idx1_df.hi;  // not clamped
+        if ((int)t2 == j) d2.d[0] = y[2].d[0] * im.idx2_df.hi;
         const F1 k[4] = {to_f1(y[4]), to_f1(y[5]), to_f1(y[6]), to_f1(y[7])};
         return sample_common_f<K>(im, g, cc.base, d1, d2, k, to_f1(adl), out);
     }

@@ -142,7 +142,9 @@ template <int N, class T, class TD> __host__ __device__ inline Dual<N, T, TD> op
 template <int N, class T, class TD>
 __host__ __device__ inline Dual<N, T, TD> operator*(const Dual<N, T, TD>& a, double b) {
     const T bb = scalar_cast<T>(b);
-    const TD bd = scalar_cast<TD>(b);
+    // FP64 values with FP32 tangents: runtime constants (the geometry's) off
+    // the FP64 pipe, as tan_cast
+    const TD bd = std::is_same<T, double>::value ? tan_cast<TD>(b) : scalar_cast<TD>(b);
     Dual<N, T, TD> r;
     r.v = a.v * bb;
 #pragma unroll

@@ -1,13 +1,15 @@
 // Forward-mode dual numbers for the adjoint (VJP) kernels: a value of type
 // T and N directional derivatives of type TD (default T) - double for the
-// FP64 adjoint; a DF value (df64.cuh) with FP32 tangents, and FP32 values and
-// tangents, for the mixed-DF adjoint - with the arithmetic and the libm
+// FP64 adjoint; a double value with FP32 tangents for the mixed adjoint; a DF
+// value (df64.cuh) with FP32 tangents for the mixed-DF adjoint; FP32 values
+// and tangents for both mixed samples - with the arithmetic and the libm
 // functions the imaging path uses.  Comparisons act on the value, so every
 // branch of the primal computation is taken as the primal takes it
 // (derivatives of the taken branch).  Plain double constants are converted
 // to T / TD first (scalar_cast), which folds at compile time for literals;
 // values enter tangent expressions through tan_cast (the leading FP32 part
-// of a DF value).  With T = TD = double both are the identity.
+// of a DF value; an FP64 value rounded on the integer pipes by f32_of).
+// With T = TD = double both are the identity.
 #pragma once
 #include <cuda_runtime.h>
 #include <math_constants.h>

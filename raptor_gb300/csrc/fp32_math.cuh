@@ -1,5 +1,6 @@
 // FP32 quotient and square root for the FP32 transfer samples (the mixed
-// and mixed-DF forms and their adjoints).
+// and mixed-DF forms and their adjoints), and the double -> float rounding
+// those samples and the mixed adjoint's tangents use (f32_of, below).
 //
 // CUDA's IEEE-rounded FP32 division and square root carry a branch to an
 // out-of-line slow path at every use.  The samples run between geodesic

@@ -83,7 +83,13 @@ typedef struct raptor_gpu_options {
                             samples in place; 0 (default) = a warp evaluates them 32 at a time
                             from a shared-memory pool.  The same arithmetic per ray: the images
                             agree bit for bit or to rounding. */
-    int reserved[7];
+    int vjp_tape;        /* mixed and mixed-DF raptor_gpu_vjp: 0 (default) = one adjoint pass
+                            that keeps each ray's per-cell terms on a per-lane device tape of 2048
+                            records and takes the ray's I from its own sums; n > 0 = n records per
+                            lane; -1 = two passes (the forward render, then the adjoint reading
+                            each pixel's I from it).  A ray with more records than fit makes the
+                            call fall back to two passes. */
+    int reserved[6];
 } raptor_gpu_options;
 
 /* Grid geometry: the HARM header fields the hot path uses

@@ -276,6 +276,7 @@ extern "C" void raptor_gpu_destroy(raptor_gpu_ctx* ctx) {
     cudaFree(ctx->d_grad);
     cudaFree(ctx->d_dldi);
     cudaFree(ctx->d_vjp_scratch);
+    cudaFree(ctx->d_vjp_tape);
     cudaFree(ctx->d_trace);
     cudaFreeHost(ctx->h_imgs);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);

@@ -31,6 +31,7 @@ enum : int {
     kCtrVjpEmit = 9,  // adjoint pass: emitting (sample, frequency) pairs
     kCtrVjpGate = 10, // adjoint pass: terms inside the tau gate
     kCtrCheck = 11,   // the checked build's first failed check (checked.cuh), 0 if none
+    kCtrTapeFull = 12,  // one-pass adjoint: rays whose records did not fit the lane's tape
     kCtrCount = 16
 };
 

@@ -740,14 +740,14 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 template <int NF, bool K>
 void launch_vjp_pool(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                      const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                     int refill, double* scratch, RayRange rr) {
+                     int refill, double* scratch, RayRange rr, VjpTape) {
     vjp_kernel_pool<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch, rr);
 }
 
 template <int NF, bool K>
 void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                 const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                int, double*, RayRange rr) {
+                int, double*, RayRange rr, VjpTape) {
     vjp_kernel<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, rr);
 }
 
@@ -798,6 +798,11 @@ VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows,
             return ctx_fail(ctx, RAPTOR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));  \
     } while (0)
 
+// Records per lane of the one-pass adjoint's tape unless the options say
+// otherwise: above the largest sample count of a ray in the benchmark images
+// (the longest rays take some 1600 steps).
+constexpr int kVjpTapeRecords = 2048;
+
 static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, long long ray_begin,
                     long long ray_count, const double* dL_dI, double* I_out, raptor_grad* grad) {
     if (!ctx) return RAPTOR_ERR_INVALID;
@@ -819,101 +824,135 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
                         ray_count);
     const long long rb = ray_begin, re = ray_count > b.total_rays - rb ? b.total_rays : rb + ray_count;
 
-    // forward render of the range (its image is the I of the suffix identity)
-    const void* fnp = nullptr;
-    RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp, !ctx->opt.no_sample_pool);
-    LaunchShape ls = choose_shape(ctx, b, precision, fn, fnp);
-    rc = enqueue_render(ctx, b, precision, rb, re, ls, fn, true);
-    if (rc) return rc;
-
     const size_t nout = (size_t)b.out_len;
     rc = ensure_buffer(ctx, (void**)&ctx->d_dldi, &ctx->dldi_cap, sizeof(double) * nout);
     if (!rc) rc = ensure_buffer(ctx, (void**)&ctx->d_grad, &ctx->grad_cap, sizeof(double) * (4 + 3 * ncell));
     if (rc) return rc;
     CK(cudaMemcpyAsync(ctx->d_dldi, dL_dI, sizeof(double) * nout, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_grad, 0, sizeof(double) * (4 + 3 * ncell), ctx->stream));
-    unsigned long long fwd_ctr[kCtrCount];
-    CK(cudaMemcpyAsync(fwd_ctr, ctx->d_counters, sizeof fwd_ctr, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    float fwd_ms = 0.f;
-    CK(cudaEventElapsedTime(&fwd_ms, ctx->evA, ctx->evB));
-    CK(cudaMemsetAsync(ctx->d_counters, 0, kCtrCount * sizeof(unsigned long long), ctx->stream));
 
     const CamT<D1> cam = camera_tangent(him, img->inclination, gs.geom.a, gs.geom.hslope);
-    // the adjoint of the form that rendered: FP64 duals for the FP64 form;
-    // for the mixed and mixed-DF forms their own geodesic with FP32
-    // tangents and the FP32 dual sample (vjp_df.cu)
-    int occ = 1;
-    const void* kp = nullptr;
-    int scratch_rows = 0;
     const bool kappa = img->emission == RAPTOR_EMISSION_KAPPA;
-    const VjpLaunchFn vfn = precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp, kappa)
-                            : precision == RAPTOR_PREC_MIXED
-                                ? pick_vjp_mixed(b.max_nf, &kp, kappa)
-                                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows, kappa);
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
-    const int grid = ctx->num_sms * std::max(occ, 1);
-    // the pooled adjoint's per-warp result slices (several frequencies)
-    if (scratch_rows > 0) {
-        rc = ensure_buffer(ctx, (void**)&ctx->d_vjp_scratch, &ctx->vjp_scratch_cap,
-                           sizeof(double) * (size_t)grid * (kVjpBlock / 32) * scratch_rows * kPoolCap);
-        if (rc) return rc;
-    }
-    double* gsc = ctx->d_grad;
     // the per-cell scatter runs when any of the three fields is asked for
     const bool fields = grad->d_rho || grad->d_u || grad->d_lnthetae;
+    double* gsc = ctx->d_grad;
     double* grho = fields ? ctx->d_grad + 4 : nullptr;
     double* gu = fields ? ctx->d_grad + 4 + ncell : nullptr;
     double* gth = fields ? ctx->d_grad + 4 + 2 * ncell : nullptr;
-    CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    vfn(grid, ctx->stream, ctx->d_imgs, cam, ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc, grho, gu, gth,
-        kVjpRefill, ctx->d_vjp_scratch, RayRange{rb, re});
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    double scal[4];
-    CK(cudaMemcpyAsync(scal, gsc, sizeof scal, cudaMemcpyDeviceToHost, ctx->stream));
-    if (grad->d_rho)
-        CK(cudaMemcpyAsync(grad->d_rho, grho, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
-    if (grad->d_u)
-        CK(cudaMemcpyAsync(grad->d_u, gu, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
-    if (grad->d_lnthetae)
-        CK(cudaMemcpyAsync(grad->d_lnthetae, gth, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
-    if (I_out) CK(cudaMemcpyAsync(I_out, ctx->d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
-    unsigned long long ctr[kCtrCount];
-    CK(cudaMemcpyAsync(ctr, ctx->d_counters, sizeof ctr, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    float vjp_ms = 0.f;
-    CK(cudaEventElapsedTime(&vjp_ms, ctx->ev0, ctx->ev1));
+    // The mixed and mixed-DF adjoints run in one pass (their own I, records
+    // on a tape) unless the options ask for two; a tape too small for some
+    // ray, or one that cannot be allocated, falls back to two passes.
+    bool one_pass = precision != RAPTOR_PREC_FP64 && ctx->opt.vjp_tape >= 0;
+    const int tape_cap = ctx->opt.vjp_tape > 0 ? ctx->opt.vjp_tape : kVjpTapeRecords;
+    const int tape_stride = vjp_tape_stride(b.max_nf);
+    for (;;) {
+        // two passes: the forward render of the range (its image is the I
+        // of the suffix identity)
+        float fwd_ms = 0.f;
+        unsigned long long fwd_ctr[kCtrCount] = {};
+        if (!one_pass) {
+            const void* fnp = nullptr;
+            RayLaunchFn fn = pick_ray_kernel(b.max_nf, precision, &fnp, !ctx->opt.no_sample_pool);
+            LaunchShape ls = choose_shape(ctx, b, precision, fn, fnp);
+            rc = enqueue_render(ctx, b, precision, rb, re, ls, fn, true);
+            if (rc) return rc;
+            CK(cudaMemcpyAsync(fwd_ctr, ctx->d_counters, sizeof fwd_ctr, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            CK(cudaEventElapsedTime(&fwd_ms, ctx->evA, ctx->evB));
+        } else {
+            // pixels outside the range stay 0, as the forward render leaves them
+            CK(cudaMemsetAsync(ctx->d_out, 0, sizeof(double) * nout, ctx->stream));
+        }
+        CK(cudaMemsetAsync(ctx->d_grad, 0, sizeof(double) * (4 + 3 * ncell), ctx->stream));
+        CK(cudaMemsetAsync(ctx->d_counters, 0, kCtrCount * sizeof(unsigned long long), ctx->stream));
 
-    grad->d_inclination = scal[0];
-    grad->d_m_unit = scal[1] / img->m_unit;  // the kernel differentiates with respect to ln M_unit
-    grad->d_r_high = scal[2];
-    grad->d_r_low = scal[3];
+        // the adjoint of the form that rendered: FP64 duals for the FP64 form;
+        // for the mixed and mixed-DF forms their own geodesic with FP32
+        // tangents and the FP32 dual sample (vjp_df.cu)
+        int occ = 1;
+        const void* kp = nullptr;
+        int scratch_rows = 0;
+        const VjpLaunchFn vfn =
+            precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp, kappa, one_pass)
+            : precision == RAPTOR_PREC_MIXED
+                ? pick_vjp_mixed(b.max_nf, &kp, kappa, one_pass)
+                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows, kappa);
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
+        const int grid = ctx->num_sms * std::max(occ, 1);
+        // the pooled adjoint's per-warp result slices (several frequencies)
+        if (scratch_rows > 0) {
+            rc = ensure_buffer(ctx, (void**)&ctx->d_vjp_scratch, &ctx->vjp_scratch_cap,
+                               sizeof(double) * (size_t)grid * (kVjpBlock / 32) * scratch_rows * kPoolCap);
+            if (rc) return rc;
+        }
+        VjpTape tape{nullptr, tape_cap, tape_stride, ctx->d_out};
+        if (one_pass && fields) {
+            const size_t bytes = sizeof(float) * (size_t)grid * kVjpBlock * (size_t)tape_cap * (size_t)tape_stride;
+            if (ensure_buffer(ctx, (void**)&ctx->d_vjp_tape, &ctx->vjp_tape_cap, bytes)) {
+                ctx->err[0] = 0;  // no room for the tape: two passes
+                one_pass = false;
+                continue;
+            }
+            tape.rec = ctx->d_vjp_tape;
+        }
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        vfn(grid, ctx->stream, ctx->d_imgs, cam, ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc, grho, gu, gth,
+            kVjpRefill, ctx->d_vjp_scratch, RayRange{rb, re}, tape);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        unsigned long long ctr[kCtrCount];
+        CK(cudaMemcpyAsync(ctr, ctx->d_counters, sizeof ctr, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (one_pass && ctr[kCtrTapeFull] > 0 && !ctr[kCtrCheck]) {
+            one_pass = false;  // some ray's records did not fit: two passes
+            continue;
+        }
+        double scal[4];
+        CK(cudaMemcpyAsync(scal, gsc, sizeof scal, cudaMemcpyDeviceToHost, ctx->stream));
+        if (grad->d_rho)
+            CK(cudaMemcpyAsync(grad->d_rho, grho, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
+        if (grad->d_u)
+            CK(cudaMemcpyAsync(grad->d_u, gu, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
+        if (grad->d_lnthetae)
+            CK(cudaMemcpyAsync(grad->d_lnthetae, gth, sizeof(double) * ncell, cudaMemcpyDeviceToHost, ctx->stream));
+        if (I_out)
+            CK(cudaMemcpyAsync(I_out, ctx->d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        float vjp_ms = 0.f;
+        CK(cudaEventElapsedTime(&vjp_ms, ctx->ev0, ctx->ev1));
 
-    raptor_gpu_stats& s = ctx->stats;
-    memset(&s, 0, sizeof s);
-    s.kernel_ms = vjp_ms;
-    s.device_ms = fwd_ms + vjp_ms;
-    // counters of the adjoint pass (the forward pass takes the same steps)
-    s.rays = (long long)ctr[kCtrRays];
-    s.steps = (long long)ctr[kCtrSteps];
-    s.rt_calls = (long long)ctr[kCtrRtCalls];
-    s.rt_samples = (long long)ctr[kCtrRtSamples];
-    s.vjp_terms = (long long)ctr[kCtrVjpEmit];
-    s.vjp_gated_terms = (long long)ctr[kCtrVjpGate];
-    s.n_nonfinite = (long long)fwd_ctr[kCtrNonFinite];
-    s.n_stepcap = (long long)fwd_ctr[kCtrStepCap];
-    const unsigned long long check = fwd_ctr[kCtrCheck] ? fwd_ctr[kCtrCheck] : ctr[kCtrCheck];
-    s.block_size = kVjpBlock;
-    s.grid_blocks = grid;
-    s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (check) return render_status(ctx, re - rb, re - rb, 0, 0, check);
-    if ((long long)ctr[kCtrRays] != re - rb)
-        return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "vjp kernel retired %lld rays, expected %lld",
-                        (long long)ctr[kCtrRays], re - rb);
-    // the forward render's status: its non-finite rays make the gradients
-    // meaningless, its step-capped rays are the reference's own behaviour
-    return render_status(ctx, (long long)fwd_ctr[kCtrRays], re - rb, s.n_nonfinite, s.n_stepcap, 0);
+        grad->d_inclination = scal[0];
+        grad->d_m_unit = scal[1] / img->m_unit;  // the kernel differentiates with respect to ln M_unit
+        grad->d_r_high = scal[2];
+        grad->d_r_low = scal[3];
+
+        // the render's counters: the forward pass's, or the one pass's own
+        const unsigned long long* rctr = one_pass ? ctr : fwd_ctr;
+        raptor_gpu_stats& s = ctx->stats;
+        memset(&s, 0, sizeof s);
+        s.kernel_ms = vjp_ms;
+        s.device_ms = fwd_ms + vjp_ms;
+        // counters of the adjoint pass (the forward pass takes the same steps)
+        s.rays = (long long)ctr[kCtrRays];
+        s.steps = (long long)ctr[kCtrSteps];
+        s.rt_calls = (long long)ctr[kCtrRtCalls];
+        s.rt_samples = (long long)ctr[kCtrRtSamples];
+        s.vjp_terms = (long long)ctr[kCtrVjpEmit];
+        s.vjp_gated_terms = (long long)ctr[kCtrVjpGate];
+        s.n_nonfinite = (long long)rctr[kCtrNonFinite];
+        s.n_stepcap = (long long)rctr[kCtrStepCap];
+        const unsigned long long check = fwd_ctr[kCtrCheck] ? fwd_ctr[kCtrCheck] : ctr[kCtrCheck];
+        s.block_size = kVjpBlock;
+        s.grid_blocks = grid;
+        s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (check) return render_status(ctx, re - rb, re - rb, 0, 0, check);
+        if ((long long)ctr[kCtrRays] != re - rb)
+            return ctx_fail(ctx, RAPTOR_ERR_DEVICE, "vjp kernel retired %lld rays, expected %lld",
+                            (long long)ctr[kCtrRays], re - rb);
+        // the render's status: its non-finite rays make the gradients
+        // meaningless, its step-capped rays are the reference's own behaviour
+        return render_status(ctx, (long long)(one_pass ? ctr[kCtrRays] : fwd_ctr[kCtrRays]), re - rb,
+                             s.n_nonfinite, s.n_stepcap, 0);
+    }
 }
 
 extern "C" int raptor_gpu_vjp(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int precision, const double* dL_dI,

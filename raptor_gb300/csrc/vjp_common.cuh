@@ -111,18 +111,34 @@ struct RayRange {
     long long begin, end;
 };
 
+// The one-pass adjoint's record tape (mixed and mixed-DF forms): lane l of
+// the launch (block * kVjpBlock + thread) keeps its ray's records at
+// rec + l * cap * stride, stride floats each (a multiple of 4), and writes
+// the pass's own image to out (image layout).  rec == nullptr: two passes.
+struct VjpTape {
+    float* rec;
+    int cap;     // records per lane
+    int stride;  // floats per record
+    double* out;
+};
+// floats per record for nf frequencies: cell, two offsets, d ln Theta_e /
+// d ln u, the two gated sums, and per frequency I before the sample and the
+// two suffix coefficients; padded to whole float4s
+inline int vjp_tape_stride(int nf) { return (6 + 3 * nf + 3) & ~3; }
+
 // Launch of the adjoint pass: grid blocks of kVjpBlock threads on stream st
 // for image im (device pointer), camera constants with their inclination
-// tangent, the forward image fwd and dL/dI dl (device, image layout);
-// accumulates into counters, gscal[4] and the per-cell arrays (which may be
-// null); lanes take new rays every refill steps; scratch is the sample
-// pool's result buffer where the kernel has one; rr the rays to cover.
+// tangent, the forward image fwd (unused with a tape) and dL/dI dl (device,
+// image layout); accumulates into counters, gscal[4] and the per-cell arrays
+// (which may be null); lanes take new rays every refill steps; scratch is
+// the sample pool's result buffer where the kernel has one; rr the rays to
+// cover; tape the one-pass tape where the kernel has one.
 using VjpLaunchFn = void (*)(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                              const double* dl, unsigned long long* counters, double* gscal, double* g_rho,
-                             double* g_u, double* g_th, int refill, double* scratch, RayRange rr);
-// the mixed-DF and the mixed adjoints for nf frequencies (vjp_df.cu); *fn
-// gets the kernel
-VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa);
-VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa);
+                             double* g_u, double* g_th, int refill, double* scratch, RayRange rr, VjpTape tape);
+// the mixed-DF and the mixed adjoints for nf frequencies (vjp_df.cu), the
+// one-pass (tape) or the two-pass kernel; *fn gets the kernel
+VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa, bool tape);
+VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa, bool tape);
 
 }  // namespace raptor

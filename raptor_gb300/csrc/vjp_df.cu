@@ -245,6 +245,10 @@ struct FormDF {
     __device__ static bool escaped(const DevImage& im, const S y[8]) {
         return y[1].v > im.stopx1_df && y[5].v.hi < 0.0f;
     }
+    // a finite photon state at the ray's end, as finish_ray tests it
+    __device__ static bool finite(const MksPointT<S>& p, const S y[8]) {
+        return p.rp.v.hi == p.rp.v.hi && isfinite(y[5].v.hi);
+    }
     __device__ static bool in_grid(const DevImage& im, const S y[8]) {
         return y[1].v < im.stopx1_df && y[1].v > im.startx1_df && y[2].v > im.startx2_df && y[2].v < im.stopx2_df;
     }
@@ -296,6 +300,9 @@ struct FormMixed {
     __device__ static bool in_grid(const DevImage& im, const S y[8]) {
         return y[1].v < im.stopx1 && y[1].v > im.startx1 && y[2].v > im.startx2 && y[2].v < im.stopx2;
     }
+    __device__ static bool finite(const MksPointT<S>& p, const S y[8]) {
+        return p.rp.v == p.rp.v && isfinite(y[5].v);
+    }
     // rt_sample_fp32's inputs: the metric in FP32 from the FP64 point
     // rounded (with its tangent), Xtoij in FP64 (cell_coef), the wave vector
     // rounded to FP32
@@ -325,6 +332,9 @@ struct AdjState {
     float dtg[NF][4];
     float dIw[4];
     int wexp;  // w[f] holds dL/dI_f * 2^-wexp; the ray's gradient terms are scaled back by 2^wexp
+    int nrec;     // one-pass adjoint: records on the lane's tape
+    bool full;    // one-pass adjoint: a record did not fit
+    bool replay;  // one-pass adjoint: the ended ray's records wait for the warp
 };
 
 // 2^e as a double for e in [-1022, 1023] (built from the exponent field).
@@ -333,22 +343,100 @@ __device__ __forceinline__ double pow2_double(int e) {
     return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// One sample's loss gradient with respect to the four cells' fields: Gr,
+// Gt, Gu the derivatives with respect to ln rho, ln Theta_e and ln u at the
+// sample (scaled by 2^-wexp), spread bilinearly over the cells.
+__device__ __forceinline__ void scatter_sample(float Gr, float Gt, float Gu, int base, float d1, float d2, int n2,
+                                               int wexp, double* __restrict__ g_rho, double* __restrict__ g_u,
+                                               double* __restrict__ g_th) {
+    if ((Gr != 0.0f || Gt != 0.0f) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu)) {
+        const float w0 = (1.0f - d1) * (1.0f - d2), w1 = (1.0f - d1) * d2;
+        const float w2 = d1 * (1.0f - d2), w3 = d1 * d2;
+        const long long c = base, cn = (long long)base + n2;
+        const double un = pow2_double(wexp);
+        const double gr = (double)Gr * un, gu = (double)Gu * un, gt = (double)Gt * un;
+        atomicAdd(&g_rho[c], gr * w0);
+        atomicAdd(&g_rho[c + 1], gr * w1);
+        atomicAdd(&g_rho[cn], gr * w2);
+        atomicAdd(&g_rho[cn + 1], gr * w3);
+        atomicAdd(&g_u[c], gu * w0);
+        atomicAdd(&g_u[c + 1], gu * w1);
+        atomicAdd(&g_u[cn], gu * w2);
+        atomicAdd(&g_u[cn + 1], gu * w3);
+        atomicAdd(&g_th[c], gt * w0);
+        atomicAdd(&g_th[c + 1], gt * w1);
+        atomicAdd(&g_th[cn], gt * w2);
+        atomicAdd(&g_th[cn + 1], gt * w3);
+    }
+}
+
 // The adjoint pass: lanes take rays from the queue and refill every
 // refill_interval steps, as the forward kernels do.
-template <int NF, class F, bool K>
+//
+// A sample's loss gradient with respect to its cells' fields takes, per
+// frequency, the intensity the ray gathers after it (the suffix I - I_before
+// of the transfer's exact derivative).  Two passes (TAPE false) read the
+// ray's I from the forward render of the same form.  One pass (TAPE) has
+// none: each sample inside the tau gate of some frequency writes a record to
+// the lane's tape - cell, offsets, d ln Theta_e / d ln u, the gated parts of
+// Gr and Gt, and per frequency I_before and the suffix coefficients - and
+// when the ray ends its own I (the same sums) closes the records, which are
+// then scattered; the pass also writes that I as the image.  Samples with
+// every frequency past the gate need no record: tau does not decrease (the
+// absorptivities are non-negative), so no later sample adds to I and their
+// suffix is exactly 0.
+template <int NF, class F, bool K, bool TAPE>
 __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>& cam, const double* __restrict__ fwd,
                                              const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                                              double* __restrict__ gscal, double* __restrict__ g_rho,
                                              double* __restrict__ g_u, double* __restrict__ g_th,
-                                             int refill_interval, RayRange rr) {
+                                             int refill_interval, RayRange rr, VjpTape tape) {
     using S = typename F::S;
     using G = typename std::remove_cv<typename std::remove_reference<decltype(F::geo(im))>::type>::type;
     const int lane = threadIdx.x & 31;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
+    unsigned long long n_nan = 0, n_cap = 0, n_full = 0;
+    // this lane's records (one pass, per-cell gradients asked for)
+    const size_t lane_floats = (size_t)tape.cap * (size_t)tape.stride;
+    float* const lane_tape =
+        TAPE && g_rho ? tape.rec + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * lane_floats : nullptr;
     AdjState<NF, F> s;
+    s.replay = false;
     bool active = false, live = true;
     while (true) {
+        if constexpr (TAPE) {
+            // The records of rays that ended, closed with their I and
+            // scattered by the whole warp, 32 records at a time: replayed by
+            // their own lane they would hold the warp for ~nrec record
+            // bodies, with the other lanes idle.
+            unsigned pend = __ballot_sync(kFull, s.replay);
+            if (pend) __syncwarp();  // the owners' record stores before the loads
+            while (pend) {
+                const int owner = __ffs(pend) - 1;
+                pend &= pend - 1;
+                const int nrec = __shfl_sync(kFull, s.nrec, owner);
+                const int wexp = __shfl_sync(kFull, s.wexp, owner);
+                float itot[NF];
+#pragma unroll
+                for (int f = 0; f < NF; ++f) itot[f] = __shfl_sync(kFull, s.Ipart[f], owner);
+                const float* otape = lane_tape + (long long)(owner - lane) * (long long)lane_floats;
+                for (int r = lane; r < nrec; r += 32) {
+                    const float* rq = otape + (size_t)r * (size_t)tape.stride;
+                    float Gr = rq[4], Gt = rq[5];
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        if (f >= im.nfreq) break;
+                        const float suffix = itot[f] - rq[6 + 3 * f];
+                        Gr -= rq[7 + 3 * f] * suffix;
+                        Gt -= rq[8 + 3 * f] * suffix;
+                    }
+                    scatter_sample(Gr, Gt, Gt * rq[3], __float_as_int(rq[0]), rq[1], rq[2], im.n2, wexp, g_rho,
+                                   g_u, g_th);
+                }
+            }
+            s.replay = false;
+        }
         const unsigned need = __ballot_sync(kFull, !active && live);
         if (need) {
             const int leader = __ffs(need) - 1;
@@ -393,7 +481,7 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                             // I in the units of the FP32 transfer (without e2_c)
                             const long long o = (long long)s.pix * im.nfreq + f;
                             const double dOdI = scale_output(im, ps, 1.0, f) * kE2C;
-                            s.Itot[f] = (float)(fwd[o] / dOdI);
+                            if constexpr (!TAPE) s.Itot[f] = (float)(fwd[o] / dOdI);
                             s.w[f] = (float)(dLdO[o] * dOdI * wscale);
                         }
                     }
@@ -403,6 +491,8 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                     s.turns = 0;
                     s.stop = 0;
                     s.thdot_prev = 0;
+                    s.nrec = 0;
+                    s.full = false;
                     active = true;
                 } else {
                     live = false;
@@ -430,23 +520,48 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                     if (F::template sample<K>(im, s.y, s.p, fabs(dl), sc)) {
                         ++n_samples;
                         float Gr = 0.0f, Gt = 0.0f;
+                        // one pass: this sample's record, if it has room
+                        float* const rp = lane_tape && s.nrec < tape.cap
+                                              ? lane_tape + (size_t)s.nrec * (size_t)tape.stride
+                                              : nullptr;
+                        bool live = false;
                         // one copy of the frequency body (the per-frequency
                         // state of a multi-frequency ray lives in local memory)
 #pragma unroll 1
                         for (int f = 0; f < NF; ++f) {
                             if (f >= im.nfreq) break;
                             F3 S3, dt;
-                            if (!sample_freq_f<K>(im, sc, f, S3, dt)) continue;
+                            if (!sample_freq_f<K>(im, sc, f, S3, dt)) {
+                                if (TAPE && rp) {
+                                    rp[6 + 3 * f] = 0.0f;
+                                    rp[7 + 3 * f] = 0.0f;
+                                    rp[8 + 3 * f] = 0.0f;
+                                }
+                                continue;
+                            }
                             ++n_emit;
                             s.tau[f] += dt.v;
 #pragma unroll
                             for (int q = 0; q < 4; ++q) s.dtg[f][q] += scalar_tangent(dt, sc.ss, q);
                             const float e = expf(-s.tau[f]);
                             const bool gate = s.tau[f] < 6.9077553f && !(s.tau[f] < 0.0f);
-                            const float suffix = s.Itot[f] - s.Ipart[f];
                             const float eS = gate ? e : 0.0f;
-                            Gr += s.w[f] * (eS * rho_tangent(S3, sc.ss) - suffix * rho_tangent(dt, sc.ss));
-                            Gt += s.w[f] * (eS * S3.d[kSLnTh] - suffix * dt.d[kSLnTh]);
+                            if constexpr (TAPE) {
+                                // the gated part now; the suffix part, with I,
+                                // when the ray ends
+                                Gr += s.w[f] * (eS * rho_tangent(S3, sc.ss));
+                                Gt += s.w[f] * (eS * S3.d[kSLnTh]);
+                                if (rp) {
+                                    rp[6 + 3 * f] = s.Ipart[f];
+                                    rp[7 + 3 * f] = s.w[f] * rho_tangent(dt, sc.ss);
+                                    rp[8 + 3 * f] = s.w[f] * dt.d[kSLnTh];
+                                }
+                                live = live || gate;
+                            } else {
+                                const float suffix = s.Itot[f] - s.Ipart[f];
+                                Gr += s.w[f] * (eS * rho_tangent(S3, sc.ss) - suffix * rho_tangent(dt, sc.ss));
+                                Gt += s.w[f] * (eS * S3.d[kSLnTh] - suffix * dt.d[kSLnTh]);
+                            }
                             if (gate) {
                                 ++n_gate;
                                 const float we = s.w[f] * e;
@@ -456,30 +571,47 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
                                 s.Ipart[f] += S3.v * e;
                             }
                         }
-                        const float Gu = Gt * sc.ss.dlnth[1];
-                        if ((Gr != 0.0f || Gt != 0.0f) && isfinite(Gr) && isfinite(Gt) && isfinite(Gu) && g_rho) {
-                            const float w0 = (1.0f - sc.d1) * (1.0f - sc.d2), w1 = (1.0f - sc.d1) * sc.d2;
-                            const float w2 = sc.d1 * (1.0f - sc.d2), w3 = sc.d1 * sc.d2;
-                            const long long c = sc.base, cn = sc.base + im.n2;
-                            const double un = pow2_double(s.wexp);
-                            const double gr = (double)Gr * un, gu = (double)Gu * un, gt = (double)Gt * un;
-                            atomicAdd(&g_rho[c], gr * w0);
-                            atomicAdd(&g_rho[c + 1], gr * w1);
-                            atomicAdd(&g_rho[cn], gr * w2);
-                            atomicAdd(&g_rho[cn + 1], gr * w3);
-                            atomicAdd(&g_u[c], gu * w0);
-                            atomicAdd(&g_u[c + 1], gu * w1);
-                            atomicAdd(&g_u[cn], gu * w2);
-                            atomicAdd(&g_u[cn + 1], gu * w3);
-                            atomicAdd(&g_th[c], gt * w0);
-                            atomicAdd(&g_th[c + 1], gt * w1);
-                            atomicAdd(&g_th[cn], gt * w2);
-                            atomicAdd(&g_th[cn + 1], gt * w3);
+                        if constexpr (TAPE) {
+                            if (live && lane_tape) {
+                                if (rp) {
+                                    rp[0] = __int_as_float(sc.base);
+                                    rp[1] = sc.d1;
+                                    rp[2] = sc.d2;
+                                    rp[3] = sc.ss.dlnth[1];
+                                    rp[4] = Gr;
+                                    rp[5] = Gt;
+                                    ++s.nrec;
+                                } else {
+                                    s.full = true;
+                                }
+                            }
+                        } else if (g_rho) {
+                            scatter_sample(Gr, Gt, Gt * sc.ss.dlnth[1], sc.base, sc.d1, sc.d2, im.n2, s.wexp, g_rho,
+                                           g_u, g_th);
                         }
                     }
                 }
             }
             if (done) {
+                if constexpr (TAPE) {
+                    // the ray's own I: the pass's image, and the suffixes
+                    // that close its records
+                    const long long oi = im.out_offset + (long long)s.pix * im.nfreq;
+                    const bool in_bounds = chk(oi >= 0 && oi + im.nfreq <= im.out_end, im.check_word, kChkOutput, oi);
+                    const PixelScale ps = pixel_scale(im, s.pix % im.width);
+                    bool finite = F::finite(s.p, s.y);
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        if (f >= im.nfreq || !in_bounds) break;
+                        const double o = scale_output(im, ps, (double)s.Ipart[f] * kE2C, f);
+                        tape.out[oi + f] = o;
+                        finite = finite && isfinite(o);
+                    }
+                    if (!finite) ++n_nan;
+                    if ((double)s.steps >= kMaxSteps) ++n_cap;
+                    if (s.full) ++n_full;  // the call falls back to two passes
+                    else s.replay = lane_tape && s.nrec > 0;  // at the warp's next refill
+                }
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (isfinite(s.dIw[q])) acc[q] += (double)s.dIw[q] * pow2_double(s.wexp);
@@ -498,6 +630,11 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
         n_samples += __shfl_xor_sync(kFull, n_samples, o);
         n_emit += __shfl_xor_sync(kFull, n_emit, o);
         n_gate += __shfl_xor_sync(kFull, n_gate, o);
+        if (TAPE) {
+            n_nan += __shfl_xor_sync(kFull, n_nan, o);
+            n_cap += __shfl_xor_sync(kFull, n_cap, o);
+            n_full += __shfl_xor_sync(kFull, n_full, o);
+        }
     }
     if (lane == 0) {
         atomicAdd(&counters[kCtrSteps], n_steps);
@@ -506,6 +643,11 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
         atomicAdd(&counters[kCtrRtSamples], n_samples);
         atomicAdd(&counters[kCtrVjpEmit], n_emit);
         atomicAdd(&counters[kCtrVjpGate], n_gate);
+        if (TAPE) {
+            atomicAdd(&counters[kCtrNonFinite], n_nan);
+            atomicAdd(&counters[kCtrStepCap], n_cap);
+            atomicAdd(&counters[kCtrTapeFull], n_full);
+        }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -529,54 +671,79 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
 #endif
 using MixedTangent = std::conditional<RAPTOR_VJP_MIXED_TANGENT_FP32 != 0, float, double>::type;
 
-template <int NF, bool K>
+template <int NF, bool K, bool TAPE>
 __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_DF_MIN_BLOCKS)
     vjp_kernel_df(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                   const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                   double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                  double* __restrict__ g_th, int refill_interval, RayRange rr) {
-    vjp_f32_body<NF, FormDF, K>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval, rr);
+                  double* __restrict__ g_th, int refill_interval, RayRange rr, VjpTape tape) {
+    vjp_f32_body<NF, FormDF, K, TAPE>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th, refill_interval, rr,
+                                      tape);
 }
 
-template <int NF, bool K>
+template <int NF, bool K, bool TAPE>
 __global__ void __launch_bounds__(kVjpBlock, RAPTOR_VJP_MIXED_MIN_BLOCKS)
     vjp_kernel_mixed(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                      const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                      double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                     double* __restrict__ g_th, int refill_interval, RayRange rr) {
-    vjp_f32_body<NF, FormMixed<MixedTangent>, K>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th,
-                                              refill_interval, rr);
+                     double* __restrict__ g_th, int refill_interval, RayRange rr, VjpTape tape) {
+    vjp_f32_body<NF, FormMixed<MixedTangent>, K, TAPE>(*imp, cam, fwd, dLdO, counters, gscal, g_rho, g_u, g_th,
+                                                       refill_interval, rr, tape);
 }
 
-template <int NF, bool K>
+template <int NF, bool K, bool TAPE>
 void launch_vjp_df(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                    const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                   int refill, double*, RayRange rr) {
-    vjp_kernel_df<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
+                   int refill, double*, RayRange rr, VjpTape tape) {
+    vjp_kernel_df<NF, K, TAPE><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr, tape);
 }
 
-template <int NF, bool K>
+template <int NF, bool K, bool TAPE>
 void launch_vjp_mixed(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                       const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                      int refill, double*, RayRange rr) {
-    vjp_kernel_mixed<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr);
+                      int refill, double*, RayRange rr, VjpTape tape) {
+    vjp_kernel_mixed<NF, K, TAPE><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, rr,
+                                                              tape);
+}
+
+template <bool TAPE>
+VjpLaunchFn pick_df(int nf, const void** fn, bool kappa) {
+    if (kappa) {
+        *fn = (const void*)vjp_kernel_df<kMaxFreqs, true, TAPE>;
+        return launch_vjp_df<kMaxFreqs, true, TAPE>;
+    }
+    if (nf <= 1) {
+        *fn = (const void*)vjp_kernel_df<1, false, TAPE>;
+        return launch_vjp_df<1, false, TAPE>;
+    }
+    *fn = (const void*)vjp_kernel_df<kMaxFreqs, false, TAPE>;
+    return launch_vjp_df<kMaxFreqs, false, TAPE>;
+}
+
+template <bool TAPE>
+VjpLaunchFn pick_mixed(int nf, const void** fn, bool kappa) {
+    if (kappa) {
+        *fn = (const void*)vjp_kernel_mixed<kMaxFreqs, true, TAPE>;
+        return launch_vjp_mixed<kMaxFreqs, true, TAPE>;
+    }
+    if (nf <= 1) {
+        *fn = (const void*)vjp_kernel_mixed<1, false, TAPE>;
+        return launch_vjp_mixed<1, false, TAPE>;
+    }
+    *fn = (const void*)vjp_kernel_mixed<kMaxFreqs, false, TAPE>;
+    return launch_vjp_mixed<kMaxFreqs, false, TAPE>;
 }
 
 }  // namespace
 
-// kappa: the kappa fits' instantiation (any frequency count)
-VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa) {
-    if (kappa) { *fn = (const void*)vjp_kernel_df<kMaxFreqs, true>; return launch_vjp_df<kMaxFreqs, true>; }
-    if (nf <= 1) { *fn = (const void*)vjp_kernel_df<1, false>; return launch_vjp_df<1, false>; }
-    *fn = (const void*)vjp_kernel_df<kMaxFreqs, false>;
-    return launch_vjp_df<kMaxFreqs, false>;
+// kappa: the kappa fits' instantiation (any frequency count); tape: the
+// one-pass kernel
+VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa, bool tape) {
+    return tape ? pick_df<true>(nf, fn, kappa) : pick_df<false>(nf, fn, kappa);
 }
 
-VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa) {
-    if (kappa) { *fn = (const void*)vjp_kernel_mixed<kMaxFreqs, true>; return launch_vjp_mixed<kMaxFreqs, true>; }
-    if (nf <= 1) { *fn = (const void*)vjp_kernel_mixed<1, false>; return launch_vjp_mixed<1, false>; }
-    *fn = (const void*)vjp_kernel_mixed<kMaxFreqs, false>;
-    return launch_vjp_mixed<kMaxFreqs, false>;
+VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa, bool tape) {
+    return tape ? pick_mixed<true>(nf, fn, kappa) : pick_mixed<false>(nf, fn, kappa);
 }
 
 }  // namespace raptor

@@ -59,7 +59,8 @@ class EngineWarning(UserWarning):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("block_size", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("refill_interval", ctypes.c_int), ("autotune", ctypes.c_int), ("use_graph", ctypes.c_int),
-                ("no_sample_pool", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("no_sample_pool", ctypes.c_int), ("vjp_tape", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
 
 
 class GridGeomC(ctypes.Structure):
@@ -157,11 +158,15 @@ class Engine:
     """One engine context on one CUDA device."""
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, refill_interval: int = 0,
-                 autotune: int = 0, use_graph: int = 0, no_sample_pool: int = 0, checked: bool = False):
+                 autotune: int = 0, use_graph: int = 0, no_sample_pool: int = 0, checked: bool = False,
+                 vjp_tape: int = 0):
         """checked: use the bounds-checked build of the library, where a
-        failed device-side index check fails the call with RAPTOR_ERR_DEVICE."""
+        failed device-side index check fails the call with RAPTOR_ERR_DEVICE.
+        vjp_tape: records per lane of the mixed and mixed-DF one-pass adjoint's
+        tape (0: 2048; -1: the two-pass VJP), raptor_gpu_options.vjp_tape."""
         self.lib = load(CHECKED_LIB_PATH if checked else LIB_PATH)
-        opt = Options(device, block_size, blocks_per_sm, refill_interval, autotune, use_graph, no_sample_pool)
+        opt = Options(device, block_size, blocks_per_sm, refill_interval, autotune, use_graph, no_sample_pool,
+                      vjp_tape)
         h = ctypes.c_void_p()
         rc = self.lib.raptor_gpu_init(ctypes.byref(opt), ctypes.byref(h))
         if rc != 0:

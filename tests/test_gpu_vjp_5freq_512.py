@@ -7,9 +7,11 @@
   --workload 5freq512): the four scalars and rho and u of 8 seeded cells, at the 1e-3
   bar of tests/test_gpu_vjp.py.
 * At full size (2048x2048), the mixed form's forward render and VJP: every
-  ray retired, finite gradients, the Theta_e-field identity, and peak device
-  memory within the workload's 60 GB budget (the adjoint keeps no
-  checkpoints).
+  ray retired, the one-pass adjoint's own image within 1e-5 of the forward
+  render's largest pixel, finite gradients, the Theta_e-field identity, and
+  peak device memory within the workload's 60 GB budget (the adjoint keeps
+  no checkpoints; the one pass's record tape holds 2048 records for each
+  resident lane).
 """
 import numpy as np
 import pytest
@@ -75,7 +77,8 @@ def test_full_size_2048_5freq_memory_and_identity(torus512):
         st = eng.stats()
     finally:
         eng.close()
-    assert np.array_equal(fimg, img)
+    assert float(np.abs(fimg - img).max()) <= 1e-5 * float(np.abs(img).max())
+    assert st["device_ms"] == pytest.approx(st["kernel_ms"])  # one pass
     assert st["rays"] == 2048 * 2048 and st["n_nonfinite"] == 0
     assert st["peak_device_bytes"] <= 60e9, st["peak_device_bytes"]
     for k in ("d_m_unit", "d_r_high", "d_r_low", "d_inclination"):

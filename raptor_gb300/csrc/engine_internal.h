@@ -70,7 +70,7 @@ struct raptor_gpu_ctx {
     size_t dldi_cap = 0;
     double* d_vjp_scratch = nullptr;  // the pooled FP64 adjoint's per-warp results (several frequencies)
     size_t vjp_scratch_cap = 0;
-    float* d_vjp_tape = nullptr;  // the one-pass adjoint's per-lane records
+    void* d_vjp_tape = nullptr;  // the one-pass adjoint's per-lane records
     size_t vjp_tape_cap = 0;
     double* d_trace = nullptr;
     size_t trace_cap = 0;

@@ -227,11 +227,21 @@ __device__ __forceinline__ int sample_freq(const DevImage& im, const SampleCommo
 // One frequency's terms of a sample, consumed in step order: tau, the part
 // of I accumulated so far, d tau / d(scalars), dL/dI dI/d(scalars) (dIw), and
 // the sample's sums Gr, Gt of w (g e^-tau dS/dx - (I - I_<k) ddelta/dx) for
-// x = rho_s and ln Theta_e.  kind is sample_freq's.
+// x = rho_s and ln Theta_e.  kind is sample_freq's.  One pass (TAPE): Gr, Gt
+// get the gated part only; the suffix part's I_<k and coefficients go to the
+// record's three slots rec (when it has room), and live tells whether the
+// sample is inside the gate (vjp_df.cu, vjp_f32_body, has the scheme).
+template <bool TAPE = false>
 __device__ __forceinline__ void consume_term(int kind, const D3& S, const D3& dt, const SampleScalars& ss, double w,
                                              double Itot, double& tau, double& Ipart, double (&dtg)[4],
                                              double (&dIw)[4], double& Gr, double& Gt,
-                                             unsigned long long& n_emit, unsigned long long& n_gate) {
+                                             unsigned long long& n_emit, unsigned long long& n_gate,
+                                             double* rec = nullptr, bool* live = nullptr) {
+    if (TAPE && rec && kind != 1) {
+        rec[0] = 0.0;
+        rec[1] = 0.0;
+        rec[2] = 0.0;
+    }
     if (kind == 1) {
         ++n_emit;
         tau += dt.v;
@@ -239,11 +249,24 @@ __device__ __forceinline__ void consume_term(int kind, const D3& S, const D3& dt
         for (int q = 0; q < 4; ++q) dtg[q] += scalar_tangent(dt, ss, q);
         const double e = fast_exp(-tau);
         const bool gate = tau < 6.907755278982137 && !(tau < 0.0);
-        const double suffix = Itot - Ipart;
         const double eS = gate ? e : 0.0;
-        if (suffix != 0.0 || gate) {
-            Gr += w * (eS * rho_tangent(S, ss) - suffix * rho_tangent(dt, ss));
-            Gt += w * (eS * S.d[kSLnTh] - suffix * dt.d[kSLnTh]);
+        if constexpr (TAPE) {
+            if (rec) {
+                rec[0] = Ipart;
+                rec[1] = w * rho_tangent(dt, ss);
+                rec[2] = w * dt.d[kSLnTh];
+            }
+            if (gate) {
+                Gr += w * (eS * rho_tangent(S, ss));
+                Gt += w * (eS * S.d[kSLnTh]);
+                *live = true;
+            }
+        } else {
+            const double suffix = Itot - Ipart;
+            if (suffix != 0.0 || gate) {
+                Gr += w * (eS * rho_tangent(S, ss) - suffix * rho_tangent(dt, ss));
+                Gt += w * (eS * S.d[kSLnTh] - suffix * dt.d[kSLnTh]);
+            }
         }
         if (gate) {
             ++n_gate;
@@ -481,12 +504,14 @@ struct Layout {
 };
 }  // namespace vpool
 
-template <int NF, bool K>
+// TAPE: one pass, the ray's records on the lane's tape (consume_term).
+template <int NF, bool K, bool TAPE>
 __global__ void __launch_bounds__(kVjpBlock, 1)
     vjp_kernel_pool(const DevImage* __restrict__ imp, CamT<D1> cam, const double* __restrict__ fwd,
                     const double* __restrict__ dLdO, unsigned long long* __restrict__ counters,
                     double* __restrict__ gscal, double* __restrict__ g_rho, double* __restrict__ g_u,
-                    double* __restrict__ g_th, int refill_interval, double* __restrict__ scratch, RayRange rr) {
+                    double* __restrict__ g_th, int refill_interval, double* __restrict__ scratch, RayRange rr,
+                    VjpTape tape) {
     using namespace vpool;
     using L = Layout<NF>;
     __shared__ double pool_mem[(kVjpBlock / 32) * L::kWarpDoubles];
@@ -504,6 +529,14 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                                                       L::kScratchRows * C;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     unsigned long long n_calls = 0, n_samples = 0, n_emit = 0, n_gate = 0, n_steps = 0, n_rays = 0;
+    unsigned long long n_nan = 0, n_cap = 0, n_full = 0;
+    // one pass: this lane's records (per-cell gradients asked for)
+    const size_t lane_elems = (size_t)tape.cap * (size_t)tape.stride;
+    double* const lane_tape =
+        TAPE && g_rho ? static_cast<double*>(tape.rec) + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * lane_elems
+                      : nullptr;
+    int nrec = 0, pix = 0;
+    bool full = false, replay = false;
 
     D1 y[8];
     MksPointT<D1> p;
@@ -518,6 +551,35 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     int since_refill = refill_interval;
 
     while (true) {
+        if constexpr (TAPE) {
+            // the records of rays that ended, closed with their I and
+            // scattered by the whole warp, 32 at a time (vjp_df.cu has the
+            // reason)
+            unsigned pend = __ballot_sync(kFull, replay);
+            if (pend) __syncwarp();  // the owners' record stores before the loads
+            while (pend) {
+                const int owner = __ffs(pend) - 1;
+                pend &= pend - 1;
+                const int onrec = __shfl_sync(kFull, nrec, owner);
+                double itot[NF];
+#pragma unroll
+                for (int f = 0; f < NF; ++f) itot[f] = __shfl_sync(kFull, Ipart[f], owner);
+                const double* otape = lane_tape + (long long)(owner - lane) * (long long)lane_elems;
+                for (int r = lane; r < onrec; r += 32) {
+                    const double* rq = otape + (size_t)r * (size_t)tape.stride;
+                    double Gr = rq[4], Gt = rq[5];
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) {
+                        if (f >= im.nfreq) break;
+                        const double suffix = itot[f] - rq[6 + 3 * f];
+                        Gr -= rq[7 + 3 * f] * suffix;
+                        Gt -= rq[8 + 3 * f] * suffix;
+                    }
+                    scatter_cells(g_rho, g_u, g_th, (long long)rq[0], im.n2, rq[1], rq[2], Gr, Gt, rq[3]);
+                }
+            }
+            replay = false;
+        }
         const unsigned need = __ballot_sync(kFull, mode == 0 && live);
         if (need && (since_refill >= refill_interval || !__any_sync(kFull, mode != 0))) {
             since_refill = 0;
@@ -528,7 +590,9 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             if (mode == 0 && live) {
                 const long long rid = rr.begin + (long long)(base + __popc(need & ((1u << lane) - 1u)));
                 if (rid < rr.end) {
-                    const int pix = (int)rid;
+                    pix = (int)rid;
+                    nrec = 0;
+                    full = false;
                     init_photon(im, cam, pix % im.width, pix / im.width, y, beta);
                     mks_point(y[1], y[2], im.geo, p);
                     const PixelScale ps = pixel_scale(im, pix % im.width);
@@ -543,7 +607,7 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                         if (f < im.nfreq) {
                             const long long o = (long long)pix * im.nfreq + f;
                             const double dOdI = scale_output(im, ps, 1.0, f);
-                            Itot[f] = fwd[o] / dOdI;
+                            if constexpr (!TAPE) Itot[f] = fwd[o] / dOdI;
                             w[f] = dLdO[o] * dOdI;
                         }
                     }
@@ -677,6 +741,11 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
 #pragma unroll
                         for (int q = 0; q < 4; ++q) ss.dlnth[q] = o[(3 + q) * C];
                         double Gr = 0.0, Gt = 0.0;
+                        // one pass: this sample's record, if it has room
+                        double* const rp = TAPE && lane_tape && nrec < tape.cap
+                                               ? lane_tape + (size_t)nrec * (size_t)tape.stride
+                                               : nullptr;
+                        bool in_gate = false;
 #pragma unroll 1
                         for (int f = 0; f < NF; ++f) {
                             if (f >= im.nfreq) break;
@@ -692,10 +761,26 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
                                     dt.d[q] = of[(5 + q) * C];
                                 }
                             }
-                            consume_term(kd, S, dt, ss, w[f], Itot[f], tau[f], Ipart[f], dtg[f], dIw, Gr, Gt,
-                                         n_emit, n_gate);
+                            consume_term<TAPE>(kd, S, dt, ss, w[f], Itot[f], tau[f], Ipart[f], dtg[f], dIw, Gr, Gt,
+                                               n_emit, n_gate, rp ? rp + 6 + 3 * f : nullptr, &in_gate);
                         }
-                        scatter_cells(g_rho, g_u, g_th, tbase[ta], im.n2, o[0], o[1 * C], Gr, Gt, ss.dlnth[1]);
+                        if constexpr (TAPE) {
+                            if (in_gate && lane_tape) {
+                                if (rp) {
+                                    rp[0] = (double)tbase[ta];
+                                    rp[1] = o[0];
+                                    rp[2] = o[1 * C];
+                                    rp[3] = ss.dlnth[1];
+                                    rp[4] = Gr;
+                                    rp[5] = Gt;
+                                    ++nrec;
+                                } else {
+                                    full = true;
+                                }
+                            }
+                        } else {
+                            scatter_cells(g_rho, g_u, g_th, tbase[ta], im.n2, o[0], o[1 * C], Gr, Gt, ss.dlnth[1]);
+                        }
                     }
                     ring.pop(nxt, ta);
                 }
@@ -709,6 +794,25 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
             n_steps += (unsigned long long)steps;
             n_rays += 1;
             mode = 0;
+            if constexpr (TAPE) {
+                // the ray's own I: the pass's image, and the suffixes that
+                // close its records (at the warp's next refill)
+                const long long oi = im.out_offset + (long long)pix * im.nfreq;
+                const bool in_bounds = chk(oi >= 0 && oi + im.nfreq <= im.out_end, cw, kChkOutput, oi);
+                const PixelScale ps = pixel_scale(im, pix % im.width);
+                bool finite = p.rp.v == p.rp.v && isfinite(y[5].v);
+#pragma unroll
+                for (int f = 0; f < NF; ++f) {
+                    if (f >= im.nfreq || !in_bounds) break;
+                    const double ov = scale_output(im, ps, Ipart[f], f);
+                    tape.out[oi + f] = ov;
+                    finite = finite && isfinite(ov);
+                }
+                if (!finite) ++n_nan;
+                if ((double)steps >= kMaxSteps) ++n_cap;
+                if (full) ++n_full;  // the call falls back to two passes
+                else replay = lane_tape && nrec > 0;
+            }
         }
     }
 #pragma unroll
@@ -719,6 +823,11 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
         n_samples += __shfl_xor_sync(kFull, n_samples, o);
         n_emit += __shfl_xor_sync(kFull, n_emit, o);
         n_gate += __shfl_xor_sync(kFull, n_gate, o);
+        if (TAPE) {
+            n_nan += __shfl_xor_sync(kFull, n_nan, o);
+            n_cap += __shfl_xor_sync(kFull, n_cap, o);
+            n_full += __shfl_xor_sync(kFull, n_full, o);
+        }
     }
     if (lane == 0) {
         atomicAdd(&counters[kCtrSteps], n_steps);
@@ -727,6 +836,11 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
         atomicAdd(&counters[kCtrRtSamples], n_samples);
         atomicAdd(&counters[kCtrVjpEmit], n_emit);
         atomicAdd(&counters[kCtrVjpGate], n_gate);
+        if (TAPE) {
+            atomicAdd(&counters[kCtrNonFinite], n_nan);
+            atomicAdd(&counters[kCtrStepCap], n_cap);
+            atomicAdd(&counters[kCtrTapeFull], n_full);
+        }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -737,11 +851,12 @@ __global__ void __launch_bounds__(kVjpBlock, 1)
     }
 }
 
-template <int NF, bool K>
+template <int NF, bool K, bool TAPE>
 void launch_vjp_pool(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& cam, const double* fwd,
                      const double* dl, unsigned long long* ctr, double* gs, double* gr, double* gu, double* gt,
-                     int refill, double* scratch, RayRange rr, VjpTape) {
-    vjp_kernel_pool<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch, rr);
+                     int refill, double* scratch, RayRange rr, VjpTape tape) {
+    vjp_kernel_pool<NF, K, TAPE><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, refill, scratch,
+                                                             rr, tape);
 }
 
 template <int NF, bool K>
@@ -751,40 +866,51 @@ void launch_vjp(int grid, cudaStream_t st, const DevImage* im, const CamT<D1>& c
     vjp_kernel<NF, K><<<grid, kVjpBlock, 0, st>>>(im, cam, fwd, dl, ctr, gs, gr, gu, gt, rr);
 }
 
-// pool: the sample-pool kernel; *scratch_rows gets the scratch rows (of
-// kPoolCap doubles) it needs per warp.  kappa: the kappa fits'
-// instantiation (any frequency count).
-VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows, bool kappa) {
-    *scratch_rows = 0;
+// The pooled kernel for nf frequencies, one pass (TAPE) or two.
+template <bool TAPE>
+VjpLaunchFn pick_pool(int nf, const void** fn, int* scratch_rows, bool kappa) {
     if (kappa) {
-        if (pool) {
-            *fn = (const void*)vjp_kernel_pool<8, true>;
-            *scratch_rows = vpool::Layout<8>::kScratchRows;
-            return launch_vjp_pool<8, true>;
-        }
-        *fn = (const void*)vjp_kernel<8, true>;
-        return launch_vjp<8, true>;
+        *fn = (const void*)vjp_kernel_pool<8, true, TAPE>;
+        *scratch_rows = vpool::Layout<8>::kScratchRows;
+        return launch_vjp_pool<8, true, TAPE>;
     }
-#define PICK(NF)                                                                         \
-    if (nf <= NF) {                                                                      \
-        if (pool) {                                                                      \
-            *fn = (const void*)vjp_kernel_pool<NF, false>;                               \
-            *scratch_rows = vpool::Layout<NF>::kScratchRows;                             \
-            return launch_vjp_pool<NF, false>;                                           \
-        }                                                                                \
-        *fn = (const void*)vjp_kernel<NF, false>;                                        \
-        return launch_vjp<NF, false>;                                                    \
+#define PICK(NF)                                                  \
+    if (nf <= NF) {                                               \
+        *fn = (const void*)vjp_kernel_pool<NF, false, TAPE>;      \
+        *scratch_rows = vpool::Layout<NF>::kScratchRows;          \
+        return launch_vjp_pool<NF, false, TAPE>;                  \
     }
     PICK(1)
     PICK(2)
     PICK(4)
     PICK(5)
 #undef PICK
-    if (pool) {
-        *fn = (const void*)vjp_kernel_pool<8, false>;
-        *scratch_rows = vpool::Layout<8>::kScratchRows;
-        return launch_vjp_pool<8, false>;
+    *fn = (const void*)vjp_kernel_pool<8, false, TAPE>;
+    *scratch_rows = vpool::Layout<8>::kScratchRows;
+    return launch_vjp_pool<8, false, TAPE>;
+}
+
+// pool: the sample-pool kernel (one pass with tape, two without); else the
+// in-place kernel (two passes); *scratch_rows gets the scratch rows (of
+// kPoolCap doubles) the pooled kernel needs per warp.  kappa: the kappa
+// fits' instantiation (any frequency count).
+VjpLaunchFn pick_vjp_fp64(int nf, const void** fn, bool pool, int* scratch_rows, bool kappa, bool tape) {
+    *scratch_rows = 0;
+    if (pool) return tape ? pick_pool<true>(nf, fn, scratch_rows, kappa) : pick_pool<false>(nf, fn, scratch_rows, kappa);
+    if (kappa) {
+        *fn = (const void*)vjp_kernel<8, true>;
+        return launch_vjp<8, true>;
     }
+#define PICK(NF)                                 \
+    if (nf <= NF) {                              \
+        *fn = (const void*)vjp_kernel<NF, false>; \
+        return launch_vjp<NF, false>;            \
+    }
+    PICK(1)
+    PICK(2)
+    PICK(4)
+    PICK(5)
+#undef PICK
     *fn = (const void*)vjp_kernel<8, false>;
     return launch_vjp<8, false>;
 }
@@ -838,12 +964,15 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
     double* grho = fields ? ctx->d_grad + 4 : nullptr;
     double* gu = fields ? ctx->d_grad + 4 + ncell : nullptr;
     double* gth = fields ? ctx->d_grad + 4 + 2 * ncell : nullptr;
-    // The mixed and mixed-DF adjoints run in one pass (their own I, records
-    // on a tape) unless the options ask for two; a tape too small for some
-    // ray, or one that cannot be allocated, falls back to two passes.
-    bool one_pass = precision != RAPTOR_PREC_FP64 && ctx->opt.vjp_tape >= 0;
+    // The adjoints run in one pass (their own I, records on a tape) unless
+    // the options ask for two (or, in FP64, for the in-place kernel); a tape
+    // too small for some ray, or one that cannot be allocated, falls back to
+    // two passes.
+    const bool fp64 = precision == RAPTOR_PREC_FP64;
+    bool one_pass = ctx->opt.vjp_tape >= 0 && !(fp64 && ctx->opt.no_sample_pool);
     const int tape_cap = ctx->opt.vjp_tape > 0 ? ctx->opt.vjp_tape : kVjpTapeRecords;
-    const int tape_stride = vjp_tape_stride(b.max_nf);
+    const int tape_stride = vjp_tape_stride(b.max_nf, fp64);
+    const size_t tape_elem = fp64 ? sizeof(double) : sizeof(float);
     for (;;) {
         // two passes: the forward render of the range (its image is the I
         // of the suffix identity)
@@ -875,7 +1004,7 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
             precision == RAPTOR_PREC_MIXED_DF ? pick_vjp_df(b.max_nf, &kp, kappa, one_pass)
             : precision == RAPTOR_PREC_MIXED
                 ? pick_vjp_mixed(b.max_nf, &kp, kappa, one_pass)
-                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows, kappa);
+                : pick_vjp_fp64(b.max_nf, &kp, !ctx->opt.no_sample_pool, &scratch_rows, kappa, one_pass);
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, kVjpBlock, 0));
         const int grid = ctx->num_sms * std::max(occ, 1);
         // the pooled adjoint's per-warp result slices (several frequencies)
@@ -886,7 +1015,7 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
         }
         VjpTape tape{nullptr, tape_cap, tape_stride, ctx->d_out};
         if (one_pass && fields) {
-            const size_t bytes = sizeof(float) * (size_t)grid * kVjpBlock * (size_t)tape_cap * (size_t)tape_stride;
+            const size_t bytes = tape_elem * (size_t)grid * kVjpBlock * (size_t)tape_cap * (size_t)tape_stride;
             if (ensure_buffer(ctx, (void**)&ctx->d_vjp_tape, &ctx->vjp_tape_cap, bytes)) {
                 ctx->err[0] = 0;  // no room for the tape: two passes
                 one_pass = false;

@@ -111,20 +111,24 @@ struct RayRange {
     long long begin, end;
 };
 
-// The one-pass adjoint's record tape (mixed and mixed-DF forms): lane l of
-// the launch (block * kVjpBlock + thread) keeps its ray's records at
-// rec + l * cap * stride, stride floats each (a multiple of 4), and writes
-// the pass's own image to out (image layout).  rec == nullptr: two passes.
+// The one-pass adjoint's record tape: lane l of the launch (block *
+// kVjpBlock + thread) keeps its ray's records at rec + l * cap * stride,
+// stride elements each (FP32 for the mixed and mixed-DF adjoints, FP64 for
+// the FP64 one), and the pass writes its own image to out (image layout).
+// A record: cell, two offsets, d ln Theta_e / d ln u, the two gated sums,
+// and per frequency I before the sample and the two suffix coefficients.
+// rec == nullptr: two passes.
 struct VjpTape {
-    float* rec;
+    void* rec;
     int cap;     // records per lane
-    int stride;  // floats per record
+    int stride;  // elements per record
     double* out;
 };
-// floats per record for nf frequencies: cell, two offsets, d ln Theta_e /
-// d ln u, the two gated sums, and per frequency I before the sample and the
-// two suffix coefficients; padded to whole float4s
-inline int vjp_tape_stride(int nf) { return (6 + 3 * nf + 3) & ~3; }
+// elements per record for nf frequencies, padded to 16 bytes
+inline int vjp_tape_stride(int nf, bool fp64) {
+    const int n = 6 + 3 * nf;
+    return fp64 ? (n + 1) & ~1 : (n + 3) & ~3;
+}
 
 // Launch of the adjoint pass: grid blocks of kVjpBlock threads on stream st
 // for image im (device pointer), camera constants with their inclination
@@ -137,7 +141,8 @@ using VjpLaunchFn = void (*)(int grid, cudaStream_t st, const DevImage* im, cons
                              const double* dl, unsigned long long* counters, double* gscal, double* g_rho,
                              double* g_u, double* g_th, int refill, double* scratch, RayRange rr, VjpTape tape);
 // the mixed-DF and the mixed adjoints for nf frequencies (vjp_df.cu), the
-// one-pass (tape) or the two-pass kernel; *fn gets the kernel
+// one-pass (tape) or the two-pass kernel; *fn gets the kernel.  (The FP64
+// adjoints' picker is pick_vjp_fp64, vjp.cu.)
 VjpLaunchFn pick_vjp_df(int nf, const void** fn, bool kappa, bool tape);
 VjpLaunchFn pick_vjp_mixed(int nf, const void** fn, bool kappa, bool tape);
 

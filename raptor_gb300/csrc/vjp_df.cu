@@ -400,7 +400,8 @@ __device__ __forceinline__ void vjp_f32_body(const DevImage& im, const CamT<D1>&
     // this lane's records (one pass, per-cell gradients asked for)
     const size_t lane_floats = (size_t)tape.cap * (size_t)tape.stride;
     float* const lane_tape =
-        TAPE && g_rho ? tape.rec + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * lane_floats : nullptr;
+        TAPE && g_rho ? static_cast<float*>(tape.rec) + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * lane_floats
+                      : nullptr;
     AdjState<NF, F> s;
     s.replay = false;
     bool active = false, live = true;

@@ -120,7 +120,8 @@ def test_vjp_against_reference_finite_differences(torus256, prec):
     dl = img - target
     assert 0.5 * np.sum(dl ** 2) == pytest.approx(z["L0"][0], rel=1e-6)
     fimg, g = eng.vjp(desc, dl, prec)
-    assert np.abs(fimg - img).max() <= (0.0 if prec == 0 else 1e-4) * np.abs(img).max()
+    # the one pass's own image: the adjoint's sums, rounded differently (FP64)
+    assert np.abs(fimg - img).max() <= (1e-11 if prec == 0 else 1e-4) * np.abs(img).max()
     bad = Mismatches()
     bad.check("M_unit", g["d_m_unit"], z["rich_m_unit"][0])
     bad.check("R_high", g["d_r_high"], z["rich_r_high"][0])
@@ -196,7 +197,7 @@ def test_vjp_mixed(torus64, freqs):
     i32, g32 = eng.vjp(desc, dl, engine.PREC_MIXED)
     s32 = eng.stats()
     eng.close()
-    assert np.array_equal(i64, img)
+    assert np.abs(i64 - img).max() <= 1e-11 * np.abs(img).max()  # the FP64 one pass's own image
     assert np.abs(i32 - img).max() <= 1e-4 * np.abs(img).max()
     for key in ("rays", "steps", "rt_calls", "rt_samples"):
         assert s32[key] == s64[key], key
@@ -280,14 +281,14 @@ def test_vjp_log_camera_and_rk2(torus64, camera, integrator):
 def test_vjp_sample_pool_matches_in_place(torus256, camera, integrator, freqs):
     """The FP64 adjoint with the per-warp sample pool (vjp_kernel_pool; with
     several frequencies its results go through the scratch buffer) against
-    the in-place kernel (no_sample_pool): the same step, sample and term
-    counts, scalar gradients within 1e-12 and per-cell gradients within 1e-12
-    of the largest (the FP64 atomics of the per-cell scatter add in a
-    different order)."""
+    the in-place kernel (no_sample_pool), both in two passes: the same step,
+    sample and term counts, scalar gradients within 1e-12 and per-cell
+    gradients within 1e-12 of the largest (the FP64 atomics of the per-cell
+    scatter add in a different order)."""
     from raptor_gb300 import engine
     out = {}
     for nsp in (0, 1):
-        eng = engine.Engine(no_sample_pool=nsp)
+        eng = engine.Engine(no_sample_pool=nsp, vjp_tape=-1)
         gid = eng.upload_grid(torus256.geom, torus256.prims)
         mk = lambda **o: engine.image_desc(64, 64, freqs, **dict(dict(grid=gid, inclination=60.0, camera=camera, integrator=integrator), **o))  # noqa: E731
         target, _ = eng.render(mk(inclination=62.0, m_unit=1.3e19, r_high=4.0, r_low=4.0), engine.PREC_FP64)

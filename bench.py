@@ -234,9 +234,9 @@ def workload_config(n_gpus=1):
 def run_vjp_adjoint256(reps=3):
     """Adjoint configuration: 256x256 image of the 256x256 torus, loss = L2
     distance to a target at M_unit x 1.3, R = 4, i = 62 deg.  Reports, for
-    the FP64, mixed and mixed-DF forms, the forward and VJP (forward pass +
-    that form's adjoint pass) device times; the mixed and mixed-DF gradients
-    are compared with the FP64 ones."""
+    the FP64, mixed and mixed-DF forms, the forward and VJP (the
+    raptor_gpu_vjp call: that form's one-pass adjoint) device times; the
+    mixed and mixed-DF gradients are compared with the FP64 ones."""
     from raptor_gb300 import engine, synth
     d = synth.make_torus(n1=256, n2=256)
     eng = engine.Engine()
@@ -319,10 +319,12 @@ def run_differentiable(dev, n_cells=4, reps=2, incl_hs=(1e-4, 1e-6, 1e-7)):
     (with its spectrum) of the 512x512 torus, and the VJP of
     L = 1/2 |O - O_target|^2 (target at M_unit x 1.3, R = 4, i = 62 deg) with
     respect to the four scalars and the per-cell rho, u and ln Theta_e
-    fields, in each form as a forward render and that form's adjoint pass:
-    mixed (the workload's: FP64 geodesic, FP32 transfer; its adjoint keeps
-    the FP64 path with FP32 tangents and the FP32 dual sample), FP64, and
-    mixed-DF.  Reports forward, adjoint and VJP device times, the engine's
+    fields, in each form as a forward render and that form's VJP call (one
+    adjoint pass that takes each ray's I from its own sums and keeps the
+    ray's per-cell terms on a record tape): mixed (the workload's: FP64
+    geodesic, FP32 transfer; its adjoint keeps the FP64 path with FP32
+    tangents and the FP32 dual sample), FP64, and mixed-DF.  Reports
+    forward, adjoint and VJP device times, the engine's
     peak device memory, and each form's gradients against central
     differences of the FP64 forward: the four scalars (h = 1e-4 relative,
     and the inclination also at the smaller incl_hs, where the piecewise
@@ -423,6 +425,7 @@ def run_differentiable(dev, n_cells=4, reps=2, incl_hs=(1e-4, 1e-6, 1e-7)):
         "config": {"workload": "2048x2048 image at 86/140/230/345/690 GHz with spectrum, 512x512 torus a=0.9375, "
                                "i=60, M_unit=1e19, R_high=R_low=3; loss to target at M_unit*1.3, R=4, i=62",
                    "forward": "mixed", "adjoint": m["adjoint"] + " (forward-mode tangents + suffix identity, "
+                                                               "one pass with a per-lane record tape, "
                                                                "no checkpoints)"},
         "forward_ms": m["forward_ms"], "adjoint_kernel_ms": m["adjoint_kernel_ms"], "vjp_total_ms": m["vjp_total_ms"],
         "adjoint_over_forward": m["adjoint_over_forward"], "vjp_total_over_forward": m["vjp_total_over_forward"],

@@ -83,12 +83,13 @@ typedef struct raptor_gpu_options {
                             samples in place; 0 (default) = a warp evaluates them 32 at a time
                             from a shared-memory pool.  The same arithmetic per ray: the images
                             agree bit for bit or to rounding. */
-    int vjp_tape;        /* mixed and mixed-DF raptor_gpu_vjp: 0 (default) = one adjoint pass
-                            that keeps each ray's per-cell terms on a per-lane device tape of 2048
-                            records and takes the ray's I from its own sums; n > 0 = n records per
-                            lane; -1 = two passes (the forward render, then the adjoint reading
-                            each pixel's I from it).  A ray with more records than fit makes the
-                            call fall back to two passes. */
+    int vjp_tape;        /* raptor_gpu_vjp: 0 (default) = one adjoint pass that keeps each ray's
+                            per-cell terms on a per-lane device tape of 2048 records and takes
+                            the ray's I from its own sums; n > 0 = n records per lane; -1 = two
+                            passes (the forward render, then the adjoint reading each pixel's I
+                            from it).  A ray with more records than fit, or a tape that cannot
+                            be allocated, makes the call fall back to two passes; the in-place
+                            FP64 adjoint (no_sample_pool) always takes two. */
     int reserved[6];
 } raptor_gpu_options;
 
@@ -195,9 +196,9 @@ long long raptor_gpu_output_size(const raptor_image_desc *imgs, int n_imgs);
 long long raptor_gpu_spectrum_size(const raptor_image_desc *imgs, int n_imgs);
 
 /* Statistics of the last render or VJP on this context (for a VJP: the
- * adjoint pass's counters with the forward render's n_stepcap and
- * n_nonfinite; kernel_ms is the adjoint pass, device_ms forward plus
- * adjoint). */
+ * adjoint pass's counters, with n_stepcap and n_nonfinite of the image it
+ * returns; kernel_ms is the adjoint pass, device_ms all of the call's
+ * device work: the adjoint pass in one pass, forward plus adjoint in two). */
 int raptor_gpu_get_stats(const raptor_gpu_ctx *ctx, raptor_gpu_stats *out);
 
 /* Per-step record of one ray, the engine's form of the reference's GEOD
@@ -214,11 +215,17 @@ int raptor_gpu_trace_ray(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int 
 /* Vector-Jacobian product of one image: given dL_dI [W*H][n_freq] (same
  * layout and nu^3 scaling as I_out), returns dL/d(M_UNIT, R_HIGH, R_LOW,
  * INCLINATION) and, if the pointers are set, the per-cell gradients on the
- * image's grid.  precision selects the form: the forward render in that form
- * and that form's adjoint pass (FP64: FP64 tangents and dual sample; mixed:
- * the FP64 geodesic with FP32 tangents and the FP32 dual sample; mixed-DF:
- * the double-float geodesic with FP32 tangents and sample).  I_out receives
- * the forward image (may be NULL).
+ * image's grid.  precision selects the form and its adjoint pass (FP64:
+ * FP64 tangents and dual sample; mixed: the FP64 geodesic with FP32 tangents
+ * and the FP32 dual sample; mixed-DF: the double-float geodesic with FP32
+ * tangents and sample).  By default the adjoint runs in one pass, taking
+ * each ray's I from its own sums and keeping the ray's per-cell terms on a
+ * device tape until the ray ends (raptor_gpu_options.vjp_tape); I_out
+ * (may be NULL) then receives the image that pass renders, equal to
+ * raptor_gpu_render's to rounding (1e-11 of the largest pixel in FP64, 1e-5
+ * with the FP32 transfers).  In two passes (vjp_tape = -1, the in-place FP64
+ * adjoint, or a tape too small) the form's forward render runs first and
+ * I_out receives it.
  * No counterpart in the reference, which has no derivatives. */
 int raptor_gpu_vjp(raptor_gpu_ctx *ctx, const raptor_image_desc *img, int precision,
                    const double *dL_dI, double *I_out, raptor_grad *grad);

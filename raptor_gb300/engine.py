@@ -162,8 +162,8 @@ class Engine:
                  vjp_tape: int = 0):
         """checked: use the bounds-checked build of the library, where a
         failed device-side index check fails the call with RAPTOR_ERR_DEVICE.
-        vjp_tape: records per lane of the mixed and mixed-DF one-pass adjoint's
-        tape (0: 2048; -1: the two-pass VJP), raptor_gpu_options.vjp_tape."""
+        vjp_tape: records per lane of the one-pass adjoint's tape (0: 2048;
+        -1: the two-pass VJP), raptor_gpu_options.vjp_tape."""
         self.lib = load(CHECKED_LIB_PATH if checked else LIB_PATH)
         opt = Options(device, block_size, blocks_per_sm, refill_interval, autotune, use_graph, no_sample_pool,
                       vjp_tape)
@@ -244,7 +244,8 @@ class Engine:
 
     def vjp(self, img: ImageDesc, dL_dI: np.ndarray, precision=PREC_FP64, want_fields=True, ray_begin=None,
             ray_count=None):
-        """Forward image and gradients of L given dL/dI (raptor_gpu_vjp); with
+        """Image and gradients of L given dL/dI (raptor_gpu_vjp: the image the
+        one-pass adjoint renders, or the forward render in two passes); with
         ray_begin / ray_count, of those rays only (raptor_gpu_vjp_range)."""
         geom = self.grids[img.grid]
         dldi = np.ascontiguousarray(dL_dI, dtype=np.float64)

@@ -35,24 +35,30 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_struct_layouts_match_header(lib):
-    """ctypes mirrors of the ABI structs have the sizes the C compiler gives."""
+    """ctypes mirrors of the ABI structs have the sizes the C compiler gives,
+    and every field of the options struct its offset."""
     import subprocess
     import tempfile
     from raptor_gb300 import engine
+    opt_fields = [f for f, _ in engine.Options._fields_]
+    offs = "".join(f' printf("%zu\\n", offsetof(raptor_gpu_options, {f}));' for f in opt_fields)
     src = r'''
+#include <stddef.h>
 #include <stdio.h>
 #include "raptor_gpu.h"
 int main(void){printf("%zu %zu %zu %zu %zu\n", sizeof(raptor_gpu_options), sizeof(raptor_grid_geom),
- sizeof(raptor_image_desc), sizeof(raptor_gpu_stats), sizeof(raptor_grad));return 0;}
+ sizeof(raptor_image_desc), sizeof(raptor_gpu_stats), sizeof(raptor_grad));''' + offs + r'''return 0;}
 '''
     d = tempfile.mkdtemp()
     c = os.path.join(d, "s.c")
     open(c, "w").write(src)
     exe = os.path.join(d, "s")
     subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe], check=True)
-    sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    vals = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    sizes, offsets = vals[:5], vals[5:]
     assert sizes == [ctypes.sizeof(engine.Options), ctypes.sizeof(engine.GridGeomC),
                      ctypes.sizeof(engine.ImageDesc), ctypes.sizeof(engine.Stats), ctypes.sizeof(engine.GradC)]
+    assert offsets == [getattr(engine.Options, f).offset for f in opt_fields]
 
 
 def test_init_without_device_fails_cleanly(lib):

@@ -90,7 +90,7 @@ typedef struct raptor_gpu_options {
                             from it).  A ray with more records than fit, or a tape that cannot
                             be allocated, makes the call fall back to two passes; the in-place
                             FP64 adjoint (no_sample_pool) always takes two.  The tape (resident
-                            lanes x records x 48-176 bytes: up to 14 GB at five frequencies in
+                            lanes x records x 48 to 240 bytes: 14 GB at five frequencies in
                             FP64) stays allocated on the context for later calls. */
     int reserved[6];
 } raptor_gpu_options;

@@ -60,8 +60,8 @@ def merge_grads(grads: dict, group=None) -> dict:
 
 def vjp_sharded(eng, img, dL_dI, precision, rank: int, world: int, group=None):
     """This rank's share of one image's VJP (its ray range), merged over the
-    ranks: returns (the full forward image, the full gradients) on every
-    rank."""
+    ranks: returns (the full image the VJP returns, the full gradients) on
+    every rank."""
     begin, end = ray_range(img.width * img.height, world, rank)
     fimg, g = eng.vjp(img, dL_dI, precision, ray_begin=begin, ray_count=end - begin)
     return merge(fimg, group).numpy(), merge_grads(g, group)

@@ -106,9 +106,9 @@ def test_vjp_against_engine_finite_differences(torus64, emission):
 @pytest.mark.parametrize("prec", [0, 1, 2], ids=["fp64", "mixed", "mixed_df"])
 def test_vjp_against_reference_finite_differences(torus256, prec):
     """The reference rerun at perturbed parameters (the 256x256 adjoint workload), for
-    each form's VJP: its forward render and its adjoint pass (FP64; mixed:
-    FP64 geodesic with FP32 tangents and the FP32 dual sample; mixed-DF:
-    double-float geodesic, FP32 tangents and sample), all at the 1e-3 bar."""
+    each form's VJP: its one-pass adjoint (FP64; mixed: FP64 geodesic with
+    FP32 tangents and the FP32 dual sample; mixed-DF: double-float geodesic,
+    FP32 tangents and sample), all at the 1e-3 bar."""
     from raptor_gb300 import engine
     z = load_golden("vjp_fd_256.npz")
     eng = engine.Engine()
@@ -310,9 +310,8 @@ def test_vjp_sample_pool_matches_in_place(torus256, camera, integrator, freqs):
 def test_vjp_ranges_add_up(torus64, prec):
     """raptor_gpu_vjp_range: the gradients of disjoint ray ranges add up to
     the whole image's (every gradient is a sum over rays; the per-cell
-    atomics add in another order), and the partial forward images to the
-    whole forward image - the split raptor_gb300/shard.py makes across
-    processes."""
+    atomics add in another order), and the partial images to the whole
+    image - the split raptor_gb300/shard.py makes across processes."""
     from raptor_gb300 import engine
     eng = engine.Engine()
     gid = eng.upload_grid(torus64.geom, torus64.prims)

@@ -6,9 +6,10 @@ fails the call with RAPTOR_ERR_DEVICE.  The small parity cases run clean
 under it (status OK, so no check failed) in every form and through every
 kernel: the pooled and in-place FP64 kernels with one and five frequencies,
 RK2, the log-polar camera, a mixed batch, a ray range and a trace, the mixed
-and mixed-DF kernels, and the four adjoints (pooled FP64 with one and three
-frequencies, in-place FP64, mixed, mixed-DF).  The checked build's images
-and gradients equal the normal build's to rounding.
+and mixed-DF kernels, and the adjoints (pooled FP64 with one and three
+frequencies, mixed, mixed-DF, each in one pass with its record tape and in
+two passes; in-place FP64).  The checked build's images and gradients equal
+the normal build's to rounding.
 """
 import numpy as np
 import pytest
@@ -61,13 +62,14 @@ def test_checked_build_renders_clean(torus64, torus256, no_pool):
         ref.close()
 
 
+@pytest.mark.parametrize("tape", [0, -1], ids=["one_pass", "two_pass"])
 @pytest.mark.parametrize("prec,freqs", [(0, [230e9]), (0, [86e9, 230e9, 345e9]), (1, [230e9]), (2, [230e9])],
                          ids=["fp64", "fp64_3freq", "mixed", "mixed_df"])
-def test_checked_build_adjoints_clean(torus64, prec, freqs):
+def test_checked_build_adjoints_clean(torus64, prec, freqs, tape):
     from raptor_gb300 import engine
     out = {}
     for checked in (True, False):
-        eng = engine.Engine(checked=checked)
+        eng = engine.Engine(checked=checked, vjp_tape=tape)
         try:
             gid = eng.upload_grid(torus64.geom, torus64.prims)
             mk = lambda **o: engine.image_desc(32, 32, freqs, **dict(dict(grid=gid, inclination=60.0), **o))  # noqa: E731

@@ -1024,8 +1024,9 @@ static int vjp_impl(raptor_gpu_ctx* ctx, const raptor_image_desc* img, int preci
             tape.rec = ctx->d_vjp_tape;
         }
         CK(cudaEventRecord(ctx->ev0, ctx->stream));
-        vfn(grid, ctx->stream, ctx->d_imgs, cam, ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc, grho, gu, gth,
-            kVjpRefill, ctx->d_vjp_scratch, RayRange{rb, re}, tape);
+        // one pass: no forward image (the pass writes its own to tape.out)
+        vfn(grid, ctx->stream, ctx->d_imgs, cam, one_pass ? nullptr : ctx->d_out, ctx->d_dldi, ctx->d_counters, gsc,
+            grho, gu, gth, kVjpRefill, ctx->d_vjp_scratch, RayRange{rb, re}, tape);
         CK(cudaGetLastError());
         CK(cudaEventRecord(ctx->ev1, ctx->stream));
         unsigned long long ctr[kCtrCount];
